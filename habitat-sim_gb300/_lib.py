@@ -1,0 +1,135 @@
+"""ctypes bindings of libgbr.so (the C ABI declared in include/gbr.h)."""
+import ctypes
+import os
+
+from . import build as _build
+
+c_float_p = ctypes.POINTER(ctypes.c_float)
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("flags", ctypes.c_uint32), ("tile_size", ctypes.c_int32 * 2),
+                ("tile_count", ctypes.c_int32 * 2), ("max_light_count", ctypes.c_uint32),
+                ("ambient_factor", ctypes.c_float), ("cuda_device", ctypes.c_int32),
+                ("standalone_flags", ctypes.c_uint32), ("planes", ctypes.c_uint32),
+                ("draw_mode", ctypes.c_uint32), ("scene_count", ctypes.c_uint32),
+                ("viewports", ctypes.POINTER(ctypes.c_int32))]
+
+
+class MeshData(ctypes.Structure):
+    _fields_ = [("vertex_count", ctypes.c_uint32), ("positions", ctypes.c_void_p),
+                ("colors", ctypes.c_void_p), ("texcoords", ctypes.c_void_p),
+                ("object_ids", ctypes.c_void_p), ("index_count", ctypes.c_uint32),
+                ("indices", ctypes.c_void_p)]
+
+
+class TextureData(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("layers", ctypes.c_int32),
+                ("rgba8", ctypes.c_void_p), ("filter", ctypes.c_int32),
+                ("wrap_s", ctypes.c_int32), ("wrap_t", ctypes.c_int32)]
+
+
+class MaterialData(ctypes.Structure):
+    _fields_ = [("color", ctypes.c_float * 4), ("texture", ctypes.c_uint32),
+                ("layer", ctypes.c_uint32), ("matrix", ctypes.c_float * 9)]
+
+
+class MeshView(ctypes.Structure):
+    _fields_ = [("mesh", ctypes.c_uint32), ("index_offset", ctypes.c_uint32),
+                ("index_count", ctypes.c_uint32), ("material", ctypes.c_uint32),
+                ("transform", ctypes.c_float * 16)]
+
+
+class SceneStatsInfo(ctypes.Structure):
+    _fields_ = [("node_count", ctypes.c_uint64), ("draw_count", ctypes.c_uint64),
+                ("draw_batch_count", ctypes.c_uint64)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int32), ("region_width", ctypes.c_int32),
+                ("region_height", ctypes.c_int32), ("small_area", ctypes.c_int32),
+                ("ctas_per_sm", ctypes.c_int32)]
+
+
+class DrawStats(ctypes.Structure):
+    _fields_ = [("scenes", ctypes.c_uint64), ("draws", ctypes.c_uint64),
+                ("visible_draws", ctypes.c_uint64), ("triangles", ctypes.c_uint64),
+                ("kernel_launches", ctypes.c_uint64)]
+
+
+_P = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+_I32 = ctypes.c_int32
+_U64 = ctypes.c_uint64
+_ST = ctypes.c_int
+
+PROTOTYPES = {
+    "gbr_config_init": (None, [ctypes.POINTER(Config)]),
+    "gbr_create": (_ST, [ctypes.POINTER(Config), ctypes.POINTER(_P)]),
+    "gbr_destroy": (None, [_P]),
+    "gbr_last_error": (ctypes.c_char_p, []),
+    "gbr_tile_size_count": (_ST, [_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
+    "gbr_scene_count": (_ST, [_P, ctypes.POINTER(_U32)]),
+    "gbr_framebuffer_size": (_ST, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    "gbr_scene_viewport": (_ST, [_P, _U32, ctypes.POINTER(ctypes.c_int64)]),
+    "gbr_add_file": (_ST, [_P, ctypes.c_char_p, _U32, ctypes.c_char_p]),
+    "gbr_add_mesh": (_ST, [_P, ctypes.POINTER(MeshData), ctypes.POINTER(_U32)]),
+    "gbr_add_texture": (_ST, [_P, ctypes.POINTER(TextureData), ctypes.POINTER(_U32)]),
+    "gbr_add_material": (_ST, [_P, ctypes.POINTER(MaterialData), ctypes.POINTER(_U32)]),
+    "gbr_add_node_hierarchy_template": (_ST, [_P, ctypes.c_char_p, _U32, ctypes.POINTER(MeshView)]),
+    "gbr_has_node_hierarchy": (_ST, [_P, ctypes.c_char_p, ctypes.POINTER(_I32)]),
+    "gbr_add_node_hierarchy": (_ST, [_P, _U32, ctypes.c_char_p, c_float_p, ctypes.POINTER(_U64)]),
+    "gbr_add_empty_node": (_ST, [_P, _U32, ctypes.POINTER(_U64)]),
+    "gbr_clear": (_ST, [_P, _U32]),
+    "gbr_set_semantic_id": (_ST, [_P, _U32, _U64, _U32]),
+    "gbr_update_camera": (_ST, [_P, _U32, c_float_p, c_float_p]),
+    "gbr_update_cameras": (_ST, [_P, _U32, _U32, c_float_p, c_float_p]),
+    "gbr_camera": (_ST, [_P, _U32, c_float_p]),
+    "gbr_camera_depth_unprojection": (_ST, [_P, _U32, c_float_p]),
+    "gbr_transformations": (_ST, [_P, _U32, ctypes.POINTER(c_float_p), ctypes.POINTER(_U64)]),
+    "gbr_draw": (_ST, [_P, _P]),
+    "gbr_draw_mode": (_ST, [_P, _P, _U32, _I32]),
+    "gbr_scene_stats": (_ST, [_P, _U32, ctypes.POINTER(SceneStatsInfo)]),
+    "gbr_image_into": (_ST, [_P, _U32, ctypes.POINTER(_I32), _P, _U64]),
+    "gbr_color_image_into": (_ST, [_P, ctypes.POINTER(_I32), _P, _U64]),
+    "gbr_depth_image_into": (_ST, [_P, ctypes.POINTER(_I32), _P, _U64]),
+    "gbr_scene_image_into": (_ST, [_P, _U32, _U32, _P, _U64]),
+    "gbr_plane_device_pointer": (_ST, [_P, _U32, ctypes.POINTER(_P), ctypes.POINTER(_U64)]),
+    "gbr_plane_dlpack": (_ST, [_P, _U32, ctypes.POINTER(_P)]),
+    "gbr_unproject_depth": (_ST, [c_float_p, c_float_p, _U64, _U64, _U64]),
+    "gbr_unproject_depth_device": (_ST, [c_float_p, _P, _U64, _U64, _U64, _P]),
+    "gbr_get_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
+    "gbr_set_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
+    "gbr_last_draw_stats": (_ST, [_P, ctypes.POINTER(DrawStats)]),
+}
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load():
+    """Load libgbr.so (compiling it first if its sources changed)."""
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in PROTOTYPES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+class GbrError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"[gbr status {status}] {message}")
+        self.status = status
+
+
+def check(status):
+    if status != 0:
+        raise GbrError(status, load().gbr_last_error().decode(errors="replace"))

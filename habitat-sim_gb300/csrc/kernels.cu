@@ -1,0 +1,772 @@
+// sm_103a kernels of the batch renderer.
+//
+// Replaces the GPU half of esp::gfx_batch::Renderer::draw
+// (src/esp/gfx_batch/Renderer.cpp:1203-1351): the per-frame transform
+// hierarchy and per-draw uniforms (:1203-1290) become prepare_kernel; the
+// per-tile multi-draw through PhongGL and the GL fixed-function pipeline
+// (:1292-1351) become raster_kernel.
+//
+// Arithmetic: this translation unit is compiled with --fmad=false, so no
+// multiply-add is fused unless written as __fmaf_rn.  Every operation that
+// decides a pixel (transform, clip, snap, edge functions, depth, barycentric
+// interpolation, texel fetch, unorm conversion) is written out in a fixed
+// order so that the results are reproducible bit for bit on any IEEE-754
+// machine that evaluates the same sequence.
+//
+// Rasterisation method (GL leaves the exact rules to the implementation):
+//   - clip-space trivial reject; homogeneous clipping only for triangles
+//     that cross the near plane z = -w or a guard band |x|,|y| <= G*w
+//     (Sutherland & Hodgman 1974), fan re-triangulation;
+//   - window coordinates snapped to 1/256 pixel, round half to even;
+//   - integer edge functions (Pineda 1988) in 64-bit with the top-left
+//     fill rule, pixel centres at (x+0.5, y+0.5), origin bottom-left;
+//   - depth interpolated linearly in window space, LESS semantics realised
+//     as an atomic minimum of (depth bits << 32 | triangle ordinal) in a
+//     shared-memory z-buffer: the smallest depth wins, ties go to the
+//     earliest submitted triangle, as with a sequential GL depth test;
+//   - deferred shading of the winner only, with homogeneous barycentrics of
+//     the unclipped triangle (Olano & Greer 1997).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.h"
+
+namespace gbr {
+namespace {
+
+constexpr uint64_t kEmptyKey = ~0ull;
+constexpr uint32_t kBackground = 0xFF1F1F1Fu;
+constexpr int kMaxHierarchyDepth = 64;
+
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// C = A * B, column-major 4x4.
+__device__ __forceinline__ void matmul(const float* a, const float* b, float* c) {
+#pragma unroll
+  for (int col = 0; col < 4; ++col) {
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+      float t = __fmul_rn(a[row], b[col * 4 + 0]);
+      t = fma_(a[4 + row], b[col * 4 + 1], t);
+      t = fma_(a[8 + row], b[col * 4 + 2], t);
+      t = fma_(a[12 + row], b[col * 4 + 3], t);
+      c[col * 4 + row] = t;
+    }
+  }
+}
+
+__device__ __forceinline__ float mrow(const float* m, int row, float x, float y, float z) {
+  float r = m[12 + row];
+  r = fma_(m[row], x, r);
+  r = fma_(m[4 + row], y, r);
+  r = fma_(m[8 + row], z, r);
+  return r;
+}
+
+// ------------------------------------------------------------ block scan
+template <int T>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp,
+                                                         uint32_t* s_total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t n = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += n;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int kWarps = T / 32;
+    uint32_t w = lane < kWarps ? s_warp[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t n = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += n;
+    }
+    if (lane < kWarps) s_warp[lane] = wi - w;
+    if (lane == kWarps - 1) *s_total = wi;
+  }
+  __syncthreads();
+  uint32_t out = s_warp[warp] + incl - v;
+  __syncthreads();
+  return out;
+}
+
+// ================================================================ prepare
+template <int T>
+__global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
+  __shared__ uint32_t s_warp[T / 32], s_total, s_count, s_tris;
+  const uint32_t s = p.scene_base + blockIdx.x;
+  const SceneRec sc = p.scenes[s];
+  if (threadIdx.x == 0) {
+    s_count = 0;
+    s_tris = 0;
+  }
+  float pv[16], vrow[4];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) pv[i] = p.cameras[s].pv[i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) vrow[i] = p.cameras[s].vrow[i];
+  __syncthreads();
+  for (uint32_t base = 0; base < sc.draw_count; base += T) {
+    const uint32_t j = base + threadIdx.x;
+    uint32_t vis = 0, tris = 0;
+    VisibleRec rec;
+    if (j < sc.draw_count) {
+      const DrawRec d = p.draws[sc.draw_base + j];
+      // Absolute transform: abs = L_root * ... * L_node (parents precede children).
+      uint32_t chain[kMaxHierarchyDepth];
+      int depth = 0;
+      int32_t n = int32_t(d.node);
+      bool ok = n >= 0 && uint32_t(n) < sc.node_count;
+      while (ok && n >= 0 && depth < kMaxHierarchyDepth) {
+        chain[depth++] = uint32_t(n);
+        n = p.parents[sc.node_base + n];
+        if (n >= 0 && uint32_t(n) >= sc.node_count) ok = false;
+      }
+      if (!ok) atomicOr(p.status, kStatusBadNode);
+      if (ok && n >= 0) {
+        atomicOr(p.status, kStatusHierarchyTooDeep);
+        ok = false;
+      }
+      if (ok) {
+        float a[16], t[16];
+        const float* l = p.local + size_t(sc.node_base + chain[depth - 1]) * 16;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) a[i] = l[i];
+        for (int k = depth - 2; k >= 0; --k) {
+          const float* lk = p.local + size_t(sc.node_base + chain[k]) * 16;
+          float b[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) b[i] = lk[i];
+          matmul(a, b, t);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) a[i] = t[i];
+        }
+        matmul(pv, a, rec.mvp);
+#pragma unroll
+        for (int col = 0; col < 4; ++col) {
+          float z = __fmul_rn(vrow[0], a[col * 4 + 0]);
+          z = fma_(vrow[1], a[col * 4 + 1], z);
+          z = fma_(vrow[2], a[col * 4 + 2], z);
+          z = fma_(vrow[3], a[col * 4 + 3], z);
+          rec.zrow[col] = z;
+        }
+        // Frustum test of the view's bounding box: culled only when all
+        // eight corners lie beyond the same clip plane by a relative margin,
+        // so rounding can never drop a triangle that would cover a pixel.
+        uint32_t all_out = 0x3fu;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const float x = d.bbox[(c & 1) ? 3 : 0], y = d.bbox[(c & 2) ? 4 : 1],
+                      z = d.bbox[(c & 4) ? 5 : 2];
+          const float cx = mrow(rec.mvp, 0, x, y, z), cy = mrow(rec.mvp, 1, x, y, z),
+                      cz = mrow(rec.mvp, 2, x, y, z), cw = mrow(rec.mvp, 3, x, y, z);
+          const float ax = 1e-5f * (fabsf(cx) + fabsf(cw)), ay = 1e-5f * (fabsf(cy) + fabsf(cw)),
+                      az = 1e-5f * (fabsf(cz) + fabsf(cw));
+          uint32_t out = 0;
+          out |= (cx - cw > ax) ? 1u : 0u;
+          out |= (-cx - cw > ax) ? 2u : 0u;
+          out |= (cy - cw > ay) ? 4u : 0u;
+          out |= (-cy - cw > ay) ? 8u : 0u;
+          out |= (cz - cw > az) ? 16u : 0u;
+          out |= (-cz - cw > az) ? 32u : 0u;
+          all_out &= out;
+        }
+        if (all_out == 0 && d.tri_count > 0) {
+          const MeshRec m = p.meshes[d.mesh];
+          vis = 1;
+          tris = d.tri_count;
+          rec.vertex_base = m.vertex_base;
+          rec.first_index = d.first_index;
+          rec.tri_count = d.tri_count;
+          rec.material = d.material;
+          rec.semantic_id = d.semantic_id;
+          rec.flags = m.flags;
+          rec.pad = 0;
+        }
+      }
+    }
+    const uint32_t vo = block_exclusive_scan<T>(vis, s_warp, &s_total);
+    const uint32_t vtot = s_total;
+    __syncthreads();
+    const uint32_t to = block_exclusive_scan<T>(tris, s_warp, &s_total);
+    const uint32_t ttot = s_total;
+    if (vis) {
+      rec.ordinal = s_tris + to;
+      p.visible[sc.draw_base + s_count + vo] = rec;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s_count += vtot;
+      s_tris += ttot;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    p.vis_count[s] = s_count;
+    p.vis_tris[s] = s_tris;
+  }
+}
+
+// ================================================================= raster
+struct QEntry {
+  int32_t X[3], Y[3];
+  float zw0, d1, d2, inva;
+  uint32_t ordinal;
+  uint32_t bias;  // bit i: edge i owns its pixels (top-left)
+  int16_t x0, y0, x1, y1;
+};
+
+struct Setup {
+  int32_t X[3], Y[3];
+  float zw0, d1, d2, inva;
+  uint32_t bias;
+  int x0, y0, x1, y1;
+};
+
+struct Ctx {
+  uint64_t* keys;
+  QEntry* queue;
+  uint32_t* qcount;
+  int qcap;
+  int rx0, ry0, rw, rh;  // region
+  int W, H;              // viewport
+  int small_area;
+};
+
+// Project, snap, orient and bound one (sub)triangle.  False if it covers
+// no pixel centre of the region.
+__device__ __forceinline__ bool setup_sub(const float4* q, const Ctx& c, Setup& st) {
+  const float hw = __fmul_rn(0.5f, float(c.W)), hh = __fmul_rn(0.5f, float(c.H));
+  float zw[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float iw = __frcp_rn(q[i].w);
+    const float nx = __fmul_rn(q[i].x, iw), ny = __fmul_rn(q[i].y, iw),
+                nz = __fmul_rn(q[i].z, iw);
+    const float xw = fma_(nx, hw, hw), yw = fma_(ny, hh, hh);
+    zw[i] = fma_(nz, 0.5f, 0.5f);
+    st.X[i] = __float2int_rn(__fmul_rn(xw, 256.0f));
+    st.Y[i] = __float2int_rn(__fmul_rn(yw, 256.0f));
+  }
+  const int64_t area = int64_t(st.X[1] - st.X[0]) * int64_t(st.Y[2] - st.Y[0]) -
+                       int64_t(st.X[2] - st.X[0]) * int64_t(st.Y[1] - st.Y[0]);
+  if (area <= 0) return false;
+  uint32_t bias = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int a = (i + 1) % 3, b = (i + 2) % 3;
+    const int dx = st.X[b] - st.X[a], dy = st.Y[b] - st.Y[a];
+    if (dy < 0 || (dy == 0 && dx < 0)) bias |= 1u << i;
+  }
+  st.bias = bias;
+  const int minX = min(st.X[0], min(st.X[1], st.X[2])), maxX = max(st.X[0], max(st.X[1], st.X[2]));
+  const int minY = min(st.Y[0], min(st.Y[1], st.Y[2])), maxY = max(st.Y[0], max(st.Y[1], st.Y[2]));
+  st.x0 = max((minX - 128 + 255) >> 8, c.rx0);
+  st.x1 = min((maxX - 128) >> 8, c.rx0 + c.rw - 1);
+  st.y0 = max((minY - 128 + 255) >> 8, c.ry0);
+  st.y1 = min((maxY - 128) >> 8, c.ry0 + c.rh - 1);
+  if (st.x0 > st.x1 || st.y0 > st.y1) return false;
+  st.inva = __frcp_rn(__ll2float_rn(area));
+  st.zw0 = zw[0];
+  st.d1 = __fsub_rn(zw[1], zw[0]);
+  st.d2 = __fsub_rn(zw[2], zw[0]);
+  return true;
+}
+
+// Coverage and depth of pixel (px, py); false if not covered or beyond far.
+__device__ __forceinline__ bool cover(const int32_t* X, const int32_t* Y, uint32_t bias,
+                                      float zw0, float d1, float d2, float inva, int px, int py,
+                                      float& z) {
+  const int32_t Px = px * 256 + 128, Py = py * 256 + 128;
+  int64_t e[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int a = (i + 1) % 3, b = (i + 2) % 3;
+    e[i] = int64_t(X[b] - X[a]) * int64_t(Py - Y[a]) - int64_t(Y[b] - Y[a]) * int64_t(Px - X[a]);
+    if (e[i] + ((bias >> i) & 1u ? 0 : -1) < 0) return false;
+  }
+  const float b1 = __fmul_rn(__ll2float_rn(e[1]), inva), b2 = __fmul_rn(__ll2float_rn(e[2]), inva);
+  float zz = fma_(b2, d2, fma_(b1, d1, zw0));
+  if (!(zz > 0.0f)) zz = 0.0f;
+  if (!(zz < 1.0f)) return false;
+  z = zz;
+  return true;
+}
+
+__device__ __forceinline__ void depth_write(uint64_t* keys, int idx, float z, uint32_t ordinal) {
+  const uint64_t key = (uint64_t(__float_as_uint(z)) << 32) | ordinal;
+  if (key < *reinterpret_cast<volatile uint64_t*>(keys + idx))
+    atomicMin(reinterpret_cast<unsigned long long*>(keys + idx), (unsigned long long)key);
+}
+
+__device__ __forceinline__ void raster_setup(const Setup& st, uint32_t ordinal, const Ctx& c) {
+  for (int py = st.y0; py <= st.y1; ++py)
+    for (int px = st.x0; px <= st.x1; ++px) {
+      float z;
+      if (cover(st.X, st.Y, st.bias, st.zw0, st.d1, st.d2, st.inva, px, py, z))
+        depth_write(c.keys, (py - c.ry0) * c.rw + (px - c.rx0), z, ordinal);
+    }
+}
+
+__device__ __forceinline__ void emit(const float4* q, uint32_t ordinal, const Ctx& c) {
+  Setup st;
+  if (!setup_sub(q, c, st)) return;
+  const int area = (st.x1 - st.x0 + 1) * (st.y1 - st.y0 + 1);
+  if (area > c.small_area) {
+    const uint32_t slot = atomicAdd(c.qcount, 1u);
+    if (slot < uint32_t(c.qcap)) {
+      QEntry& e = c.queue[slot];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        e.X[i] = st.X[i];
+        e.Y[i] = st.Y[i];
+      }
+      e.zw0 = st.zw0;
+      e.d1 = st.d1;
+      e.d2 = st.d2;
+      e.inva = st.inva;
+      e.ordinal = ordinal;
+      e.bias = st.bias;
+      e.x0 = int16_t(st.x0);
+      e.y0 = int16_t(st.y0);
+      e.x1 = int16_t(st.x1);
+      e.y1 = int16_t(st.y1);
+      return;
+    }
+  }
+  raster_setup(st, ordinal, c);
+}
+
+__device__ __forceinline__ float plane_dist(const float4& v, int p, float gx, float gy) {
+  switch (p) {
+    case 0: return __fadd_rn(v.z, v.w);
+    case 1: return __fsub_rn(__fmul_rn(gx, v.w), v.x);
+    case 2: return __fadd_rn(__fmul_rn(gx, v.w), v.x);
+    case 3: return __fsub_rn(__fmul_rn(gy, v.w), v.y);
+    default: return __fadd_rn(__fmul_rn(gy, v.w), v.y);
+  }
+}
+
+__device__ __forceinline__ float4 lerp_clip(const float4& in, const float4& out, float din,
+                                            float dout) {
+  const float t = __fdiv_rn(din, __fsub_rn(din, dout));
+  return make_float4(fma_(t, __fsub_rn(out.x, in.x), in.x), fma_(t, __fsub_rn(out.y, in.y), in.y),
+                     fma_(t, __fsub_rn(out.z, in.z), in.z), fma_(t, __fsub_rn(out.w, in.w), in.w));
+}
+
+__device__ __noinline__ void clip_and_emit(const float4* c3, uint32_t ordinal, const Ctx& c,
+                                           float gx, float gy) {
+  float4 poly[9], next[9];
+  int n = 3;
+  for (int i = 0; i < 3; ++i) poly[i] = c3[i];
+  for (int p = 0; p < 5 && n >= 3; ++p) {
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+      const float4 a = poly[i];
+      const float4 b = poly[(i + 1) % n];
+      const float da = plane_dist(a, p, gx, gy), db = plane_dist(b, p, gx, gy);
+      const bool ina = da >= 0.0f, inb = db >= 0.0f;
+      if (ina) next[m++] = a;
+      if (ina != inb) next[m++] = ina ? lerp_clip(a, b, da, db) : lerp_clip(b, a, db, da);
+    }
+    n = m;
+    for (int i = 0; i < n; ++i) poly[i] = next[i];
+  }
+  for (int i = 1; i + 1 < n; ++i) {
+    const float4 sub[3] = {poly[0], poly[i], poly[i + 1]};
+    emit(sub, ordinal, c);
+  }
+}
+
+__device__ __forceinline__ void triangle(const float4* cv, uint32_t ordinal, const Ctx& c) {
+  // Trivial reject: all three vertices beyond one frustum plane.
+  if ((cv[0].x > cv[0].w && cv[1].x > cv[1].w && cv[2].x > cv[2].w) ||
+      (cv[0].x < -cv[0].w && cv[1].x < -cv[1].w && cv[2].x < -cv[2].w) ||
+      (cv[0].y > cv[0].w && cv[1].y > cv[1].w && cv[2].y > cv[2].w) ||
+      (cv[0].y < -cv[0].w && cv[1].y < -cv[1].w && cv[2].y < -cv[2].w) ||
+      (cv[0].z > cv[0].w && cv[1].z > cv[1].w && cv[2].z > cv[2].w) ||
+      (cv[0].z < -cv[0].w && cv[1].z < -cv[1].w && cv[2].z < -cv[2].w))
+    return;
+  const float gx = __fdiv_rn(32768.0f, float(c.W)), gy = __fdiv_rn(32768.0f, float(c.H));
+  bool need_clip = false;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int p = 0; p < 5; ++p) need_clip |= plane_dist(cv[i], p, gx, gy) < 0.0f;
+  if (!need_clip)
+    emit(cv, ordinal, c);
+  else
+    clip_and_emit(cv, ordinal, c, gx, gy);
+}
+
+// Largest d in [0, n) with ordinal(d) <= g.
+__device__ __forceinline__ uint32_t find_draw(const uint32_t* prefix, const VisibleRec* vis,
+                                              bool cached, uint32_t n, uint32_t g) {
+  uint32_t lo = 0, hi = n;  // invariant: ord(lo) <= g < ord(hi)
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint32_t o = cached ? prefix[mid] : __ldg(&vis[mid].ordinal);
+    if (o <= g)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int wrap(int i, int n, int mode) {
+  if (mode == 0) {
+    int m = i % n;
+    return m < 0 ? m + n : m;
+  }
+  if (mode == 1) return i < 0 ? 0 : (i >= n ? n - 1 : i);
+  const int p = 2 * n;
+  int m = i % p;
+  if (m < 0) m += p;
+  return m >= n ? p - 1 - m : m;
+}
+
+__device__ __forceinline__ float clampc(float f) {
+  const float lim = 16777216.0f;
+  if (!(f > -lim)) return -lim;
+  if (!(f < lim)) return lim;
+  return f;
+}
+
+__device__ __forceinline__ float chan(uint32_t t, int c) {
+  return __fdiv_rn(float((t >> (8 * c)) & 255u), 255.0f);
+}
+
+__device__ void sample(const TextureRec& t, const uint32_t* texels, int layer, float s, float u,
+                       float out[4]) {
+  const int L = layer < 0 ? 0 : (layer >= t.layers ? t.layers - 1 : layer);
+  const float fw = float(t.width), fh = float(t.height);
+  const uint32_t* base = texels + t.offset + size_t(L) * t.height * t.width;
+  if (t.filter == 0) {
+    const int x = wrap(int(floorf(clampc(__fmul_rn(s, fw)))), t.width, t.wrap_s);
+    const int y = wrap(int(floorf(clampc(__fmul_rn(u, fh)))), t.height, t.wrap_t);
+    const uint32_t v = __ldg(base + size_t(y) * t.width + x);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) out[c] = chan(v, c);
+    return;
+  }
+  const float fx = clampc(__fsub_rn(__fmul_rn(s, fw), 0.5f));
+  const float fy = clampc(__fsub_rn(__fmul_rn(u, fh), 0.5f));
+  const float flx = floorf(fx), fly = floorf(fy);
+  const float a = __fsub_rn(fx, flx), b = __fsub_rn(fy, fly);
+  const int x0 = wrap(int(flx), t.width, t.wrap_s), x1 = wrap(int(flx) + 1, t.width, t.wrap_s);
+  const int y0 = wrap(int(fly), t.height, t.wrap_t), y1 = wrap(int(fly) + 1, t.height, t.wrap_t);
+  const uint32_t v00 = __ldg(base + size_t(y0) * t.width + x0);
+  const uint32_t v10 = __ldg(base + size_t(y0) * t.width + x1);
+  const uint32_t v01 = __ldg(base + size_t(y1) * t.width + x0);
+  const uint32_t v11 = __ldg(base + size_t(y1) * t.width + x1);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float t00 = chan(v00, c), t10 = chan(v10, c), t01 = chan(v01, c), t11 = chan(v11, c);
+    const float lo = fma_(a, __fsub_rn(t10, t00), t00);
+    const float hi = fma_(a, __fsub_rn(t11, t01), t01);
+    out[c] = fma_(b, __fsub_rn(hi, lo), lo);
+  }
+}
+
+__device__ __forceinline__ uint32_t unorm8(float c) {
+  if (!(c > 0.0f)) c = 0.0f;
+  if (c > 1.0f) c = 1.0f;
+  float t = __fmul_rn(c, 255.0f);
+  t = __fadd_rn(t, 0.5f);
+  return __float2uint_rz(t);
+}
+
+// Shade the winning triangle `t` of visible draw `rec` at pixel (px, py).
+__device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec, uint32_t t,
+                      int px, int py, uint32_t& color, float& lin, uint32_t& sid) {
+  float mvp[16], zr[4];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) mvp[i] = __ldg(&rec->mvp[i]);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) zr[i] = __ldg(&rec->zrow[i]);
+  const uint32_t flags = __ldg(&rec->flags);
+  const uint32_t vb = __ldg(&rec->vertex_base);
+  const uint32_t fi = __ldg(&rec->first_index) + 3u * t;
+  uint32_t v[3];
+  float4 c[3];
+  float d[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    v[k] = vb + __ldg(&p.indices[fi + k]);
+    const float4 q = __ldg(&p.pos[v[k]]);
+    c[k] = make_float4(mrow(mvp, 0, q.x, q.y, q.z), mrow(mvp, 1, q.x, q.y, q.z),
+                       mrow(mvp, 2, q.x, q.y, q.z), mrow(mvp, 3, q.x, q.y, q.z));
+    float ze = zr[3];
+    ze = fma_(zr[0], q.x, ze);
+    ze = fma_(zr[1], q.y, ze);
+    ze = fma_(zr[2], q.z, ze);
+    d[k] = -ze;
+  }
+  const float sx = __fdiv_rn(float(2 * px + 1 - W), float(W));
+  const float sy = __fdiv_rn(float(2 * py + 1 - H), float(H));
+  float l[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float4 a = c[(i + 1) % 3];
+    const float4 b = c[(i + 2) % 3];
+    const float ex = __fsub_rn(__fmul_rn(a.y, b.w), __fmul_rn(a.w, b.y));
+    const float ey = __fsub_rn(__fmul_rn(a.w, b.x), __fmul_rn(a.x, b.w));
+    const float ez = __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x));
+    l[i] = fma_(ex, sx, fma_(ey, sy, ez));
+  }
+  const float s = __fadd_rn(__fadd_rn(l[0], l[1]), l[2]);
+  const float inv = __frcp_rn(s);
+  const float b0 = __fmul_rn(l[0], inv), b1 = __fmul_rn(l[1], inv), b2 = __fmul_rn(l[2], inv);
+#define GBR_INTERP(a0, a1, a2) fma_(b2, (a2), fma_(b1, (a1), __fmul_rn(b0, (a0))))
+  lin = GBR_INTERP(d[0], d[1], d[2]);
+  float vc[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  if (flags & kMeshVertexColor) {
+    const float4 c0 = __ldg(&p.color[v[0]]), c1 = __ldg(&p.color[v[1]]),
+                 c2 = __ldg(&p.color[v[2]]);
+    vc[0] = GBR_INTERP(c0.x, c1.x, c2.x);
+    vc[1] = GBR_INTERP(c0.y, c1.y, c2.y);
+    vc[2] = GBR_INTERP(c0.z, c1.z, c2.z);
+    vc[3] = GBR_INTERP(c0.w, c1.w, c2.w);
+  }
+  const uint32_t mi = __ldg(&rec->material);
+  const MaterialRec& mat = p.materials[mi];
+  float tc[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  const int tex = mat.texture;
+  if (!(p.flags & 1u) && tex > 0 && tex < p.texture_count) {
+    float u = 0.0f, w = 0.0f;
+    if (flags & kMeshTexcoords) {
+      const float2 t0 = __ldg(&p.uv[v[0]]), t1 = __ldg(&p.uv[v[1]]), t2 = __ldg(&p.uv[v[2]]);
+      u = GBR_INTERP(t0.x, t1.x, t2.x);
+      w = GBR_INTERP(t0.y, t1.y, t2.y);
+    }
+    float ts = mat.m[6];
+    ts = fma_(mat.m[0], u, ts);
+    ts = fma_(mat.m[3], w, ts);
+    float tt = mat.m[7];
+    tt = fma_(mat.m[1], u, tt);
+    tt = fma_(mat.m[4], w, tt);
+    sample(p.textures[tex], p.texels, mat.layer, ts, tt, tc);
+  }
+#undef GBR_INTERP
+  uint32_t packed = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float val = __fmul_rn(__fmul_rn(mat.color[k], tc[k]), vc[k]);
+    packed |= unorm8(val) << (8 * k);
+  }
+  color = packed;
+  sid = (flags & kMeshObjectId) ? __float_as_uint(__ldg(&p.pos[v[2]]).w) : __ldg(&rec->semantic_id);
+}
+
+template <int T>
+__global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t* keys = reinterpret_cast<uint64_t*>(smem);
+  QEntry* queue = reinterpret_cast<QEntry*>(keys + p.region_px);
+  uint32_t* qoff = reinterpret_cast<uint32_t*>(queue + T);
+  uint32_t* prefix = qoff + (T + 1);
+  __shared__ uint32_t s_item, s_qcount, s_total;
+  __shared__ uint32_t s_warp[T / 32];
+
+  for (uint32_t iter = 0;; ++iter) {
+    __syncthreads();
+    if (threadIdx.x == 0)
+      s_item = p.persistent ? atomicAdd(p.counter, 1u) : (iter == 0 ? blockIdx.x : p.item_count);
+    __syncthreads();
+    const uint32_t item = s_item;
+    if (item >= p.item_count) return;
+    const WorkItem wi = p.items[p.item_base + item];
+    const SceneRec sc = p.scenes[wi.scene];
+    Ctx c;
+    c.keys = keys;
+    c.queue = queue;
+    c.qcount = &s_qcount;
+    c.qcap = T;
+    c.rx0 = wi.x0;
+    c.ry0 = wi.y0;
+    c.rw = wi.w;
+    c.rh = wi.h;
+    c.W = sc.width;
+    c.H = sc.height;
+    c.small_area = p.small_area;
+    const int npx = c.rw * c.rh;
+    for (int i = threadIdx.x; i < npx; i += T) keys[i] = kEmptyKey;
+    const uint32_t nvis = p.vis_count[wi.scene];
+    const uint32_t total = p.vis_tris[wi.scene];
+    const VisibleRec* vis = p.visible + sc.draw_base;
+    const bool cached = nvis <= uint32_t(p.prefix_cap);
+    if (cached)
+      for (uint32_t i = threadIdx.x; i < nvis; i += T) prefix[i] = vis[i].ordinal;
+    if (threadIdx.x == 0) s_qcount = 0;
+    __syncthreads();
+
+    for (uint32_t base = 0; base < total; base += T) {
+      const uint32_t g = base + threadIdx.x;
+      if (g < total) {
+        const uint32_t di = find_draw(prefix, vis, cached, nvis, g);
+        const VisibleRec* rec = vis + di;
+        const uint32_t t = g - __ldg(&rec->ordinal);
+        float mvp[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) mvp[i] = __ldg(&rec->mvp[i]);
+        const uint32_t vb = __ldg(&rec->vertex_base);
+        const uint32_t fi = __ldg(&rec->first_index) + 3u * t;
+        float4 cv[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float4 q = __ldg(&p.pos[vb + __ldg(&p.indices[fi + k])]);
+          cv[k] = make_float4(mrow(mvp, 0, q.x, q.y, q.z), mrow(mvp, 1, q.x, q.y, q.z),
+                              mrow(mvp, 2, q.x, q.y, q.z), mrow(mvp, 3, q.x, q.y, q.z));
+        }
+        triangle(cv, g, c);
+      }
+      __syncthreads();
+      const uint32_t nq = min(s_qcount, uint32_t(T));
+      __syncthreads();
+      if (nq > 0) {
+        if (threadIdx.x == 0) s_qcount = 0;
+        uint32_t area = 0;
+        if (threadIdx.x < nq) {
+          const QEntry& e = queue[threadIdx.x];
+          area = uint32_t(e.x1 - e.x0 + 1) * uint32_t(e.y1 - e.y0 + 1);
+        }
+        const uint32_t off = block_exclusive_scan<T>(area, s_warp, &s_total);
+        const uint32_t tot = s_total;
+        if (threadIdx.x < nq) qoff[threadIdx.x] = off;
+        __syncthreads();
+        for (uint32_t q = threadIdx.x; q < tot; q += T) {
+          uint32_t lo = 0, hi = nq;
+          while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (qoff[mid] <= q)
+              lo = mid;
+            else
+              hi = mid;
+          }
+          const QEntry& e = queue[lo];
+          const int w = e.x1 - e.x0 + 1;
+          const int local = int(q - qoff[lo]);
+          const int px = e.x0 + local % w, py = e.y0 + local / w;
+          float z;
+          if (cover(e.X, e.Y, e.bias, e.zw0, e.d1, e.d2, e.inva, px, py, z))
+            depth_write(keys, (py - c.ry0) * c.rw + (px - c.rx0), z, e.ordinal);
+        }
+        __syncthreads();
+      }
+    }
+    __syncthreads();
+
+    // Resolve + shade + write the planes.
+    for (int i = threadIdx.x; i < npx; i += T) {
+      const int px = c.rx0 + i % c.rw, py = c.ry0 + i / c.rw;
+      const uint64_t key = keys[i];
+      const int64_t o = sc.fb_offset + int64_t(py) * sc.pitch + px;
+      uint32_t col = kBackground, sid = 0;
+      float dep = 1.0f, lin = 0.0f;
+      if (key != kEmptyKey) {
+        const uint32_t ord = uint32_t(key);
+        dep = __uint_as_float(uint32_t(key >> 32));
+        const uint32_t di = find_draw(prefix, vis, cached, nvis, ord);
+        shade(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, col, lin, sid);
+      }
+      if (p.out.color) p.out.color[o] = col;
+      if (p.out.depth) p.out.depth[o] = dep;
+      if (p.out.linear) p.out.linear[o] = lin;
+      if (p.out.semantic) p.out.semantic[o] = sid;
+    }
+  }
+}
+
+__global__ void unproject_kernel(float a, float b, float* depth, uint64_t rows, uint64_t cols,
+                                 uint64_t stride) {
+  const float far_depth = __fdiv_rn(b, __fadd_rn(1.0f, a));
+  const uint64_t n = rows * cols;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    float& d = depth[(i / cols) * stride + (i % cols)];
+    const float v = __fdiv_rn(b, __fadd_rn(d, a));
+    d = v == far_depth ? 0.0f : v;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStream_t stream) {
+  if (scene_count == 0) return cudaSuccess;
+  prepare_kernel<128><<<scene_count, 128, 0, stream>>>(p);
+  return cudaGetLastError();
+}
+
+size_t raster_smem_bytes(int threads, int region_px, int prefix_cap) {
+  size_t b = size_t(region_px) * 8 + size_t(threads) * sizeof(QEntry) +
+             size_t(threads + 1) * 4 + size_t(prefix_cap + 1) * 4;
+  return (b + 15) & ~size_t(15);
+}
+
+#define GBR_RASTER_SWITCH(threads, F) \
+  switch (threads) {                  \
+    case 256: F(256); break;          \
+    case 512: F(512); break;          \
+    case 1024: F(1024); break;        \
+    default: return cudaErrorInvalidValue; \
+  }
+
+cudaError_t raster_configure(int threads, size_t* max_dynamic) {
+  int optin = 0, dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+#define GBR_CFG(T)                                                                            \
+  {                                                                                           \
+    cudaFuncAttributes fa;                                                                    \
+    e = cudaFuncGetAttributes(&fa, raster_kernel<T>);                                         \
+    if (e != cudaSuccess) return e;                                                           \
+    const size_t dyn = size_t(optin) > fa.sharedSizeBytes ? size_t(optin) - fa.sharedSizeBytes : 0; \
+    e = cudaFuncSetAttribute(raster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                             int(dyn));                                                       \
+    if (e != cudaSuccess) return e;                                                           \
+    *max_dynamic = dyn;                                                                       \
+  }
+  GBR_RASTER_SWITCH(threads, GBR_CFG)
+#undef GBR_CFG
+  return cudaSuccess;
+}
+
+cudaError_t raster_max_ctas_per_sm(int threads, size_t smem, int* out) {
+#define GBR_OCC(T)                                                                         \
+  {                                                                                        \
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, raster_kernel<T>, T, smem); \
+    if (e != cudaSuccess) return e;                                                        \
+  }
+  GBR_RASTER_SWITCH(threads, GBR_OCC)
+#undef GBR_OCC
+  return cudaSuccess;
+}
+
+cudaError_t launch_raster(const RasterParams& p, int threads, uint32_t grid, size_t smem,
+                          cudaStream_t stream) {
+  if (grid == 0) return cudaSuccess;
+#define GBR_LAUNCH(T) raster_kernel<T><<<grid, T, smem, stream>>>(p);
+  GBR_RASTER_SWITCH(threads, GBR_LAUNCH)
+#undef GBR_LAUNCH
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unproject(float a, float b, float* depth, uint64_t rows, uint64_t cols,
+                             uint64_t row_stride, cudaStream_t stream) {
+  const uint64_t n = rows * cols;
+  if (n == 0) return cudaSuccess;
+  uint64_t blocks = (n + 255) / 256;
+  if (blocks > 65535) blocks = 65535;
+  unproject_kernel<<<unsigned(blocks), 256, 0, stream>>>(a, b, depth, rows, cols, row_stride);
+  return cudaGetLastError();
+}
+
+}  // namespace gbr

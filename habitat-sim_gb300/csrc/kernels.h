@@ -1,0 +1,74 @@
+// Launch interface of the batch renderer's sm_103a kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "records.h"
+
+namespace gbr {
+
+struct Planes {
+  uint32_t* color;
+  float* depth;
+  float* linear;
+  uint32_t* semantic;
+};
+
+// Prepare: per scene, absolute node transforms, per-draw MVP and view-z row,
+// frustum culling of each draw's bounding box, compaction of the visible
+// draws with the running triangle ordinal.  One CTA per scene.
+struct PrepareParams {
+  const SceneRec* scenes;
+  const CameraRec* cameras;
+  const DrawRec* draws;
+  const int32_t* parents;
+  const float* local;
+  const MeshRec* meshes;
+  VisibleRec* visible;
+  uint32_t* vis_count;
+  uint32_t* vis_tris;
+  uint32_t* status;
+  uint32_t scene_base;
+};
+
+// Raster: per work item (scene, region), triangle setup + clipping +
+// shared-memory (depth, ordinal) z-buffer + deferred shading + plane writes.
+struct RasterParams {
+  const SceneRec* scenes;
+  const VisibleRec* visible;
+  const uint32_t* vis_count;
+  const uint32_t* vis_tris;
+  const float4* pos;
+  const float4* color;
+  const float2* uv;
+  const uint32_t* indices;
+  const MaterialRec* materials;
+  const TextureRec* textures;
+  const uint32_t* texels;
+  int32_t texture_count;
+  uint32_t flags;  // 1 = no textures
+  const WorkItem* items;
+  uint32_t item_base;
+  uint32_t item_count;
+  uint32_t* counter;  // persistent mode: next item
+  int32_t persistent;
+  Planes out;
+  int32_t region_px;   // capacity of the shared z-buffer, pixels
+  int32_t prefix_cap;  // visible draws whose ordinals are cached in shared memory
+  int32_t small_area;
+};
+
+cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStream_t stream);
+size_t raster_smem_bytes(int threads, int region_px, int prefix_cap);
+// Raises the kernel's dynamic shared-memory limit to the device maximum and
+// returns that maximum.
+cudaError_t raster_configure(int threads, size_t* max_dynamic);
+cudaError_t launch_raster(const RasterParams& p, int threads, uint32_t grid, size_t smem,
+                          cudaStream_t stream);
+cudaError_t raster_max_ctas_per_sm(int threads, size_t smem, int* out);
+cudaError_t launch_unproject(float a, float b, float* depth, uint64_t rows, uint64_t cols,
+                             uint64_t row_stride, cudaStream_t stream);
+
+}  // namespace gbr

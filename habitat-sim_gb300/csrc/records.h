@@ -1,0 +1,95 @@
+// Device-resident records shared by the host runtime and the kernels.
+//
+// HBM layout (all arrays renderer-owned, 256-byte aligned allocations):
+//   geometry   pos[v]    float4 (x, y, z, object-id bits)   16 B / vertex
+//              color[v]  float4 RGBA                        16 B / vertex
+//              uv[v]     float2                              8 B / vertex
+//              index[i]  uint32                              4 B / index
+//   textures   texel[t]  uint32 RGBA8, layer-major, row 0 bottom
+//   tables     MeshRec, MaterialRec, TextureRec
+//   scenes     SceneRec[s]; per node parent (int32) + local 4x4 (64 B);
+//              DrawRec[] in draw-batch order; CameraRec[s] (80 B)
+//   per step   VisibleRec[] (128 B, written by the prepare kernel),
+//              vis_count[s], vis_tris[s]; WorkItem[] + one counter
+//   output     colour u32, window depth f32, linear depth f32, id u32
+//              planes, one element per framebuffer pixel.
+#pragma once
+#include <cstdint>
+
+namespace gbr {
+
+enum : uint32_t { kMeshVertexColor = 1u, kMeshObjectId = 2u, kMeshTexcoords = 4u };
+
+struct MeshRec {
+  uint32_t vertex_base;
+  uint32_t vertex_count;
+  uint32_t index_base;
+  uint32_t index_count;
+  uint32_t flags;
+  uint32_t pad[3];
+};
+
+struct MaterialRec {
+  float color[4];
+  int32_t texture;  // 0 = white
+  int32_t layer;
+  float m[9];       // 3x3 column-major texture matrix
+  int32_t pad;
+};
+
+struct TextureRec {
+  uint64_t offset;  // in texels
+  int32_t width, height, layers;
+  int32_t filter;   // 0 nearest, 1 linear
+  int32_t wrap_s, wrap_t;
+};
+
+struct SceneRec {
+  int32_t width, height;
+  int64_t fb_offset;   // pixel index of (0,0) in each plane
+  int64_t pitch;       // pixels per row
+  uint32_t node_base, node_count;
+  uint32_t draw_base, draw_count;
+};
+
+struct DrawRec {
+  uint32_t node;         // scene-local node index
+  uint32_t mesh;
+  uint32_t first_index;  // absolute index into the index array
+  uint32_t tri_count;
+  uint32_t material;
+  uint32_t semantic_id;
+  float bbox[6];         // object-space min xyz, max xyz of the view
+};
+
+struct CameraRec {
+  float pv[16];     // projection * view
+  float vrow[4];    // row 2 of the view matrix
+};
+
+struct VisibleRec {
+  float mvp[16];
+  float zrow[4];       // row 2 of view * model
+  uint32_t vertex_base;
+  uint32_t first_index;
+  uint32_t tri_count;
+  uint32_t material;
+  uint32_t semantic_id;
+  uint32_t ordinal;    // index of this draw's first triangle in the scene
+  uint32_t flags;      // mesh flags
+  uint32_t pad;
+};
+static_assert(sizeof(VisibleRec) == 112, "VisibleRec layout");
+
+struct WorkItem {
+  uint32_t scene;
+  uint16_t x0, y0, w, h;   // region of the scene's viewport
+};
+
+// Device status bits (atomicOr into one word).
+enum : uint32_t {
+  kStatusHierarchyTooDeep = 1u,
+  kStatusBadNode = 2u,
+};
+
+}  // namespace gbr

@@ -1,0 +1,1042 @@
+// Host runtime of the GB300 batch renderer.
+//
+// Scene bookkeeping follows esp::gfx_batch::Renderer
+// (src/esp/gfx_batch/Renderer.cpp): reserved white texture and material
+// (:287-304), file import offsets (:410-415), addNodeHierarchy's root node
+// plus one child per mesh view with bake * view transform and draw-batch ids
+// keyed by (vertex-colour flag, mesh, texture) (:880-961, :136-152), the
+// stable counting sort of draws by batch (:1139-1196), camera P*V and depth
+// unprojection (:1077-1088).  What the reference does on the CPU every frame
+// -- the transform hierarchy and per-draw uniform gathering (:1203-1290) --
+// and everything it asks of GL runs on the device (kernels.cu).
+#include "renderer.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+
+#include "importer.h"
+
+namespace gbr {
+
+namespace {
+thread_local std::string g_last_error;
+
+constexpr size_t kCameraBytes = sizeof(CameraRec);
+constexpr int kPrefixCapMax = 4096;
+
+const float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+
+size_t plane_elem(uint32_t plane) { return 4; }
+
+int plane_slot(uint32_t plane) {
+  switch (plane) {
+    case GBR_PLANE_COLOR: return 0;
+    case GBR_PLANE_DEPTH: return 1;
+    case GBR_PLANE_LINEAR_DEPTH: return 2;
+    case GBR_PLANE_SEMANTIC: return 3;
+    default: return -1;
+  }
+}
+}  // namespace
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error_cstr() { return g_last_error.c_str(); }
+
+// ------------------------------------------------------------- buffers
+DeviceBuffer::~DeviceBuffer() {
+  if (ptr) cudaFree(ptr);
+}
+
+bool DeviceBuffer::reserve(size_t n, bool keep, cudaStream_t stream) {
+  if (n <= bytes) return true;
+  size_t cap = std::max(n, bytes + bytes / 2);
+  cap = (cap + 255) & ~size_t(255);
+  void* p = nullptr;
+  if (cudaMalloc(&p, cap) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (keep && ptr && bytes) {
+    if (cudaMemcpy(p, ptr, bytes, cudaMemcpyDeviceToDevice) != cudaSuccess) {
+      cudaFree(p);
+      return false;
+    }
+  }
+  if (ptr) cudaFree(ptr);
+  ptr = p;
+  bytes = cap;
+  return true;
+}
+
+PinnedBuffer::~PinnedBuffer() {
+  if (ptr) cudaFreeHost(ptr);
+}
+
+bool PinnedBuffer::reserve(size_t n) {
+  if (n <= bytes) return true;
+  size_t cap = std::max(n, bytes * 2);
+  void* p = nullptr;
+  if (cudaMallocHost(&p, cap) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (ptr) cudaFreeHost(ptr);
+  ptr = p;
+  bytes = cap;
+  return true;
+}
+
+// -------------------------------------------------------------- errors
+gbr_status Renderer::fail(gbr_status s, const std::string& msg) {
+  set_last_error(msg);
+  return s;
+}
+
+gbr_status Renderer::cuda_fail(cudaError_t e, const char* what) {
+  set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? GBR_ERROR_OUT_OF_MEMORY : GBR_ERROR_CUDA;
+}
+
+gbr_status Renderer::check_scene(uint32_t scene, const char* fn) const {
+  if (scene >= scenes_.size()) {
+    set_last_error(std::string(fn) + ": index " + std::to_string(scene) + " out of range for " +
+                   std::to_string(scenes_.size()) + " scenes");
+    return GBR_ERROR_INVALID_ARGUMENT;
+  }
+  return GBR_OK;
+}
+
+#define GBR_CUDA(call, what)                         \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+// -------------------------------------------------------------- create
+Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
+  if (cfg.max_light_count != 0) {
+    err = "max_light_count > 0 (Phong lighting) is not supported; flat shading only";
+    return nullptr;
+  }
+  if (cfg.scene_count == 0 &&
+      (cfg.tile_size[0] <= 0 || cfg.tile_size[1] <= 0 || cfg.tile_count[0] <= 0 ||
+       cfg.tile_count[1] <= 0)) {
+    err = "tile size and count must be positive";
+    return nullptr;
+  }
+  if (cfg.scene_count > 0 && !cfg.viewports) {
+    err = "scene_count > 0 needs viewports";
+    return nullptr;
+  }
+  std::unique_ptr<Renderer> r(new Renderer());
+  r->cfg_ = cfg;
+  if (r->cfg_.planes == 0) r->cfg_.planes = GBR_PLANE_ALL;
+  r->device_ = cfg.cuda_device;
+  cudaError_t e = cudaSetDevice(r->device_);
+  if (e != cudaSuccess) {
+    err = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    return nullptr;
+  }
+  cudaDeviceGetAttribute(&r->sm_count_, cudaDevAttrMultiProcessorCount, r->device_);
+  uint32_t n;
+  if (cfg.scene_count > 0) {
+    r->ragged_ = true;
+    n = cfg.scene_count;
+    r->viewports_.assign(cfg.viewports, cfg.viewports + 2 * n);
+    r->cfg_.viewports = nullptr;
+    r->scenes_.resize(n);
+    int64_t off = 0;
+    for (uint32_t s = 0; s < n; ++s) {
+      const int32_t w = r->viewports_[2 * s], h = r->viewports_[2 * s + 1];
+      if (w <= 0 || h <= 0 || w > 16384 || h > 16384) {
+        err = "viewport sizes must be in [1, 16384]";
+        return nullptr;
+      }
+      SceneState& sc = r->scenes_[s];
+      sc.width = w;
+      sc.height = h;
+      sc.fb_offset = off;
+      sc.pitch = w;
+      off += int64_t(w) * h;
+    }
+    r->fb_w_ = off;
+    r->fb_h_ = 1;
+    r->fb_px_ = off;
+  } else {
+    const int tw = cfg.tile_size[0], th = cfg.tile_size[1];
+    if (tw > 16384 || th > 16384) {
+      err = "tile sizes must be at most 16384";
+      return nullptr;
+    }
+    n = uint32_t(cfg.tile_count[0]) * uint32_t(cfg.tile_count[1]);
+    r->scenes_.resize(n);
+    r->fb_w_ = int64_t(tw) * cfg.tile_count[0];
+    r->fb_h_ = int64_t(th) * cfg.tile_count[1];
+    r->fb_px_ = r->fb_w_ * r->fb_h_;
+    for (uint32_t s = 0; s < n; ++s) {
+      SceneState& sc = r->scenes_[s];
+      const int x = int(s % uint32_t(cfg.tile_count[0])), y = int(s / uint32_t(cfg.tile_count[0]));
+      sc.width = tw;
+      sc.height = th;
+      sc.pitch = r->fb_w_;
+      sc.fb_offset = int64_t(y) * th * r->fb_w_ + int64_t(x) * tw;
+    }
+  }
+  for (auto& sc : r->scenes_) {
+    std::memcpy(sc.pv, kIdentity, 64);
+    std::memcpy(sc.view, kIdentity, 64);
+  }
+  for (int i = 0; i < 4; ++i)
+    if (r->cfg_.planes & (1u << i))
+      if (!r->d_planes_[i].reserve(size_t(r->fb_px_) * 4, false)) {
+        err = "out of device memory for the framebuffer";
+        return nullptr;
+      }
+  if (cudaEventCreateWithFlags(&r->upload_done_, cudaEventDisableTiming) != cudaSuccess) {
+    err = "cudaEventCreate failed";
+    return nullptr;
+  }
+  // A blocking stream (ordered with the legacy default stream) for graph
+  // capture when the caller passes the default stream, which cannot be captured.
+  if (cudaStreamCreate(&r->own_stream_) != cudaSuccess) {
+    err = "cudaStreamCreate failed";
+    return nullptr;
+  }
+  // Texture 0: one white texel; material 0: white, untextured
+  // (Renderer.cpp:287-304).
+  const uint8_t white[4] = {255, 255, 255, 255};
+  gbr_texture_data wt{1, 1, 1, white, 0, 0, 0};
+  uint32_t id;
+  if (r->add_texture(wt, &id) != GBR_OK) {
+    err = g_last_error;
+    return nullptr;
+  }
+  gbr_material_data wm{{1, 1, 1, 1}, 0, 0, {1, 0, 0, 0, 1, 0, 0, 0, 1}};
+  r->add_material(wm, &id);
+  return r.release();
+}
+
+Renderer::~Renderer() {
+  cudaSetDevice(device_);
+  if (last_stream_ || upload_pending_) cudaDeviceSynchronize();
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  if (upload_done_) cudaEventDestroy(upload_done_);
+  if (own_stream_) cudaStreamDestroy(own_stream_);
+}
+
+// ----------------------------------------------------------- resources
+gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
+  if (!m.positions || (m.index_count && !m.indices))
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: positions and indices are required");
+  if (uint64_t(vertex_count_) + m.vertex_count > 0xffffffffull ||
+      uint64_t(index_count_) + m.index_count > 0xffffffffull)
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: more than 2^32 vertices or indices");
+  for (uint32_t i = 0; i < m.index_count; ++i)
+    if (m.indices[i] >= m.vertex_count)
+      return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: index " + std::to_string(i) +
+                                                  " out of range for " +
+                                                  std::to_string(m.vertex_count) + " vertices");
+  cudaSetDevice(device_);
+  const size_t nv = m.vertex_count, vb = vertex_count_;
+  if (!d_pos_.reserve((vb + nv) * 16, true) || !d_color_.reserve((vb + nv) * 16, true) ||
+      !d_uv_.reserve((vb + nv) * 8, true) ||
+      !d_indices_.reserve((size_t(index_count_) + m.index_count) * 4, true))
+    return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of device memory");
+  std::vector<float> pos(nv * 4), col(nv * 4), uv(nv * 2, 0.0f);
+  for (size_t v = 0; v < nv; ++v) {
+    pos[v * 4 + 0] = m.positions[v * 3 + 0];
+    pos[v * 4 + 1] = m.positions[v * 3 + 1];
+    pos[v * 4 + 2] = m.positions[v * 3 + 2];
+    uint32_t oid = m.object_ids ? m.object_ids[v] : 0u;
+    std::memcpy(&pos[v * 4 + 3], &oid, 4);
+    for (int c = 0; c < 4; ++c) col[v * 4 + c] = m.colors ? m.colors[v * 4 + c] : 1.0f;
+    if (m.texcoords) {
+      uv[v * 2] = m.texcoords[v * 2];
+      uv[v * 2 + 1] = m.texcoords[v * 2 + 1];
+    }
+  }
+  GBR_CUDA(cudaMemcpy(d_pos_.as<char>() + vb * 16, pos.data(), nv * 16, cudaMemcpyHostToDevice),
+           "addMesh upload");
+  GBR_CUDA(cudaMemcpy(d_color_.as<char>() + vb * 16, col.data(), nv * 16, cudaMemcpyHostToDevice),
+           "addMesh upload");
+  GBR_CUDA(cudaMemcpy(d_uv_.as<char>() + vb * 8, uv.data(), nv * 8, cudaMemcpyHostToDevice),
+           "addMesh upload");
+  if (m.index_count)
+    GBR_CUDA(cudaMemcpy(d_indices_.as<char>() + size_t(index_count_) * 4, m.indices,
+                        size_t(m.index_count) * 4, cudaMemcpyHostToDevice),
+             "addMesh upload");
+  MeshRec rec{};
+  rec.vertex_base = vertex_count_;
+  rec.vertex_count = m.vertex_count;
+  rec.index_base = index_count_;
+  rec.index_count = m.index_count;
+  rec.flags = (m.colors ? kMeshVertexColor : 0u) | (m.object_ids ? kMeshObjectId : 0u) |
+              (m.texcoords ? kMeshTexcoords : 0u);
+  meshes_.push_back(rec);
+  host_pos_.insert(host_pos_.end(), m.positions, m.positions + nv * 3);
+  host_indices_.insert(host_indices_.end(), m.indices, m.indices + m.index_count);
+  vertex_count_ += m.vertex_count;
+  index_count_ += m.index_count;
+  tables_dirty_ = true;
+  graph_valid_ = false;
+  *id = uint32_t(meshes_.size() - 1);
+  return GBR_OK;
+}
+
+gbr_status Renderer::add_texture(const gbr_texture_data& t, uint32_t* id) {
+  if (t.width <= 0 || t.height <= 0 || t.layers <= 0 || !t.rgba8)
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "addTexture: empty texture");
+  if (t.filter < 0 || t.filter > 1 || t.wrap_s < 0 || t.wrap_s > 2 || t.wrap_t < 0 || t.wrap_t > 2)
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "addTexture: bad filter or wrap mode");
+  cudaSetDevice(device_);
+  const size_t n = size_t(t.width) * t.height * t.layers;
+  if (!d_texels_.reserve((texel_count_ + n) * 4, true))
+    return fail(GBR_ERROR_OUT_OF_MEMORY, "addTexture: out of device memory");
+  GBR_CUDA(cudaMemcpy(d_texels_.as<char>() + texel_count_ * 4, t.rgba8, n * 4,
+                      cudaMemcpyHostToDevice),
+           "addTexture upload");
+  TextureRec rec{};
+  rec.offset = texel_count_;
+  rec.width = t.width;
+  rec.height = t.height;
+  rec.layers = t.layers;
+  rec.filter = t.filter;
+  rec.wrap_s = t.wrap_s;
+  rec.wrap_t = t.wrap_t;
+  textures_.push_back(rec);
+  texel_count_ += n;
+  tables_dirty_ = true;
+  graph_valid_ = false;
+  *id = uint32_t(textures_.size() - 1);
+  return GBR_OK;
+}
+
+gbr_status Renderer::add_material(const gbr_material_data& m, uint32_t* id) {
+  MaterialRec rec{};
+  std::memcpy(rec.color, m.color, 16);
+  rec.texture = int32_t(m.texture);
+  rec.layer = int32_t(m.layer);
+  std::memcpy(rec.m, m.matrix, 36);
+  materials_.push_back(rec);
+  tables_dirty_ = true;
+  graph_valid_ = false;
+  *id = uint32_t(materials_.size() - 1);
+  return GBR_OK;
+}
+
+gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_mesh_view* views) {
+  if (!name) return fail(GBR_ERROR_INVALID_ARGUMENT, "addNodeHierarchyTemplate: null name");
+  if (names_.count(name))
+    return fail(GBR_ERROR_INVALID_ARGUMENT,
+                std::string("addNodeHierarchyTemplate: node name ") + name + " already exists");
+  const uint32_t begin = uint32_t(views_.size());
+  for (uint32_t i = 0; i < count; ++i) {
+    const gbr_mesh_view& v = views[i];
+    if (v.mesh >= meshes_.size() || v.material >= materials_.size())
+      return fail(GBR_ERROR_INVALID_ARGUMENT, "addNodeHierarchyTemplate: bad mesh or material id");
+    const MeshRec& m = meshes_[v.mesh];
+    if (uint64_t(v.index_offset) + v.index_count > m.index_count)
+      return fail(GBR_ERROR_INVALID_ARGUMENT, "addNodeHierarchyTemplate: index range out of mesh");
+  }
+  for (uint32_t i = 0; i < count; ++i) {
+    const gbr_mesh_view& v = views[i];
+    const MeshRec& m = meshes_[v.mesh];
+    MeshView mv{};
+    mv.mesh = v.mesh;
+    mv.index_offset = v.index_offset;
+    mv.index_count = v.index_count;
+    mv.material = v.material;
+    std::memcpy(mv.transform, v.transform, 64);
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t k = 0; k < v.index_count; ++k) {
+      const uint32_t vi = host_indices_[size_t(m.index_base) + v.index_offset + k];
+      const float* p = &host_pos_[(size_t(m.vertex_base) + vi) * 3];
+      for (int c = 0; c < 3; ++c) {
+        lo[c] = std::min(lo[c], p[c]);
+        hi[c] = std::max(hi[c], p[c]);
+      }
+    }
+    for (int c = 0; c < 3; ++c) {
+      mv.bbox[c] = lo[c];
+      mv.bbox[3 + c] = hi[c];
+    }
+    views_.push_back(mv);
+  }
+  names_[name] = {begin, uint32_t(views_.size())};
+  return GBR_OK;
+}
+
+gbr_status Renderer::add_file(const char* filename, uint32_t flags, const char* name) {
+  if (!filename) return fail(GBR_ERROR_INVALID_ARGUMENT, "addFile: null filename");
+  ImportedFile f;
+  std::string err;
+  const bool no_textures = cfg_.flags & GBR_FLAG_NO_TEXTURES;
+  if (!import_gltf(filename, flags & GBR_FILE_WHOLE, name ? name : "", no_textures, f, err))
+    return fail(GBR_ERROR_IO, "Renderer::addFile(): " + err);
+  for (auto& t : f.templates)
+    if (names_.count(t.name))
+      return fail(GBR_ERROR_INVALID_ARGUMENT,
+                  "Renderer::addFile(): node name " + t.name + " in " + filename + " already exists");
+  const uint32_t texture_offset = uint32_t(textures_.size());
+  const uint32_t mesh_offset = uint32_t(meshes_.size());
+  const uint32_t material_offset = uint32_t(materials_.size());
+  // GenerateMipmap: mip levels are not sampled (see sample() in kernels.cu),
+  // so the flag changes nothing in the output.
+  for (auto& t : f.textures) {
+    gbr_texture_data td{t.width, t.height, t.layers, t.rgba.data(), t.filter, t.wrap_s, t.wrap_t};
+    uint32_t id;
+    gbr_status s = add_texture(td, &id);
+    if (s != GBR_OK) return s;
+  }
+  for (auto& m : f.meshes) {
+    gbr_mesh_data md{m.vertex_count,
+                     m.positions.data(),
+                     m.colors.empty() ? nullptr : m.colors.data(),
+                     m.texcoords.empty() ? nullptr : m.texcoords.data(),
+                     m.object_ids.empty() ? nullptr : m.object_ids.data(),
+                     uint32_t(m.indices.size()),
+                     m.indices.data()};
+    uint32_t id;
+    gbr_status s = add_mesh(md, &id);
+    if (s != GBR_OK) return s;
+  }
+  for (auto& m : f.materials) {
+    gbr_material_data md{};
+    std::memcpy(md.color, m.color, 16);
+    if (m.texture < 0) {
+      md.texture = 0;
+      md.layer = 0;
+      const float id3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+      std::memcpy(md.matrix, id3, 36);
+    } else {
+      md.texture = uint32_t(m.texture) + texture_offset;
+      md.layer = uint32_t(m.layer);
+      std::memcpy(md.matrix, m.matrix, 36);
+    }
+    uint32_t id;
+    add_material(md, &id);
+  }
+  for (auto& t : f.templates) {
+    std::vector<gbr_mesh_view> views;
+    for (uint32_t i = t.begin; i < t.end; ++i) {
+      const ImportedView& v = f.views[i];
+      gbr_mesh_view mv{};
+      mv.mesh = v.mesh + mesh_offset;
+      mv.index_offset = v.index_offset_bytes / 4;
+      mv.index_count = v.index_count;
+      mv.material = v.material < 0 ? 0u : uint32_t(v.material) + material_offset;
+      std::memcpy(mv.transform, v.transform, 64);
+      views.push_back(mv);
+    }
+    gbr_status s = add_template(t.name.c_str(), uint32_t(views.size()), views.data());
+    if (s != GBR_OK) return s;
+  }
+  return GBR_OK;
+}
+
+// --------------------------------------------------------------- scenes
+gbr_status Renderer::add_node_hierarchy(uint32_t scene, const char* name, const float* bake,
+                                        uint64_t* id) {
+  if (gbr_status s = check_scene(scene, "Renderer::addNodeHierarchy()")) return s;
+  auto found = names_.find(name ? name : "");
+  if (found == names_.end())
+    return fail(GBR_ERROR_NOT_FOUND,
+                std::string("Renderer::add(): name ") + (name ? name : "") + " not found");
+  SceneState& sc = scenes_[scene];
+  const uint32_t top = uint32_t(sc.parents.size());
+  sc.parents.push_back(-1);
+  sc.transforms.insert(sc.transforms.end(), kIdentity, kIdentity + 16);
+  const float* b = bake ? bake : kIdentity;
+  for (uint32_t i = found->second.first; i < found->second.second; ++i) {
+    const MeshView& v = views_[i];
+    const uint32_t nid = uint32_t(sc.parents.size());
+    sc.parents.push_back(int32_t(top));
+    float t[16];
+    mat4_mul(b, v.transform, t);
+    sc.transforms.insert(sc.transforms.end(), t, t + 16);
+    const BatchKey key{meshes_[v.mesh].flags & kMeshVertexColor, v.mesh,
+                       uint32_t(materials_[v.material].texture)};
+    uint32_t batch = 0;
+    while (batch < sc.batches.size() &&
+           !(sc.batches[batch].flags == key.flags && sc.batches[batch].mesh == key.mesh &&
+             sc.batches[batch].texture == key.texture))
+      ++batch;
+    if (batch == sc.batches.size()) sc.batches.push_back(key);
+    HostDraw d{batch, nid, top, v.mesh, v.index_offset, v.index_count, v.material, 0u, {}};
+    std::memcpy(d.bbox, v.bbox, 24);
+    sc.draws.push_back(d);
+  }
+  sc.transforms_dirty = true;
+  structure_dirty_ = true;
+  *id = top;
+  return GBR_OK;
+}
+
+gbr_status Renderer::add_empty_node(uint32_t scene, uint64_t* id) {
+  if (gbr_status s = check_scene(scene, "Renderer::addEmptyNode()")) return s;
+  SceneState& sc = scenes_[scene];
+  *id = sc.parents.size();
+  sc.parents.push_back(-1);
+  sc.transforms.insert(sc.transforms.end(), kIdentity, kIdentity + 16);
+  sc.transforms_dirty = true;
+  structure_dirty_ = true;
+  return GBR_OK;
+}
+
+gbr_status Renderer::clear(uint32_t scene) {
+  if (gbr_status s = check_scene(scene, "Renderer::clear()")) return s;
+  SceneState& sc = scenes_[scene];
+  sc.parents.clear();
+  sc.transforms.clear();
+  sc.draws.clear();
+  sc.batches.clear();
+  structure_dirty_ = true;
+  return GBR_OK;
+}
+
+gbr_status Renderer::set_semantic_id(uint32_t scene, uint64_t node, uint32_t id) {
+  if (gbr_status s = check_scene(scene, "Renderer::setSemanticId()")) return s;
+  SceneState& sc = scenes_[scene];
+  if (node >= sc.parents.size())
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "Renderer::setSemanticId(): node out of range");
+  for (auto& d : sc.draws)
+    if (d.top == node) d.semantic = id;
+  structure_dirty_ = true;
+  return GBR_OK;
+}
+
+gbr_status Renderer::update_camera(uint32_t scene, const float* p, const float* v) {
+  if (gbr_status s = check_scene(scene, "Renderer::updateCamera()")) return s;
+  SceneState& sc = scenes_[scene];
+  mat4_mul(p, v, sc.pv);
+  std::memcpy(sc.view, v, 64);
+  // calculateDepthUnprojection (DepthUnprojection.cpp:98-101)
+  sc.unprojection[0] = (p[2 * 4 + 2] - 1.0f) * 0.5f;
+  sc.unprojection[1] = p[3 * 4 + 2] * 0.5f;
+  return GBR_OK;
+}
+
+gbr_status Renderer::update_cameras(uint32_t first, uint32_t count, const float* p,
+                                    const float* v) {
+  if (uint64_t(first) + count > scenes_.size())
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "updateCameras: scene range out of bounds");
+  for (uint32_t i = 0; i < count; ++i) update_camera(first + i, p + 16 * size_t(i), v + 16 * size_t(i));
+  return GBR_OK;
+}
+
+gbr_status Renderer::camera(uint32_t scene, float* out) const {
+  if (gbr_status s = check_scene(scene, "Renderer::camera()")) return s;
+  std::memcpy(out, scenes_[scene].pv, 64);
+  return GBR_OK;
+}
+
+gbr_status Renderer::unprojection(uint32_t scene, float* out) const {
+  if (gbr_status s = check_scene(scene, "Renderer::cameraDepthUnprojection()")) return s;
+  out[0] = scenes_[scene].unprojection[0];
+  out[1] = scenes_[scene].unprojection[1];
+  return GBR_OK;
+}
+
+gbr_status Renderer::transformations(uint32_t scene, float** out, uint64_t* count) {
+  if (gbr_status s = check_scene(scene, "Renderer::transformations()")) return s;
+  SceneState& sc = scenes_[scene];
+  *out = sc.transforms.empty() ? nullptr : sc.transforms.data();
+  *count = sc.parents.size();
+  sc.transforms_dirty = true;
+  return GBR_OK;
+}
+
+gbr_status Renderer::stats(uint32_t scene, gbr_scene_stats_info* out) const {
+  if (gbr_status s = check_scene(scene, "Renderer::sceneStats()")) return s;
+  const SceneState& sc = scenes_[scene];
+  out->node_count = sc.parents.size();
+  out->draw_count = sc.draws.size();
+  out->draw_batch_count = sc.batches.size();
+  return GBR_OK;
+}
+
+// -------------------------------------------------------------- drawing
+gbr_status Renderer::upload_tables() {
+  if (!tables_dirty_) return GBR_OK;
+  if (!d_meshes_.reserve(std::max<size_t>(1, meshes_.size()) * sizeof(MeshRec), false) ||
+      !d_materials_.reserve(materials_.size() * sizeof(MaterialRec), false) ||
+      !d_textures_.reserve(textures_.size() * sizeof(TextureRec), false))
+    return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of device memory for tables");
+  if (!meshes_.empty())
+    GBR_CUDA(cudaMemcpy(d_meshes_.ptr, meshes_.data(), meshes_.size() * sizeof(MeshRec),
+                        cudaMemcpyHostToDevice), "table upload");
+  GBR_CUDA(cudaMemcpy(d_materials_.ptr, materials_.data(), materials_.size() * sizeof(MaterialRec),
+                      cudaMemcpyHostToDevice), "table upload");
+  GBR_CUDA(cudaMemcpy(d_textures_.ptr, textures_.data(), textures_.size() * sizeof(TextureRec),
+                      cudaMemcpyHostToDevice), "table upload");
+  tables_dirty_ = false;
+  return GBR_OK;
+}
+
+gbr_status Renderer::rebuild(cudaStream_t stream) {
+  GBR_CUDA(cudaStreamSynchronize(stream), "draw: synchronise before rebuild");
+  if (upload_pending_) {
+    cudaEventSynchronize(upload_done_);
+    upload_pending_ = false;
+  }
+  const uint32_t S = uint32_t(scenes_.size());
+  std::vector<SceneRec> recs(S);
+  std::vector<int32_t> parents;
+  std::vector<DrawRec> draws;
+  std::vector<uint64_t> cost(S, 0);
+  uint32_t nodes = 0;
+  for (uint32_t s = 0; s < S; ++s) {
+    SceneState& sc = scenes_[s];
+    SceneRec& r = recs[s];
+    r.width = sc.width;
+    r.height = sc.height;
+    r.fb_offset = sc.fb_offset;
+    r.pitch = sc.pitch;
+    r.node_base = nodes;
+    r.node_count = uint32_t(sc.parents.size());
+    sc.node_base = nodes;
+    r.draw_base = uint32_t(draws.size());
+    r.draw_count = uint32_t(sc.draws.size());
+    nodes += r.node_count;
+    parents.insert(parents.end(), sc.parents.begin(), sc.parents.end());
+    // Stable counting sort of the draws by batch id (Renderer.cpp:1139-1196).
+    std::vector<uint32_t> order(sc.draws.size());
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+      return sc.draws[a].batch < sc.draws[b].batch;
+    });
+    uint64_t tris = 0;
+    for (uint32_t k : order) {
+      const HostDraw& d = sc.draws[k];
+      DrawRec dr{};
+      dr.node = d.node;
+      dr.mesh = d.mesh;
+      dr.first_index = meshes_[d.mesh].index_base + d.index_offset;
+      dr.tri_count = d.index_count / 3;
+      dr.material = d.material;
+      dr.semantic_id = d.semantic;
+      std::memcpy(dr.bbox, d.bbox, 24);
+      draws.push_back(dr);
+      tris += dr.tri_count;
+    }
+    if (tris >= (1ull << 31))
+      return fail(GBR_ERROR_INVALID_ARGUMENT, "draw: 2^31 or more triangles in one scene");
+    cost[s] = tris;
+  }
+  total_nodes_ = nodes;
+  total_draws_ = uint32_t(draws.size());
+  total_tris_ = std::accumulate(cost.begin(), cost.end(), uint64_t(0));
+
+  // Work items: each scene's viewport cut into regions of at most
+  // region_width x region_height pixels.
+  std::vector<WorkItem> items;
+  std::vector<uint64_t> item_cost;
+  scene_item_base_.assign(S, 0);
+  scene_item_count_.assign(S, 0);
+  const int rwm = tuning_.region_width, rhm = tuning_.region_height;
+  for (uint32_t s = 0; s < S; ++s) {
+    scene_item_base_[s] = uint32_t(items.size());
+    const SceneState& sc = scenes_[s];
+    for (int y = 0; y < sc.height; y += rhm)
+      for (int x = 0; x < sc.width; x += rwm) {
+        WorkItem it{};
+        it.scene = s;
+        it.x0 = uint16_t(x);
+        it.y0 = uint16_t(y);
+        it.w = uint16_t(std::min(rwm, sc.width - x));
+        it.h = uint16_t(std::min(rhm, sc.height - y));
+        items.push_back(it);
+        item_cost.push_back(cost[s] + 1);
+      }
+    scene_item_count_[s] = uint32_t(items.size()) - scene_item_base_[s];
+  }
+  item_count_ = uint32_t(items.size());
+  // Longest-processing-time-first order for the persistent grid.
+  std::vector<uint32_t> perm(items.size());
+  std::iota(perm.begin(), perm.end(), 0u);
+  std::stable_sort(perm.begin(), perm.end(),
+                   [&](uint32_t a, uint32_t b) { return item_cost[a] > item_cost[b]; });
+  std::vector<WorkItem> lpt(items.size());
+  for (size_t i = 0; i < perm.size(); ++i) lpt[i] = items[perm[i]];
+
+  cudaSetDevice(device_);
+  if (gbr_status st = upload_tables()) return st;
+  const size_t S1 = std::max<size_t>(S, 1);
+  if (!d_scenes_.reserve(S1 * sizeof(SceneRec), false) ||
+      !d_parents_.reserve(std::max<size_t>(nodes, 1) * 4, false) ||
+      !d_local_.reserve(std::max<size_t>(nodes, 1) * 64, false) ||
+      !d_draws_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(DrawRec), false) ||
+      !d_cameras_.reserve(S1 * kCameraBytes, false) ||
+      !d_visible_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(VisibleRec), false) ||
+      !d_vis_count_.reserve(S1 * 4, false) || !d_vis_tris_.reserve(S1 * 4, false) ||
+      !d_status_.reserve(4, false) || !d_counter_.reserve(4, false) ||
+      !d_items_.reserve(std::max<size_t>(items.size(), 1) * sizeof(WorkItem), false) ||
+      !d_items_lpt_.reserve(std::max<size_t>(items.size(), 1) * sizeof(WorkItem), false) ||
+      !h_stage_.reserve(S1 * kCameraBytes + std::max<size_t>(nodes, 1) * 64))
+    return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of memory for scene data");
+  GBR_CUDA(cudaMemcpy(d_scenes_.ptr, recs.data(), S * sizeof(SceneRec), cudaMemcpyHostToDevice),
+           "scene upload");
+  if (nodes)
+    GBR_CUDA(cudaMemcpy(d_parents_.ptr, parents.data(), nodes * 4, cudaMemcpyHostToDevice),
+             "scene upload");
+  if (!draws.empty())
+    GBR_CUDA(cudaMemcpy(d_draws_.ptr, draws.data(), draws.size() * sizeof(DrawRec),
+                        cudaMemcpyHostToDevice), "scene upload");
+  if (!items.empty()) {
+    GBR_CUDA(cudaMemcpy(d_items_.ptr, items.data(), items.size() * sizeof(WorkItem),
+                        cudaMemcpyHostToDevice), "scene upload");
+    GBR_CUDA(cudaMemcpy(d_items_lpt_.ptr, lpt.data(), lpt.size() * sizeof(WorkItem),
+                        cudaMemcpyHostToDevice), "scene upload");
+  }
+  GBR_CUDA(cudaMemset(d_status_.ptr, 0, 4), "scene upload");
+  for (auto& sc : scenes_) sc.transforms_dirty = true;
+  structure_dirty_ = false;
+  graph_valid_ = false;
+  return GBR_OK;
+}
+
+gbr_status Renderer::ensure_raster_config() {
+  if (raster_configured_) return GBR_OK;
+  const int region_px = tuning_.region_width * tuning_.region_height;
+  size_t max_dyn = 0;
+  GBR_CUDA(raster_configure(tuning_.threads, &max_dyn), "raster configure");
+  int cap = kPrefixCapMax;
+  size_t smem = raster_smem_bytes(tuning_.threads, region_px, cap);
+  while (smem > max_dyn && cap > 64) {
+    cap /= 2;
+    smem = raster_smem_bytes(tuning_.threads, region_px, cap);
+  }
+  if (smem > max_dyn)
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "tuning: region does not fit in shared memory");
+  int occ = 0;
+  GBR_CUDA(raster_max_ctas_per_sm(tuning_.threads, smem, &occ), "raster occupancy");
+  if (occ < 1) return fail(GBR_ERROR_INVALID_ARGUMENT, "tuning: raster kernel cannot be resident");
+  ctas_per_sm_ = std::min(occ, std::max(1, tuning_.ctas_per_sm));
+  smem_bytes_ = smem;
+  prefix_cap_ = cap;
+  raster_configured_ = true;
+  return GBR_OK;
+}
+
+gbr_status Renderer::upload_step(cudaStream_t stream) {
+  // Cameras always, local transforms of scenes whose view was taken.
+  const uint32_t S = uint32_t(scenes_.size());
+  if (upload_pending_) {
+    GBR_CUDA(cudaEventSynchronize(upload_done_), "draw: wait for previous upload");
+    upload_pending_ = false;
+  }
+  char* stage = static_cast<char*>(h_stage_.ptr);
+  CameraRec* cams = reinterpret_cast<CameraRec*>(stage);
+  for (uint32_t s = 0; s < S; ++s) {
+    std::memcpy(cams[s].pv, scenes_[s].pv, 64);
+    for (int k = 0; k < 4; ++k) cams[s].vrow[k] = scenes_[s].view[k * 4 + 2];
+  }
+  float* tstage = reinterpret_cast<float*>(stage + size_t(S) * kCameraBytes);
+  // Coalesce runs of dirty scenes into single copies.
+  uint32_t s = 0;
+  while (s < S) {
+    if (!scenes_[s].transforms_dirty || scenes_[s].parents.empty()) {
+      scenes_[s].transforms_dirty = false;
+      ++s;
+      continue;
+    }
+    const uint32_t begin = s;
+    while (s < S && (scenes_[s].transforms_dirty || scenes_[s].parents.empty())) {
+      SceneState& sc = scenes_[s];
+      if (!sc.parents.empty())
+        std::memcpy(tstage + size_t(sc.node_base) * 16, sc.transforms.data(), sc.parents.size() * 64);
+      sc.transforms_dirty = false;
+      ++s;
+    }
+    const size_t nb = scenes_[begin].node_base;
+    const size_t ne = s < S ? scenes_[s].node_base : total_nodes_;
+    if (ne > nb)
+      GBR_CUDA(cudaMemcpyAsync(d_local_.as<float>() + nb * 16, tstage + nb * 16, (ne - nb) * 64,
+                               cudaMemcpyHostToDevice, stream), "transform upload");
+  }
+  return GBR_OK;
+}
+
+gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
+  const uint32_t S = uint32_t(scenes_.size());
+  PrepareParams pp{};
+  pp.scenes = d_scenes_.as<SceneRec>();
+  pp.cameras = d_cameras_.as<CameraRec>();
+  pp.draws = d_draws_.as<DrawRec>();
+  pp.parents = d_parents_.as<int32_t>();
+  pp.local = d_local_.as<float>();
+  pp.meshes = d_meshes_.as<MeshRec>();
+  pp.visible = d_visible_.as<VisibleRec>();
+  pp.vis_count = d_vis_count_.as<uint32_t>();
+  pp.vis_tris = d_vis_tris_.as<uint32_t>();
+  pp.status = d_status_.as<uint32_t>();
+  RasterParams rp{};
+  rp.scenes = pp.scenes;
+  rp.visible = pp.visible;
+  rp.vis_count = pp.vis_count;
+  rp.vis_tris = pp.vis_tris;
+  rp.pos = d_pos_.as<float4>();
+  rp.color = d_color_.as<float4>();
+  rp.uv = d_uv_.as<float2>();
+  rp.indices = d_indices_.as<uint32_t>();
+  rp.materials = d_materials_.as<MaterialRec>();
+  rp.textures = d_textures_.as<TextureRec>();
+  rp.texels = d_texels_.as<uint32_t>();
+  rp.texture_count = int32_t(textures_.size());
+  rp.flags = (cfg_.flags & GBR_FLAG_NO_TEXTURES) ? 1u : 0u;
+  rp.counter = d_counter_.as<uint32_t>();
+  rp.out.color = (cfg_.planes & GBR_PLANE_COLOR) ? d_planes_[0].as<uint32_t>() : nullptr;
+  rp.out.depth = (cfg_.planes & GBR_PLANE_DEPTH) ? d_planes_[1].as<float>() : nullptr;
+  rp.out.linear = (cfg_.planes & GBR_PLANE_LINEAR_DEPTH) ? d_planes_[2].as<float>() : nullptr;
+  rp.out.semantic = (cfg_.planes & GBR_PLANE_SEMANTIC) ? d_planes_[3].as<uint32_t>() : nullptr;
+  rp.region_px = tuning_.region_width * tuning_.region_height;
+  rp.prefix_cap = prefix_cap_;
+  rp.small_area = tuning_.small_area;
+  uint64_t launches = 0;
+  if (mode == GBR_DRAW_BATCHED) {
+    pp.scene_base = 0;
+    GBR_CUDA(launch_prepare(pp, S, stream), "prepare launch");
+    GBR_CUDA(cudaMemsetAsync(d_counter_.ptr, 0, 4, stream), "counter reset");
+    rp.items = d_items_lpt_.as<WorkItem>();
+    rp.item_base = 0;
+    rp.item_count = item_count_;
+    rp.persistent = 1;
+    const uint32_t grid =
+        std::min<uint32_t>(item_count_, uint32_t(sm_count_) * uint32_t(ctas_per_sm_));
+    GBR_CUDA(launch_raster(rp, tuning_.threads, grid, smem_bytes_, stream), "raster launch");
+    launches = 2;
+  } else {
+    rp.items = d_items_.as<WorkItem>();
+    rp.persistent = 0;
+    for (uint32_t s = 0; s < S; ++s) {
+      pp.scene_base = s;
+      GBR_CUDA(launch_prepare(pp, 1, stream), "prepare launch");
+      rp.item_base = scene_item_base_[s];
+      rp.item_count = scene_item_count_[s];
+      GBR_CUDA(launch_raster(rp, tuning_.threads, scene_item_count_[s], smem_bytes_, stream),
+               "raster launch");
+      launches += 2;
+    }
+  }
+  launches_ = launches;
+  return GBR_OK;
+}
+
+gbr_status Renderer::draw(cudaStream_t stream, uint32_t mode, bool use_graph) {
+  cudaSetDevice(device_);
+  if (use_graph && mode == GBR_DRAW_BATCHED && stream == nullptr) stream = own_stream_;
+  if (structure_dirty_)
+    if (gbr_status s = rebuild(stream)) return s;
+  if (gbr_status s = ensure_raster_config()) return s;
+  if (tables_dirty_)
+    if (gbr_status s = upload_tables()) return s;
+  if (gbr_status s = upload_step(stream)) return s;
+  const uint32_t S = uint32_t(scenes_.size());
+  const size_t cam_bytes = size_t(S) * kCameraBytes;
+  if (mode == GBR_DRAW_BATCHED && use_graph) {
+    if (!graph_valid_ || graph_stream_ != stream) {
+      if (graph_exec_) {
+        cudaGraphExecDestroy(graph_exec_);
+        graph_exec_ = nullptr;
+      }
+      cudaGraph_t g;
+      GBR_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+      cudaError_t e = cudaMemcpyAsync(d_cameras_.ptr, h_stage_.ptr, cam_bytes,
+                                      cudaMemcpyHostToDevice, stream);
+      gbr_status st = e == cudaSuccess ? enqueue_step(stream, mode) : cuda_fail(e, "graph camera copy");
+      cudaError_t e2 = cudaStreamEndCapture(stream, &g);
+      if (st != GBR_OK) return st;
+      GBR_CUDA(e2, "graph capture");
+      e = cudaGraphInstantiate(&graph_exec_, g, 0);
+      cudaGraphDestroy(g);
+      GBR_CUDA(e, "graph instantiate");
+      graph_valid_ = true;
+      graph_stream_ = stream;
+    }
+    GBR_CUDA(cudaGraphLaunch(graph_exec_, stream), "graph launch");
+  } else {
+    GBR_CUDA(cudaMemcpyAsync(d_cameras_.ptr, h_stage_.ptr, cam_bytes, cudaMemcpyHostToDevice, stream),
+             "camera upload");
+    if (gbr_status s = enqueue_step(stream, mode)) return s;
+  }
+  GBR_CUDA(cudaEventRecord(upload_done_, stream), "event record");
+  upload_pending_ = true;
+  last_stream_ = stream;
+  last_stats_.scenes = S;
+  last_stats_.draws = total_draws_;
+  last_stats_.kernel_launches = launches_;
+  return GBR_OK;
+}
+
+gbr_status Renderer::sync_and_check() {
+  cudaSetDevice(device_);
+  GBR_CUDA(cudaStreamSynchronize(last_stream_), "synchronise");
+  if (d_status_.ptr) {
+    uint32_t status = 0;
+    GBR_CUDA(cudaMemcpy(&status, d_status_.ptr, 4, cudaMemcpyDeviceToHost), "status read");
+    if (status) {
+      cudaMemset(d_status_.ptr, 0, 4);
+      return fail(GBR_ERROR_DEVICE, "draw: the device reported bad scene data (status " +
+                                        std::to_string(status) + ")");
+    }
+  }
+  return GBR_OK;
+}
+
+void* Renderer::plane_ptr(uint32_t plane, size_t* elem) const {
+  const int slot = plane_slot(plane);
+  if (slot < 0 || !(cfg_.planes & plane)) return nullptr;
+  *elem = plane_elem(plane);
+  return d_planes_[slot].ptr;
+}
+
+gbr_status Renderer::image_into(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes) {
+  if (ragged_) return fail(GBR_ERROR_STATE, "imageInto: the ragged layout has no tile grid; use sceneImageInto");
+  size_t elem;
+  const char* src = static_cast<const char*>(plane_ptr(plane, &elem));
+  if (!src) return fail(GBR_ERROR_INVALID_ARGUMENT, "imageInto: plane not enabled");
+  if (!(rect[0] >= 0 && rect[1] >= 0 && rect[2] <= fb_w_ && rect[3] <= fb_h_ && rect[0] <= rect[2] &&
+        rect[1] <= rect[3]))
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "imageInto: rectangle doesn't fit in the framebuffer");
+  const size_t w = size_t(rect[2] - rect[0]), h = size_t(rect[3] - rect[1]);
+  if (row_bytes < w * elem) return fail(GBR_ERROR_INVALID_ARGUMENT, "imageInto: row pitch too small");
+  if (gbr_status s = sync_and_check()) return s;
+  if (!w || !h) return GBR_OK;
+  GBR_CUDA(cudaMemcpy2D(dst, row_bytes, src + (size_t(rect[1]) * fb_w_ + rect[0]) * elem,
+                        size_t(fb_w_) * elem, w * elem, h, cudaMemcpyDeviceToHost),
+           "imageInto copy");
+  return GBR_OK;
+}
+
+gbr_status Renderer::scene_image_into(uint32_t plane, uint32_t scene, void* dst, uint64_t row_bytes) {
+  if (gbr_status s = check_scene(scene, "sceneImageInto()")) return s;
+  size_t elem;
+  const char* src = static_cast<const char*>(plane_ptr(plane, &elem));
+  if (!src) return fail(GBR_ERROR_INVALID_ARGUMENT, "sceneImageInto: plane not enabled");
+  const SceneState& sc = scenes_[scene];
+  if (row_bytes < size_t(sc.width) * elem)
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "sceneImageInto: row pitch too small");
+  if (gbr_status s = sync_and_check()) return s;
+  GBR_CUDA(cudaMemcpy2D(dst, row_bytes, src + size_t(sc.fb_offset) * elem, size_t(sc.pitch) * elem,
+                        size_t(sc.width) * elem, size_t(sc.height), cudaMemcpyDeviceToHost),
+           "sceneImageInto copy");
+  return GBR_OK;
+}
+
+gbr_status Renderer::plane_pointer(uint32_t plane, void** out, uint64_t* bytes) {
+  size_t elem;
+  void* p = plane_ptr(plane, &elem);
+  if (!p) return fail(GBR_ERROR_INVALID_ARGUMENT, "planeDevicePointer: plane not enabled");
+  *out = p;
+  if (bytes) *bytes = uint64_t(fb_px_) * elem;
+  return GBR_OK;
+}
+
+// ------------------------------------------------------------- DLPack
+namespace {
+struct DLDevice_ {
+  int32_t device_type;
+  int32_t device_id;
+};
+struct DLDataType_ {
+  uint8_t code;
+  uint8_t bits;
+  uint16_t lanes;
+};
+struct DLTensor_ {
+  void* data;
+  DLDevice_ device;
+  int32_t ndim;
+  DLDataType_ dtype;
+  int64_t* shape;
+  int64_t* strides;
+  uint64_t byte_offset;
+};
+struct DLManagedTensor_ {
+  DLTensor_ dl_tensor;
+  void* manager_ctx;
+  void (*deleter)(DLManagedTensor_*);
+};
+struct DLHolder {
+  DLManagedTensor_ t;
+  int64_t shape[3];
+  Renderer* owner;
+};
+void dl_deleter(DLManagedTensor_* t) {
+  DLHolder* h = static_cast<DLHolder*>(t->manager_ctx);
+  h->owner->release();
+  delete h;
+}
+}  // namespace
+
+gbr_status Renderer::plane_dlpack(uint32_t plane, void** out) {
+  size_t elem;
+  void* p = plane_ptr(plane, &elem);
+  if (!p) return fail(GBR_ERROR_INVALID_ARGUMENT, "planeDlpack: plane not enabled");
+  DLHolder* h = new DLHolder();
+  h->owner = this;
+  retain();
+  h->t.manager_ctx = h;
+  h->t.deleter = dl_deleter;
+  DLTensor_& t = h->t.dl_tensor;
+  t.data = p;
+  t.device = {2 /* kDLCUDA */, device_};
+  t.byte_offset = 0;
+  t.strides = nullptr;
+  int nd = 0;
+  if (ragged_) {
+    h->shape[nd++] = fb_px_;
+  } else {
+    h->shape[nd++] = fb_h_;
+    h->shape[nd++] = fb_w_;
+  }
+  if (plane == GBR_PLANE_COLOR) {
+    h->shape[nd++] = 4;
+    t.dtype = {1 /* uint */, 8, 1};
+  } else if (plane == GBR_PLANE_SEMANTIC) {
+    t.dtype = {1, 32, 1};
+  } else {
+    t.dtype = {2 /* float */, 32, 1};
+  }
+  t.ndim = nd;
+  t.shape = h->shape;
+  *out = &h->t;
+  return GBR_OK;
+}
+
+gbr_status Renderer::get_tuning(gbr_tuning* t) const {
+  *t = tuning_;
+  return GBR_OK;
+}
+
+gbr_status Renderer::set_tuning(const gbr_tuning& t) {
+  if ((t.threads != 256 && t.threads != 512 && t.threads != 1024) || t.region_width < 4 ||
+      t.region_height < 1 || t.region_width > 1024 || t.region_height > 1024 ||
+      t.region_width * t.region_height > 32768 || t.small_area < 1 || t.ctas_per_sm < 1)
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "setTuning: out of range");
+  tuning_ = t;
+  raster_configured_ = false;
+  structure_dirty_ = true;  // regions change
+  return GBR_OK;
+}
+
+gbr_status Renderer::last_stats(gbr_draw_stats* out) {
+  if (gbr_status s = sync_and_check()) return s;
+  const uint32_t S = uint32_t(scenes_.size());
+  std::vector<uint32_t> cnt(S), tris(S);
+  if (S && d_vis_count_.ptr) {
+    GBR_CUDA(cudaMemcpy(cnt.data(), d_vis_count_.ptr, S * 4, cudaMemcpyDeviceToHost), "stats");
+    GBR_CUDA(cudaMemcpy(tris.data(), d_vis_tris_.ptr, S * 4, cudaMemcpyDeviceToHost), "stats");
+  }
+  last_stats_.visible_draws = std::accumulate(cnt.begin(), cnt.end(), uint64_t(0));
+  last_stats_.triangles = std::accumulate(tris.begin(), tris.end(), uint64_t(0));
+  *out = last_stats_;
+  return GBR_OK;
+}
+
+}  // namespace gbr

@@ -1,0 +1,182 @@
+// Host runtime of the GB300 batch renderer: the C++ counterpart of
+// esp::gfx_batch::Renderer / RendererStandalone (src/esp/gfx_batch/Renderer.h,
+// RendererStandalone.h) with device-resident scene data.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/gbr.h"
+#include "kernels.h"
+#include "records.h"
+
+namespace gbr {
+
+// A growable device allocation.
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  ~DeviceBuffer();
+  bool reserve(size_t n, bool keep, cudaStream_t stream = nullptr);
+  template <class T>
+  T* as() const { return static_cast<T*>(ptr); }
+};
+
+struct PinnedBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  ~PinnedBuffer();
+  bool reserve(size_t n);
+};
+
+struct MeshView {
+  uint32_t mesh, index_offset, index_count, material;
+  float transform[16];
+  float bbox[6];
+};
+
+struct HostDraw {
+  uint32_t batch, node, top, mesh, index_offset, index_count, material, semantic;
+  float bbox[6];
+};
+
+struct BatchKey {
+  uint32_t flags, mesh, texture;
+};
+
+struct SceneState {
+  std::vector<int32_t> parents;
+  std::vector<float> transforms;  // 16 per node
+  std::vector<HostDraw> draws;    // add order
+  std::vector<BatchKey> batches;
+  float pv[16];
+  float view[16];
+  float unprojection[2] = {0, 0};
+  int32_t width = 0, height = 0;
+  int64_t fb_offset = 0, pitch = 0;
+  bool transforms_dirty = true;
+  uint32_t node_base = 0;  // in the flattened device arrays
+};
+
+class Renderer {
+ public:
+  static Renderer* create(const gbr_config& cfg, std::string& err);
+  ~Renderer();
+
+  std::atomic<int> refs{1};
+  void retain() { refs.fetch_add(1); }
+  void release() {
+    if (refs.fetch_sub(1) == 1) delete this;
+  }
+
+  // -- resources
+  gbr_status add_file(const char* filename, uint32_t flags, const char* name);
+  gbr_status add_mesh(const gbr_mesh_data& m, uint32_t* id);
+  gbr_status add_texture(const gbr_texture_data& t, uint32_t* id);
+  gbr_status add_material(const gbr_material_data& m, uint32_t* id);
+  gbr_status add_template(const char* name, uint32_t count, const gbr_mesh_view* views);
+
+  // -- scenes
+  bool has_hierarchy(const char* name) const { return names_.count(name) != 0; }
+  gbr_status add_node_hierarchy(uint32_t scene, const char* name, const float* bake, uint64_t* id);
+  gbr_status add_empty_node(uint32_t scene, uint64_t* id);
+  gbr_status clear(uint32_t scene);
+  gbr_status set_semantic_id(uint32_t scene, uint64_t node, uint32_t id);
+  gbr_status update_camera(uint32_t scene, const float* p, const float* v);
+  gbr_status update_cameras(uint32_t first, uint32_t count, const float* p, const float* v);
+  gbr_status camera(uint32_t scene, float* out) const;
+  gbr_status unprojection(uint32_t scene, float* out) const;
+  gbr_status transformations(uint32_t scene, float** out, uint64_t* count);
+  gbr_status stats(uint32_t scene, gbr_scene_stats_info* out) const;
+
+  // -- drawing
+  gbr_status draw(cudaStream_t stream, uint32_t mode, bool use_graph);
+  gbr_status image_into(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes);
+  gbr_status scene_image_into(uint32_t plane, uint32_t scene, void* dst, uint64_t row_bytes);
+  gbr_status plane_pointer(uint32_t plane, void** out, uint64_t* bytes);
+  gbr_status plane_dlpack(uint32_t plane, void** out);
+  gbr_status get_tuning(gbr_tuning* t) const;
+  gbr_status set_tuning(const gbr_tuning& t);
+  gbr_status last_stats(gbr_draw_stats* out);
+
+  uint32_t scene_count() const { return uint32_t(scenes_.size()); }
+  const gbr_config& config() const { return cfg_; }
+  bool ragged() const { return ragged_; }
+  int64_t fb_width() const { return fb_w_; }
+  int64_t fb_height() const { return fb_h_; }
+  const SceneState& scene(uint32_t s) const { return scenes_[s]; }
+
+ private:
+  Renderer() = default;
+  gbr_status fail(gbr_status s, const std::string& msg);
+  gbr_status cuda_fail(cudaError_t e, const char* what);
+  gbr_status check_scene(uint32_t scene, const char* fn) const;
+  gbr_status upload_tables();
+  gbr_status rebuild(cudaStream_t stream);
+  gbr_status upload_step(cudaStream_t stream);
+  gbr_status enqueue_step(cudaStream_t stream, uint32_t mode);
+  gbr_status ensure_raster_config();
+  void* plane_ptr(uint32_t plane, size_t* elem) const;
+  gbr_status sync_and_check();
+
+  gbr_config cfg_{};
+  std::vector<int32_t> viewports_;
+  bool ragged_ = false;
+  int64_t fb_w_ = 0, fb_h_ = 0, fb_px_ = 0;
+  int device_ = 0;
+  int sm_count_ = 0;
+
+  // resources (host mirrors)
+  std::vector<MeshRec> meshes_;
+  std::vector<float> host_pos_;                    // xyz per vertex, for view bounding boxes
+  std::vector<uint32_t> host_indices_;
+  std::vector<TextureRec> textures_;
+  uint64_t texel_count_ = 0;
+  std::vector<MaterialRec> materials_;
+  std::vector<MeshView> views_;
+  std::unordered_map<std::string, std::pair<uint32_t, uint32_t>> names_;
+  uint32_t vertex_count_ = 0, index_count_ = 0;
+  bool tables_dirty_ = true;
+
+  std::vector<SceneState> scenes_;
+  bool structure_dirty_ = true;
+
+  // device
+  DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_;
+  DeviceBuffer d_meshes_, d_materials_, d_textures_;
+  DeviceBuffer d_scenes_, d_parents_, d_local_, d_draws_, d_cameras_;
+  DeviceBuffer d_visible_, d_vis_count_, d_vis_tris_, d_status_, d_items_, d_items_lpt_, d_counter_;
+  DeviceBuffer d_planes_[4];
+  PinnedBuffer h_stage_;
+  cudaEvent_t upload_done_ = nullptr;
+  bool upload_pending_ = false;
+  cudaStream_t last_stream_ = nullptr;
+  cudaStream_t own_stream_ = nullptr;
+
+  uint32_t total_nodes_ = 0, total_draws_ = 0;
+  uint64_t total_tris_ = 0;
+  std::vector<uint32_t> scene_item_base_, scene_item_count_;
+  uint32_t item_count_ = 0;
+
+  gbr_tuning tuning_{512, 128, 128, 64, 1};
+  size_t smem_bytes_ = 0;
+  int prefix_cap_ = 0;
+  bool raster_configured_ = false;
+  int ctas_per_sm_ = 1;
+
+  // CUDA graph of the batched step
+  cudaGraphExec_t graph_exec_ = nullptr;
+  cudaStream_t graph_stream_ = nullptr;
+  bool graph_valid_ = false;
+
+  gbr_draw_stats last_stats_{};
+  uint64_t launches_ = 0;
+};
+
+void set_last_error(const std::string& msg);
+
+}  // namespace gbr

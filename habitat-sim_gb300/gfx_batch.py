@@ -1,0 +1,519 @@
+"""Python mirror of habitat-sim's ``esp::gfx_batch`` batch renderer API.
+
+Same names, argument meaning and error behaviour as the C++ classes in
+``src/esp/gfx_batch/Renderer.h`` / ``RendererStandalone.h`` (the reference
+binds them to Python only through its replay renderer,
+``src/esp/bindings/SimBindings.cpp:467-545``).  Calls go through the C ABI
+of ``libgbr.so``; framebuffer planes can be handed out as CUDA torch
+tensors through DLPack without a copy.
+
+Conventions: matrices are numpy float32 ``[4, 4]`` arrays indexed
+``[column, row]`` (Magnum's column-major ``Matrix4``); images have row 0 at
+the bottom (GL window origin).  Out-of-range ids raise ``GbrError`` (the
+reference asserts, or raises in Python through ``ESP_CHECK``);
+``addFile`` returns ``False`` and prints a message like the reference
+(``Renderer.cpp:405-427``).
+"""
+import ctypes
+import enum
+import sys
+
+import numpy as np
+
+from . import _lib
+from ._lib import GbrError, check
+
+
+class RendererFlags(enum.IntFlag):
+    """``RendererFlag`` (Renderer.h:21-30)."""
+    NoTextures = 1
+
+
+class RendererFileFlags(enum.IntFlag):
+    """``RendererFileFlag`` (Renderer.h:120-154)."""
+    Whole = 1
+    GenerateMipmap = 2
+
+
+class RendererStandaloneFlags(enum.IntFlag):
+    """``RendererStandaloneFlag`` (RendererStandalone.h:21-36)."""
+    QuietLog = 1
+
+
+class Plane(enum.IntFlag):
+    Color = 1
+    Depth = 2
+    LinearDepth = 4
+    Semantic = 8
+    All = 15
+
+
+class DrawMode(enum.IntEnum):
+    PerScene = 0
+    Batched = 1
+
+
+def _f32(m, shape=None):
+    a = np.ascontiguousarray(m, dtype=np.float32)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def _fptr(a):
+    return a.ctypes.data_as(_lib.c_float_p)
+
+
+class RendererConfiguration:
+    """``RendererConfiguration`` (Renderer.h:45-113, Renderer.cpp:58-92) plus
+    per-scene viewports, output planes and the default draw mode."""
+
+    def __init__(self):
+        self.flags = RendererFlags(0)
+        self.tile_size = (128, 128)
+        self.tile_count = (1, 1)
+        self.max_light_count = 0
+        self.ambient_factor = 0.1
+        self.viewports = None
+        self.planes = Plane.All
+        self.draw_mode = DrawMode.PerScene
+
+    def setFlags(self, flags):
+        self.flags = RendererFlags(flags)
+        return self
+
+    def setTileSizeCount(self, tile_size, tile_count):
+        self.tile_size = (int(tile_size[0]), int(tile_size[1]))
+        self.tile_count = (int(tile_count[0]), int(tile_count[1]))
+        return self
+
+    def setMaxLightCount(self, count):
+        self.max_light_count = int(count)
+        return self
+
+    def setAmbientFactor(self, factor):
+        self.ambient_factor = float(factor)
+        return self
+
+    def setViewports(self, viewports):
+        """One (width, height) per scene: a ragged framebuffer instead of the
+        tile grid, for batches whose scenes differ in resolution."""
+        self.viewports = [(int(w), int(h)) for (w, h) in viewports]
+        return self
+
+    def setPlanes(self, planes):
+        self.planes = Plane(planes)
+        return self
+
+    def setDrawMode(self, mode):
+        self.draw_mode = DrawMode(mode)
+        return self
+
+
+class RendererStandaloneConfiguration:
+    """``RendererStandaloneConfiguration`` (RendererStandalone.h:47-100)."""
+
+    def __init__(self):
+        self.cuda_device = 0
+        self.flags = RendererStandaloneFlags(0)
+
+    def setCudaDevice(self, device):
+        self.cuda_device = int(device)
+        return self
+
+    def setFlags(self, flags):
+        self.flags = RendererStandaloneFlags(flags)
+        return self
+
+
+class SceneStats:
+    """``SceneStats`` (Renderer.h:745-779)."""
+
+    def __init__(self, node_count, draw_count, draw_batch_count):
+        self.nodeCount = node_count
+        self.drawCount = draw_count
+        self.drawBatchCount = draw_batch_count
+
+    def __repr__(self):
+        return (f"SceneStats(nodeCount={self.nodeCount}, drawCount={self.drawCount}, "
+                f"drawBatchCount={self.drawBatchCount})")
+
+
+def _stream_handle(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream or None
+    handle = getattr(stream, "cuda_stream", None)
+    if handle is not None:
+        return handle or None
+    raise TypeError("stream must be an int handle or a torch.cuda.Stream")
+
+
+class RendererStandalone:
+    """``RendererStandalone`` with its ``Renderer`` base, on the GPU."""
+
+    def __init__(self, configuration=None, standalone_configuration=None):
+        configuration = configuration or RendererConfiguration()
+        standalone_configuration = standalone_configuration or RendererStandaloneConfiguration()
+        self._lib = _lib.load()
+        cfg = _lib.Config()
+        self._lib.gbr_config_init(ctypes.byref(cfg))
+        cfg.flags = int(configuration.flags)
+        cfg.tile_size[0], cfg.tile_size[1] = configuration.tile_size
+        cfg.tile_count[0], cfg.tile_count[1] = configuration.tile_count
+        cfg.max_light_count = configuration.max_light_count
+        cfg.ambient_factor = configuration.ambient_factor
+        cfg.cuda_device = standalone_configuration.cuda_device
+        cfg.standalone_flags = int(standalone_configuration.flags)
+        cfg.planes = int(configuration.planes)
+        cfg.draw_mode = int(configuration.draw_mode)
+        self._viewports = None
+        if configuration.viewports:
+            vp = np.ascontiguousarray(np.array(configuration.viewports, np.int32).reshape(-1))
+            self._viewports = vp
+            cfg.scene_count = len(configuration.viewports)
+            cfg.viewports = vp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        handle = ctypes.c_void_p()
+        check(self._lib.gbr_create(ctypes.byref(cfg), ctypes.byref(handle)))
+        self._h = handle
+        self._config = configuration
+        self._standalone = standalone_configuration
+        self._quiet = bool(standalone_configuration.flags & RendererStandaloneFlags.QuietLog)
+        size = (ctypes.c_int64 * 2)()
+        check(self._lib.gbr_framebuffer_size(self._h, size))
+        self._fb = (int(size[0]), int(size[1]))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.gbr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ----------------------------------------------------------- queries
+    def flags(self):
+        return self._config.flags
+
+    def standaloneFlags(self):
+        return self._standalone.flags
+
+    def tileSize(self):
+        return self._config.tile_size
+
+    def tileCount(self):
+        return self._config.tile_count
+
+    def sceneCount(self):
+        n = ctypes.c_uint32()
+        check(self._lib.gbr_scene_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def maxLightCount(self):
+        return self._config.max_light_count
+
+    def framebufferSize(self):
+        """(width, height) of the tile-grid framebuffer, or (pixels, 1) for
+        the ragged layout."""
+        return self._fb
+
+    def sceneViewport(self, scene):
+        """(offset, pitch, width, height) of a scene inside each plane."""
+        out = (ctypes.c_int64 * 4)()
+        check(self._lib.gbr_scene_viewport(self._h, scene, out))
+        return tuple(int(v) for v in out)
+
+    # ------------------------------------------------------------- files
+    def addFile(self, filename, flags=0, name=None):
+        st = self._lib.gbr_add_file(self._h, str(filename).encode(), int(flags),
+                                    None if name is None else name.encode())
+        if st != 0:
+            if not self._quiet:
+                print(self._lib.gbr_last_error().decode(errors="replace"), file=sys.stderr)
+            return False
+        return True
+
+    # -------------------------------------------------------- procedural
+    def addMesh(self, positions, colors=None, texcoords=None, objectIds=None, indices=None):
+        pos = _f32(positions, (-1, 3))
+        n = len(pos)
+        col = None if colors is None else _f32(colors, (n, 4))
+        uv = None if texcoords is None else _f32(texcoords, (n, 2))
+        ids = None if objectIds is None else np.ascontiguousarray(objectIds, np.uint32).reshape(n)
+        idx = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+        md = _lib.MeshData(n, pos.ctypes.data, None if col is None else col.ctypes.data,
+                           None if uv is None else uv.ctypes.data,
+                           None if ids is None else ids.ctypes.data, len(idx), idx.ctypes.data)
+        out = ctypes.c_uint32()
+        check(self._lib.gbr_add_mesh(self._h, ctypes.byref(md), ctypes.byref(out)))
+        return out.value
+
+    def addTexture(self, pixels, filter=1, wrapS=0, wrapT=0):
+        """pixels: uint8 [layers, h, w, 4] or [h, w, 4], row 0 = bottom."""
+        p = np.ascontiguousarray(pixels, np.uint8)
+        if p.ndim == 3:
+            p = p[None]
+        td = _lib.TextureData(p.shape[2], p.shape[1], p.shape[0], p.ctypes.data, int(filter),
+                              int(wrapS), int(wrapT))
+        out = ctypes.c_uint32()
+        check(self._lib.gbr_add_texture(self._h, ctypes.byref(td), ctypes.byref(out)))
+        return out.value
+
+    def addMaterial(self, color=(1, 1, 1, 1), texture=0, layer=0, matrix=None):
+        m = np.eye(3, dtype=np.float32) if matrix is None else _f32(matrix, (3, 3))
+        md = _lib.MaterialData((ctypes.c_float * 4)(*[float(c) for c in color]), int(texture),
+                               int(layer), (ctypes.c_float * 9)(*m.reshape(-1).tolist()))
+        out = ctypes.c_uint32()
+        check(self._lib.gbr_add_material(self._h, ctypes.byref(md), ctypes.byref(out)))
+        return out.value
+
+    def addNodeHierarchyTemplate(self, name, views):
+        """views: iterable of (mesh, index_offset, index_count, material, transform|None);
+        index_offset counts indices."""
+        views = list(views)
+        arr = (_lib.MeshView * max(1, len(views)))()
+        for i, (mesh, off, cnt, mat, tr) in enumerate(views):
+            t = np.eye(4, dtype=np.float32) if tr is None else _f32(tr, (4, 4))
+            arr[i] = _lib.MeshView(int(mesh), int(off), int(cnt), int(mat),
+                                   (ctypes.c_float * 16)(*t.reshape(-1).tolist()))
+        check(self._lib.gbr_add_node_hierarchy_template(self._h, name.encode(), len(views), arr))
+
+    # ------------------------------------------------------------ scenes
+    def hasNodeHierarchy(self, name):
+        out = ctypes.c_int32()
+        check(self._lib.gbr_has_node_hierarchy(self._h, name.encode(), ctypes.byref(out)))
+        return bool(out.value)
+
+    def addNodeHierarchy(self, sceneId, name, bakeTransformation=None):
+        bake = None if bakeTransformation is None else _f32(bakeTransformation, (4, 4))
+        out = ctypes.c_uint64()
+        check(self._lib.gbr_add_node_hierarchy(self._h, sceneId, name.encode(),
+                                               None if bake is None else _fptr(bake),
+                                               ctypes.byref(out)))
+        return out.value
+
+    def addEmptyNode(self, sceneId):
+        out = ctypes.c_uint64()
+        check(self._lib.gbr_add_empty_node(self._h, sceneId, ctypes.byref(out)))
+        return out.value
+
+    def clear(self, sceneId):
+        check(self._lib.gbr_clear(self._h, sceneId))
+
+    def setSemanticId(self, sceneId, nodeId, semanticId):
+        check(self._lib.gbr_set_semantic_id(self._h, sceneId, nodeId, semanticId))
+
+    def camera(self, sceneId):
+        out = np.empty((4, 4), np.float32)
+        check(self._lib.gbr_camera(self._h, sceneId, _fptr(out)))
+        return out
+
+    def cameraDepthUnprojection(self, sceneId):
+        out = np.empty(2, np.float32)
+        check(self._lib.gbr_camera_depth_unprojection(self._h, sceneId, _fptr(out)))
+        return out
+
+    def updateCamera(self, sceneId, projection, view):
+        p = _f32(projection, (4, 4))
+        v = _f32(view, (4, 4))
+        check(self._lib.gbr_update_camera(self._h, sceneId, _fptr(p), _fptr(v)))
+
+    def updateCameras(self, projections, views, first=0):
+        p = _f32(projections, (-1, 4, 4))
+        v = _f32(views, (-1, 4, 4))
+        if p.shape != v.shape:
+            raise ValueError("projections and views differ in count")
+        check(self._lib.gbr_update_cameras(self._h, first, len(p), _fptr(p), _fptr(v)))
+
+    def transformations(self, sceneId):
+        """Writable [nodes, 4, 4] view of the scene's node transforms; valid
+        until the next add/clear on this scene (Renderer.cpp:1090-1099)."""
+        ptr = _lib.c_float_p()
+        n = ctypes.c_uint64()
+        check(self._lib.gbr_transformations(self._h, sceneId, ctypes.byref(ptr), ctypes.byref(n)))
+        if n.value == 0:
+            return np.zeros((0, 4, 4), np.float32)
+        return np.ctypeslib.as_array(ptr, shape=(n.value, 4, 4))
+
+    def sceneStats(self, sceneId):
+        s = _lib.SceneStatsInfo()
+        check(self._lib.gbr_scene_stats(self._h, sceneId, ctypes.byref(s)))
+        return SceneStats(s.node_count, s.draw_count, s.draw_batch_count)
+
+    # -------------------------------------------------------------- draw
+    def draw(self, stream=None, mode=None, graph=False):
+        """Render every scene into the framebuffer, asynchronously on
+        ``stream`` (a torch.cuda.Stream or a raw handle; None = default)."""
+        h = _stream_handle(stream)
+        if mode is None and not graph:
+            check(self._lib.gbr_draw(self._h, h))
+        else:
+            m = self._config.draw_mode if mode is None else DrawMode(mode)
+            check(self._lib.gbr_draw_mode(self._h, h, int(m), 1 if graph else 0))
+
+    def lastDrawStats(self):
+        s = _lib.DrawStats()
+        check(self._lib.gbr_last_draw_stats(self._h, ctypes.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in _lib.DrawStats._fields_}
+
+    def tuning(self):
+        t = _lib.Tuning()
+        check(self._lib.gbr_get_tuning(self._h, ctypes.byref(t)))
+        return {k: int(getattr(t, k)) for k, _ in _lib.Tuning._fields_}
+
+    def setTuning(self, **kw):
+        t = _lib.Tuning()
+        check(self._lib.gbr_get_tuning(self._h, ctypes.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        check(self._lib.gbr_set_tuning(self._h, ctypes.byref(t)))
+
+    # ------------------------------------------------------------ images
+    def _image(self, plane, dtype, channels=None):
+        if self._config.viewports:
+            raise GbrError(7, "the ragged layout has no tile grid; use sceneImage()")
+        w, h = self._fb
+        shape = (h, w) if channels is None else (h, w, channels)
+        out = np.empty(shape, dtype)
+        rect = (ctypes.c_int32 * 4)(0, 0, w, h)
+        check(self._lib.gbr_image_into(self._h, int(plane), rect, out.ctypes.data,
+                                       out.strides[0]))
+        return out
+
+    def colorImage(self):
+        """RGBA8 [H, W, 4] (``RendererStandalone::colorImage``, RendererStandalone.cpp:161-166)."""
+        return self._image(Plane.Color, np.uint8, 4)
+
+    def depthImage(self):
+        """Window depth [H, W] float32 (``RendererStandalone::depthImage``, :182-187)."""
+        return self._image(Plane.Depth, np.float32)
+
+    def linearDepthImage(self):
+        """Metres along the view axis, 0 where nothing was drawn."""
+        return self._image(Plane.LinearDepth, np.float32)
+
+    def semanticImage(self):
+        return self._image(Plane.Semantic, np.uint32)
+
+    def _image_into(self, plane, rectangle, image):
+        (x0, y0), (x1, y1) = rectangle
+        if image.shape[0] != y1 - y0 or image.shape[1] != x1 - x0:
+            raise GbrError(1, f"expected image size of {(x1 - x0, y1 - y0)} pixels but got "
+                              f"{(image.shape[1], image.shape[0])}")
+        if not image.flags.c_contiguous:
+            raise GbrError(1, "image must be C-contiguous")
+        rect = (ctypes.c_int32 * 4)(x0, y0, x1, y1)
+        check(self._lib.gbr_image_into(self._h, int(plane), rect, image.ctypes.data,
+                                       image.strides[0]))
+
+    def colorImageInto(self, rectangle, image):
+        """``colorImageInto`` (RendererStandalone.cpp:168-180); rectangle is
+        ((x0, y0), (x1, y1)), image a uint8 [y1-y0, x1-x0, 4] array."""
+        self._image_into(Plane.Color, rectangle, image)
+
+    def depthImageInto(self, rectangle, image):
+        """``depthImageInto`` (RendererStandalone.cpp:189-202)."""
+        self._image_into(Plane.Depth, rectangle, image)
+
+    def linearDepthImageInto(self, rectangle, image):
+        self._image_into(Plane.LinearDepth, rectangle, image)
+
+    def semanticImageInto(self, rectangle, image):
+        self._image_into(Plane.Semantic, rectangle, image)
+
+    def sceneImage(self, plane, sceneId):
+        """One scene's rectangle of a plane (either layout), row 0 = bottom."""
+        _, _, w, h = self.sceneViewport(sceneId)
+        plane = Plane(plane)
+        if plane == Plane.Color:
+            out = np.empty((h, w, 4), np.uint8)
+        elif plane == Plane.Semantic:
+            out = np.empty((h, w), np.uint32)
+        else:
+            out = np.empty((h, w), np.float32)
+        self.sceneImageInto(plane, sceneId, out)
+        return out
+
+    def sceneImageInto(self, plane, sceneId, image):
+        check(self._lib.gbr_scene_image_into(self._h, int(plane), sceneId, image.ctypes.data,
+                                             image.strides[0]))
+
+    # ----------------------------------------------------- device access
+    def planeDevicePointer(self, plane):
+        out = ctypes.c_void_p()
+        n = ctypes.c_uint64()
+        check(self._lib.gbr_plane_device_pointer(self._h, int(plane), ctypes.byref(out),
+                                                 ctypes.byref(n)))
+        return out.value, n.value
+
+    def colorCudaBufferDevicePointer(self):
+        """RendererStandalone.cpp:205-233; the live framebuffer, no copy."""
+        return self.planeDevicePointer(Plane.Color)[0]
+
+    def depthCudaBufferDevicePointer(self):
+        """RendererStandalone.cpp:235-263; returns the depth plane."""
+        return self.planeDevicePointer(Plane.Depth)[0]
+
+    def deviceTensor(self, plane):
+        """A CUDA torch tensor viewing a whole plane (DLPack, no copy).  The
+        tensor keeps the renderer alive; its contents change at each draw."""
+        import torch
+
+        out = ctypes.c_void_p()
+        check(self._lib.gbr_plane_dlpack(self._h, int(plane), ctypes.byref(out)))
+        new = ctypes.pythonapi.PyCapsule_New
+        new.restype = ctypes.py_object
+        new.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+        capsule = new(out, b"dltensor", None)
+        return torch.utils.dlpack.from_dlpack(capsule)
+
+    def colorTensor(self):
+        return self.deviceTensor(Plane.Color)
+
+    def depthTensor(self):
+        return self.deviceTensor(Plane.Depth)
+
+    def linearDepthTensor(self):
+        return self.deviceTensor(Plane.LinearDepth)
+
+    def semanticTensor(self):
+        return self.deviceTensor(Plane.Semantic)
+
+
+def calculateDepthUnprojection(projection):
+    """``calculateDepthUnprojection`` (DepthUnprojection.cpp:98-101)."""
+    p = _f32(projection, (4, 4))
+    return np.array([(p[2, 2] - np.float32(1.0)) * np.float32(0.5),
+                     p[3, 2] * np.float32(0.5)], np.float32)
+
+
+def unprojectDepth(unprojection, depth):
+    """``unprojectDepth`` (DepthUnprojection.cpp:107-129) in place on a
+    float32 [rows, cols] array whose rows may be strided."""
+    lib = _lib.load()
+    u = _f32(unprojection, (2,))
+    if depth.dtype != np.float32 or depth.ndim != 2 or depth.strides[1] != 4:
+        raise ValueError("depth must be a float32 [rows, cols] array with contiguous rows")
+    check(lib.gbr_unproject_depth(_fptr(u), depth.ctypes.data_as(_lib.c_float_p),
+                                  depth.shape[0], depth.shape[1], depth.strides[0] // 4))
+    return depth
+
+
+def unprojectDepthDevice(unprojection, tensor, stream=None):
+    """unprojectDepth on a CUDA float32 [rows, cols] torch tensor, on its GPU."""
+    lib = _lib.load()
+    u = _f32(unprojection, (2,))
+    rows, cols = tensor.shape
+    check(lib.gbr_unproject_depth_device(_fptr(u), tensor.data_ptr(), rows, cols,
+                                         tensor.stride(0), _stream_handle(stream)))
+    return tensor

@@ -1,0 +1,252 @@
+/* gbr.h -- C ABI of the GB300 batch renderer.
+ *
+ * A drop-in for the draw path of habitat-sim's esp::gfx_batch::Renderer /
+ * RendererStandalone (src/esp/gfx_batch/Renderer.h:437-743,
+ * src/esp/gfx_batch/RendererStandalone.h:120-241).  The reference has no C
+ * ABI; each entry point below names the C++ member it replaces.  Plain
+ * pointers and sizes only: no CUDA, torch or STL types cross the boundary.
+ *
+ * Conventions
+ *  - Every call returns gbr_status; on failure gbr_last_error() holds a
+ *    message for the calling thread (the reference asserts or returns false
+ *    with a message: Renderer.cpp:405-427, 883-895).
+ *  - Matrices are 4x4 float, column-major (m[col*4 + row]), as Magnum's
+ *    Matrix4.
+ *  - Images have row 0 at the bottom (GL window origin), as the reference's
+ *    colorImage()/depthImage().
+ *  - One renderer per host thread; gbr_draw is asynchronous on the given
+ *    CUDA stream, the *_image_into readbacks synchronise that stream.
+ */
+#ifndef GBR_H
+#define GBR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gbr_status {
+  GBR_OK = 0,
+  GBR_ERROR_INVALID_ARGUMENT = 1, /* out-of-range scene/node id, bad size  */
+  GBR_ERROR_NOT_FOUND = 2,        /* unknown hierarchy name                */
+  GBR_ERROR_IO = 3,               /* file cannot be opened or parsed       */
+  GBR_ERROR_CUDA = 4,             /* a CUDA runtime call failed            */
+  GBR_ERROR_OUT_OF_MEMORY = 5,    /* device or host allocation failed      */
+  GBR_ERROR_DEVICE = 6,           /* a kernel reported a bad input         */
+  GBR_ERROR_STATE = 7             /* call not valid in the current state   */
+} gbr_status;
+
+typedef struct gbr_renderer gbr_renderer;
+
+/* RendererFlag (Renderer.h:20-30). */
+#define GBR_FLAG_NO_TEXTURES 1u
+/* RendererFileFlag (Renderer.h:120-154). */
+#define GBR_FILE_WHOLE 1u
+#define GBR_FILE_GENERATE_MIPMAP 2u
+/* RendererStandaloneFlag::QuietLog (RendererStandalone.h:21-36). */
+#define GBR_STANDALONE_QUIET_LOG 1u
+
+/* Output planes of the framebuffer. */
+#define GBR_PLANE_COLOR 1u        /* RGBA8, background (31,31,31,255)       */
+#define GBR_PLANE_DEPTH 2u        /* window depth [0,1], D32F, cleared 1.0  */
+#define GBR_PLANE_LINEAR_DEPTH 4u /* metres along -z_eye, background 0      */
+#define GBR_PLANE_SEMANTIC 8u     /* uint32 object id, background 0         */
+#define GBR_PLANE_ALL 15u
+
+/* Draw modes for gbr_draw_mode. */
+#define GBR_DRAW_PER_SCENE 0u /* one prepare + one raster launch per scene */
+#define GBR_DRAW_BATCHED 1u   /* one prepare + one persistent raster launch */
+
+/* RendererConfiguration (Renderer.h:45-113) + RendererStandaloneConfiguration
+ * (RendererStandalone.h:47-100, setCudaDevice at :67), plus the per-scene viewport extension. */
+typedef struct gbr_config {
+  uint32_t flags;            /* GBR_FLAG_*                                  */
+  int32_t tile_size[2];      /* default {128,128}                           */
+  int32_t tile_count[2];     /* default {1,1}                               */
+  uint32_t max_light_count;  /* must be 0 (flat shading); lights not built  */
+  float ambient_factor;      /* default 0.1, used by lit materials only     */
+  int32_t cuda_device;       /* default 0                                   */
+  uint32_t standalone_flags; /* GBR_STANDALONE_*                            */
+  uint32_t planes;           /* GBR_PLANE_* mask, default GBR_PLANE_ALL     */
+  uint32_t draw_mode;        /* GBR_DRAW_*, default GBR_DRAW_PER_SCENE      */
+  /* Ragged layout: if scene_count > 0, scene i renders viewports[2i] x
+   * viewports[2i+1] pixels into its own contiguous block (row pitch = width)
+   * instead of a tile of the tile_size x tile_count grid. */
+  uint32_t scene_count;
+  const int32_t* viewports;
+} gbr_config;
+
+/* Fills *config with the reference defaults. */
+void gbr_config_init(gbr_config* config);
+
+/* RendererStandalone::RendererStandalone (RendererStandalone.cpp:115-135). */
+gbr_status gbr_create(const gbr_config* config, gbr_renderer** out);
+/* RendererStandalone::~RendererStandalone. */
+void gbr_destroy(gbr_renderer* renderer);
+/* Message of the last failed call on this thread ("" if none). */
+const char* gbr_last_error(void);
+
+/* Renderer::tileSize / tileCount / sceneCount (Renderer.cpp:321-331). */
+gbr_status gbr_tile_size_count(gbr_renderer* r, int32_t tile_size[2], int32_t tile_count[2]);
+gbr_status gbr_scene_count(gbr_renderer* r, uint32_t* count);
+/* Framebuffer geometry: for the tile grid {width, height} of the whole image;
+ * for the ragged layout {total pixels, 1}. */
+gbr_status gbr_framebuffer_size(gbr_renderer* r, int64_t size[2]);
+/* Scene rectangle inside its plane: {pixel offset of (0,0), row pitch, width, height}. */
+gbr_status gbr_scene_viewport(gbr_renderer* r, uint32_t scene, int64_t out[4]);
+
+/* Renderer::addFile (Renderer.cpp:337-867): glTF 2.0 (.gltf/.glb) with the
+ * MAGNUMX_mesh_views extras, KHR_texture_ktx (KTX2 RGB8/RGBA8/BC1),
+ * KHR_texture_transform, KHR_materials_unlit, PNG images.  name may be NULL. */
+gbr_status gbr_add_file(gbr_renderer* r, const char* filename, uint32_t file_flags,
+                        const char* name);
+
+/* Procedural resources: the pieces addFile creates from a file, for callers
+ * that generate geometry (no reference counterpart; they mirror the imported
+ * MeshData / TextureData / MaterialData of Renderer.cpp:410-633). */
+typedef struct gbr_mesh_data {
+  uint32_t vertex_count;
+  const float* positions;     /* 3 per vertex                               */
+  const float* colors;        /* 4 per vertex (RGBA in [0,1]) or NULL       */
+  const float* texcoords;     /* 2 per vertex (Y-up texture space) or NULL  */
+  const uint32_t* object_ids; /* 1 per vertex or NULL                       */
+  uint32_t index_count;
+  const uint32_t* indices;    /* triangle list                              */
+} gbr_mesh_data;
+gbr_status gbr_add_mesh(gbr_renderer* r, const gbr_mesh_data* mesh, uint32_t* out_mesh_id);
+
+typedef struct gbr_texture_data {
+  int32_t width, height, layers;
+  const uint8_t* rgba8;       /* layers*height*width*4 bytes, row 0 bottom  */
+  int32_t filter;             /* 0 nearest, 1 bilinear                      */
+  int32_t wrap_s, wrap_t;     /* 0 repeat, 1 clamp to edge, 2 mirrored      */
+} gbr_texture_data;
+gbr_status gbr_add_texture(gbr_renderer* r, const gbr_texture_data* texture,
+                           uint32_t* out_texture_id);
+
+typedef struct gbr_material_data {
+  float color[4];             /* flat base colour                           */
+  uint32_t texture;           /* texture id, 0 = the reserved white texel   */
+  uint32_t layer;             /* array layer                                */
+  float matrix[9];            /* 3x3 texture matrix, column-major           */
+} gbr_material_data;
+gbr_status gbr_add_material(gbr_renderer* r, const gbr_material_data* material,
+                            uint32_t* out_material_id);
+
+typedef struct gbr_mesh_view {
+  uint32_t mesh;
+  uint32_t index_offset;      /* in indices (the reference stores bytes)    */
+  uint32_t index_count;
+  uint32_t material;
+  float transform[16];
+} gbr_mesh_view;
+/* Registers a named node-hierarchy template, as a named root node of a
+ * composite file does (Renderer.cpp:750-790). */
+gbr_status gbr_add_node_hierarchy_template(gbr_renderer* r, const char* name,
+                                           uint32_t view_count, const gbr_mesh_view* views);
+
+/* Renderer::hasNodeHierarchy (Renderer.cpp:869-878). */
+gbr_status gbr_has_node_hierarchy(gbr_renderer* r, const char* name, int32_t* out);
+/* Renderer::addNodeHierarchy (Renderer.cpp:880-961); bake may be NULL. */
+gbr_status gbr_add_node_hierarchy(gbr_renderer* r, uint32_t scene, const char* name,
+                                  const float bake[16], uint64_t* out_node_id);
+/* Renderer::addEmptyNode (Renderer.cpp:968-988). */
+gbr_status gbr_add_empty_node(gbr_renderer* r, uint32_t scene, uint64_t* out_node_id);
+/* Renderer::clear (Renderer.cpp:1017-1040). */
+gbr_status gbr_clear(gbr_renderer* r, uint32_t scene);
+/* Semantic id of every draw added by the addNodeHierarchy call that
+ * returned node (no reference counterpart: gfx_batch draws no ids; the
+ * classic renderer's per-draw object id, src/esp/gfx/GenericDrawable.cpp:112). */
+gbr_status gbr_set_semantic_id(gbr_renderer* r, uint32_t scene, uint64_t node, uint32_t id);
+
+/* Renderer::updateCamera (Renderer.cpp:1077-1088). */
+gbr_status gbr_update_camera(gbr_renderer* r, uint32_t scene, const float projection[16],
+                             const float view[16]);
+/* updateCamera for scenes first..first+count-1 in one call: projections
+ * and views hold 16 floats per scene (the batched form's per-step poses). */
+gbr_status gbr_update_cameras(gbr_renderer* r, uint32_t first, uint32_t count,
+                              const float* projections, const float* views);
+/* Renderer::camera (Renderer.cpp:1056-1064): P*V. */
+gbr_status gbr_camera(gbr_renderer* r, uint32_t scene, float out[16]);
+/* Renderer::cameraDepthUnprojection (Renderer.cpp:1066-1075). */
+gbr_status gbr_camera_depth_unprojection(gbr_renderer* r, uint32_t scene, float out[2]);
+/* Renderer::transformations (Renderer.cpp:1090-1099): a writable view of
+ * the scene's local node transforms (16 floats each), valid until the next
+ * add/clear on that scene.  Taking the view marks the scene's transforms
+ * for upload at the next draw. */
+gbr_status gbr_transformations(gbr_renderer* r, uint32_t scene, float** out, uint64_t* count);
+
+/* RendererStandalone::draw (RendererStandalone.cpp:155-159) + Renderer::draw
+ * (Renderer.cpp:1123-1354).  stream is a cudaStream_t (NULL = default). */
+gbr_status gbr_draw(gbr_renderer* r, void* stream);
+/* Same with an explicit GBR_DRAW_* mode; use_graph captures the batched
+ * step into a CUDA graph and replays it while the scene structure and the
+ * stream stay the same. */
+gbr_status gbr_draw_mode(gbr_renderer* r, void* stream, uint32_t mode, int32_t use_graph);
+
+/* Renderer::sceneStats (Renderer.cpp:1356-1375). */
+typedef struct gbr_scene_stats_info {
+  uint64_t node_count, draw_count, draw_batch_count;
+} gbr_scene_stats_info;
+gbr_status gbr_scene_stats(gbr_renderer* r, uint32_t scene, gbr_scene_stats_info* out);
+
+/* RendererStandalone::colorImageInto / depthImageInto
+ * (RendererStandalone.cpp:168-180, 189-202): copy rect {x0, y0, x1, y1} of a plane
+ * of the tile-grid framebuffer into host memory with the given row pitch.
+ * plane is one GBR_PLANE_* bit.  For the ragged layout use
+ * gbr_scene_image_into. */
+gbr_status gbr_image_into(gbr_renderer* r, uint32_t plane, const int32_t rect[4], void* dst,
+                          uint64_t dst_row_bytes);
+gbr_status gbr_color_image_into(gbr_renderer* r, const int32_t rect[4], void* dst,
+                                uint64_t dst_row_bytes);
+gbr_status gbr_depth_image_into(gbr_renderer* r, const int32_t rect[4], void* dst,
+                                uint64_t dst_row_bytes);
+/* One scene's rectangle of a plane (either layout), rows bottom-up. */
+gbr_status gbr_scene_image_into(gbr_renderer* r, uint32_t plane, uint32_t scene, void* dst,
+                                uint64_t dst_row_bytes);
+
+/* RendererStandalone::colorCudaBufferDevicePointer / depthCudaBufferDevicePointer
+ * (RendererStandalone.cpp:205-263): the device address of a whole plane,
+ * owned by the renderer, valid until it is destroyed.  Unlike the reference
+ * this is the live framebuffer (no copy) and the depth call returns depth. */
+gbr_status gbr_plane_device_pointer(gbr_renderer* r, uint32_t plane, void** out,
+                                    uint64_t* bytes);
+
+/* DLPack export of a plane (DLManagedTensor*, dlpack v0.x ABI): a kDLCUDA
+ * tensor of shape [H, W] (tile grid) or [N] (ragged); colour as uint8
+ * [H, W, 4] / [N, 4].  The tensor keeps the renderer alive. */
+gbr_status gbr_plane_dlpack(gbr_renderer* r, uint32_t plane, void** out_managed_tensor);
+
+/* unprojectDepth (src/esp/gfx_batch/DepthUnprojection.cpp:107-129) on host
+ * memory, and its device counterpart on the given stream. */
+gbr_status gbr_unproject_depth(const float unprojection[2], float* depth, uint64_t rows,
+                               uint64_t cols, uint64_t row_stride);
+gbr_status gbr_unproject_depth_device(const float unprojection[2], float* depth, uint64_t rows,
+                                      uint64_t cols, uint64_t row_stride, void* stream);
+
+/* Tuning of the raster kernel (chosen by the autotuner). */
+typedef struct gbr_tuning {
+  int32_t threads;        /* threads per CTA: 256, 512 or 1024              */
+  int32_t region_width;   /* max pixels per CTA region, x (multiple of 4)   */
+  int32_t region_height;  /* max pixels per CTA region, y                   */
+  int32_t small_area;     /* bounding boxes up to this many pixels are
+                             rasterised by one thread, larger ones by the
+                             whole CTA from a shared-memory bin            */
+  int32_t ctas_per_sm;    /* persistent grid = SMs x this                   */
+} gbr_tuning;
+gbr_status gbr_get_tuning(gbr_renderer* r, gbr_tuning* out);
+gbr_status gbr_set_tuning(gbr_renderer* r, const gbr_tuning* tuning);
+
+/* Counters of the last draw (host-read after the stream is synchronised). */
+typedef struct gbr_draw_stats {
+  uint64_t scenes, draws, visible_draws, triangles; /* triangles of visible draws */
+  uint64_t kernel_launches;
+} gbr_draw_stats;
+gbr_status gbr_last_draw_stats(gbr_renderer* r, gbr_draw_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBR_H */

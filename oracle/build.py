@@ -5,11 +5,12 @@ rounded unless the source spells out ``std::fmaf``; the same rule holds on
 x86-64 and on aarch64 (where GCC would otherwise contract to FMA)."""
 import ctypes
 import os
+import platform
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
-LIB = os.path.join(BUILD, "liboracle.so")
+LIB = os.path.join(BUILD, f"liboracle.{platform.machine()}.so")
 SRC = os.path.join(HERE, "raster.cpp")
 
 _lib = None

@@ -337,3 +337,23 @@ def unproject_depth(unprojection, depth):
     lib.oracle_unproject_depth(a.ctypes.data, depth.ctypes.data, depth.shape[0], depth.shape[1],
                                depth.shape[1])
     return depth
+
+
+# Procedural call surface shared with the GPU renderer's Python API.
+OracleRenderer.addMesh = lambda self, positions, colors=None, texcoords=None, objectIds=None, \
+    indices=None: self.add_mesh(positions, colors, texcoords, objectIds, indices)
+OracleRenderer.addTexture = lambda self, pixels, filter=1, wrapS=0, wrapT=0: \
+    self.add_texture(pixels, filter, wrapS, wrapT)
+OracleRenderer.addMaterial = lambda self, color=(1, 1, 1, 1), texture=0, layer=0, matrix=None: \
+    self.add_material(color, texture, layer, matrix)
+OracleRenderer.addNodeHierarchyTemplate = lambda self, name, views: \
+    self.add_node_hierarchy_template(name, views)
+OracleRenderer.setSemanticId = lambda self, scene, node, sid: self.set_semantic_id(scene, node, sid)
+
+
+def _update_cameras(self, projections, views, first=0):
+    for i, (p, v) in enumerate(zip(projections, views)):
+        self.updateCamera(first + i, p, v)
+
+
+OracleRenderer.updateCameras = _update_cameras

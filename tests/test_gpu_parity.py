@@ -1,0 +1,312 @@
+"""CUDA renderer vs the CPU oracle, through the C ABI (GPU tests).
+
+* every golden scenario of habitat-sim's GfxBatchRendererTest, in the
+  per-scene and the batched draw modes, against the reference screenshots
+  and bit for bit against the oracle;
+* seeded procedural workloads (the benchmark configurations at test sizes,
+  and the full 1024-env configuration through size-independent properties);
+* clipping edge cases, empty and cleared scenes, determinism, DLPack views,
+  readback rectangles, device depth unprojection, error reporting.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as graft
+import scenarios as S
+from parity import assert_parity, compare_scene
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return graft.load_package()
+
+
+@pytest.fixture(scope="module")
+def procedural(pkg):
+    from habitat_sim_gb300 import procedural
+    return procedural
+
+
+def gpu_factory(pkg, mode):
+    def make(tile_size, tile_count, flags):
+        cfg = (pkg.RendererConfiguration().setTileSizeCount(tile_size, tile_count)
+               .setFlags(flags).setDrawMode(mode))
+        return pkg.RendererStandalone(cfg, pkg.RendererStandaloneConfiguration().setFlags(
+            pkg.RendererStandaloneFlags.QuietLog))
+    return make
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["per_scene", "batched"])
+@pytest.mark.parametrize("case", range(len(S.ALL)), ids=S.ids())
+def test_golden(pkg, case, mode):
+    from oracle.model import OracleRenderer
+    _, fn, data = S.ALL[case]
+    made = []
+
+    def make(tile_size, tile_count, flags):
+        r = gpu_factory(pkg, mode)(tile_size, tile_count, flags)
+        made.append(r)
+        return r
+    fails = S.evaluate(fn(make, data))
+    assert not fails, fails
+    # Bit-exact against the oracle running the same scenario.
+    oracle_checks = fn(lambda ts, tc, fl: OracleRenderer(ts, tc, fl), data)
+    gpu_checks = fn(gpu_factory(pkg, mode), data)
+    for g, c in zip(gpu_checks, oracle_checks):
+        if g.kind == "image":
+            assert np.array_equal(g.image, c.image), g.golden
+
+
+def test_depth_unprojection_scene(pkg):
+    fails = S.evaluate(S.depth_unprojection(gpu_factory(pkg, 1), pkg.unprojectDepth))
+    assert not fails, fails
+
+
+def _parity(pkg, procedural, wl, envs=None, modes=(0, 1), graph=False, steps=(0,),
+            require_exact=True):
+    from oracle.model import OracleRenderer
+    gpu = procedural.build_renderer(pkg, wl, envs=envs)
+    cpu = procedural.build_oracle(OracleRenderer, wl, envs=envs)
+    n = gpu.sceneCount()
+    results = []
+    for step in steps:
+        poses = procedural.camera_poses(wl, step)
+        procedural.set_cameras(gpu, wl, poses, envs)
+        procedural.set_cameras(cpu, wl, poses, envs)
+        cpu.draw(threads=8)
+        for mode in modes:
+            gpu.draw(mode=mode, graph=graph and mode == 1)
+            results += [compare_scene(gpu, cpu, pkg, s) for s in range(n)]
+    assert_parity(results, require_exact)
+    return gpu, cpu
+
+
+def test_config0_full(pkg, procedural):
+    """16 envs, 128^2, the 49k-triangle room + 20 boxes, two pose sets."""
+    wl = procedural.config0()
+    _parity(pkg, procedural, wl, steps=(0, 1))
+
+
+def test_config0_graph(pkg, procedural):
+    wl = procedural.config0(envs=8)
+    _parity(pkg, procedural, wl, modes=(1,), graph=True, steps=(0, 1, 2))
+
+
+def test_config1_subset(pkg, procedural):
+    """Textured instancing: 8 of the 1024 envs (two per scene) at full detail."""
+    wl = procedural.config1(envs=1024)
+    _parity(pkg, procedural, wl, envs=[0, 1, 2, 3, 512, 513, 1022, 1023])
+
+
+def test_ragged_mixed_resolution(pkg, procedural):
+    """Per-env resolution from {64,128,256}^2 and hfov U(60,110) in one batch."""
+    wl = procedural.config2(envs=24, scenes=3, tri_range=(2e4, 1.5e5))
+    _parity(pkg, procedural, wl)
+
+
+def look_view(x, y, z, yaw, pitch):
+    """View matrix ([col][row] float32) of a camera at (x, y, z) turned by yaw
+    about +y, then pitch about its x axis."""
+    cy, sy, cp, sp = math.cos(yaw), math.sin(yaw), math.cos(pitch), math.sin(pitch)
+    ry = np.array([[cy, 0, sy, 0], [0, 1, 0, 0], [-sy, 0, cy, 0], [0, 0, 0, 1]])
+    rx = np.array([[1, 0, 0, 0], [0, cp, -sp, 0], [0, sp, cp, 0], [0, 0, 0, 1]])
+    t = np.eye(4)
+    t[:3, 3] = [x, y, z]
+    cam_to_world = t @ ry @ rx
+    return np.linalg.inv(cam_to_world).T.astype(np.float32)
+
+
+def _wall_hugging_workload(procedural):
+    wl = procedural.config0(seed=11, envs=6, resolution=96, room_subdiv=8, boxes=4)
+    return wl
+
+
+def test_near_plane_and_guard_band(pkg, procedural):
+    """Cameras 1-5 mm from walls and inside boxes: triangles cross the near
+    plane and project far outside the viewport (clipping paths)."""
+    from oracle.model import OracleRenderer
+    wl = _wall_hugging_workload(procedural)
+    gpu = procedural.build_renderer(pkg, wl)
+    cpu = procedural.build_oracle(OracleRenderer, wl)
+    projs, views = procedural.camera_poses(wl, 0)
+    spots = [(-3.999, 1.0, 0.0, 0.3), (3.995, 2.999, 3.9, 2.0), (0.0, 0.005, 0.0, 1.0),
+             (0.0, 1.25, -3.998, math.pi), (2.0, 1.0, 3.999, 0.01), (-3.99, 0.002, -3.99, 0.8)]
+    for e, (x, y, z, yaw) in enumerate(spots):
+        views[e] = look_view(x, y, z, yaw, -1.0 if e % 2 else 0.0)
+    gpu.updateCameras(projs, views)
+    cpu.updateCameras(projs, views)
+    cpu.draw()
+    results = []
+    for mode in (0, 1):
+        gpu.draw(mode=mode)
+        results += [compare_scene(gpu, cpu, pkg, s) for s in range(wl.envs)]
+    assert_parity(results)
+
+
+def test_huge_triangle_guard_band(pkg):
+    """A 2-triangle quad 1e5 m wide crossing the near plane and the guard band."""
+    from oracle.model import OracleRenderer
+    pos = np.array([[-1e5, -1, -1e5], [1e5, -1, -1e5], [1e5, -1, 1e5], [-1e5, -1, 1e5]],
+                   np.float32)
+    col = np.array([[1, 0, 0, 1], [0, 1, 0, 1], [0, 0, 1, 1], [1, 1, 1, 1]], np.float32)
+    idx = np.array([0, 3, 2, 0, 2, 1], np.uint32)  # faces +y
+    proj = S.perspective(90.0, 1.0, 0.01, 10.0)
+    outs = []
+    for r in (gpu_factory(pkg, 1)((64, 64), (2, 1), 0), OracleRenderer((64, 64), (2, 1), 0)):
+        m = r.addMesh(pos, col, None, None, idx)
+        r.addNodeHierarchyTemplate("floor", [(m, 0, 6, 0, None)])
+        for s in range(2):
+            r.addNodeHierarchy(s, "floor")
+        r.updateCamera(0, proj, S.translation(0.0, 0.0, 0.0))
+        tilt = np.eye(4, dtype=np.float32)
+        c, s_ = np.float32(math.cos(0.7)), np.float32(math.sin(0.7))
+        tilt[1, 1], tilt[1, 2], tilt[2, 1], tilt[2, 2] = c, s_, -s_, c
+        r.updateCamera(1, proj, tilt)
+        r.draw()
+        outs.append(r)
+    gpu, cpu = outs
+    res = [compare_scene(gpu, cpu, pkg, s) for s in range(2)]
+    assert_parity(res)
+    assert (gpu.colorImage()[..., 3] == 255).all()
+
+
+def test_empty_and_cleared_scenes(pkg, procedural):
+    wl = procedural.config0(seed=3, envs=4, resolution=32, room_subdiv=4, boxes=2)
+    gpu = procedural.build_renderer(pkg, wl)
+    procedural.set_cameras(gpu, wl, procedural.camera_poses(wl, 0))
+    gpu.clear(1)
+    gpu.clear(3)
+    gpu.draw()
+    for s in (1, 3):
+        assert (gpu.sceneImage(pkg.Plane.Color, s).view(np.uint32) == 0xFF1F1F1F).all()
+        assert (gpu.sceneImage(pkg.Plane.Depth, s) == 1.0).all()
+        assert (gpu.sceneImage(pkg.Plane.LinearDepth, s) == 0.0).all()
+        assert (gpu.sceneImage(pkg.Plane.Semantic, s) == 0).all()
+    assert (gpu.sceneImage(pkg.Plane.Semantic, 0) > 0).any()
+
+
+def test_no_file_added(pkg):
+    """renderNoFileAdded (GfxBatchRendererTest.cpp:1724-1735)."""
+    r = gpu_factory(pkg, 0)((64, 48), (2, 2), 0)
+    r.draw()
+    assert (r.colorImage().reshape(-1, 4) == [31, 31, 31, 255]).all()
+
+
+def test_deterministic_and_modes_agree(pkg, procedural):
+    wl = procedural.config1(envs=16, instances=60)
+    gpu = procedural.build_renderer(pkg, wl)
+    procedural.set_cameras(gpu, wl, procedural.camera_poses(wl, 5))
+    imgs = []
+    for mode, graph in ((0, False), (1, False), (1, True), (1, True)):
+        gpu.draw(mode=mode, graph=graph)
+        imgs.append((gpu.colorImage(), gpu.linearDepthImage(), gpu.semanticImage()))
+    for other in imgs[1:]:
+        for a, b in zip(imgs[0], other):
+            assert np.array_equal(a, b)
+
+
+def test_dlpack_and_device_pointers(pkg, procedural):
+    import torch
+    wl = procedural.config0(seed=5, envs=4, resolution=64, room_subdiv=8, boxes=3)
+    gpu = procedural.build_renderer(pkg, wl)
+    procedural.set_cameras(gpu, wl, procedural.camera_poses(wl, 0))
+    gpu.draw(stream=torch.cuda.current_stream())
+    col = gpu.colorTensor()
+    assert col.is_cuda and col.dtype == torch.uint8 and tuple(col.shape) == (128, 128, 4)
+    assert np.array_equal(col.cpu().numpy(), gpu.colorImage())
+    assert np.array_equal(gpu.linearDepthTensor().cpu().numpy(), gpu.linearDepthImage())
+    assert np.array_equal(gpu.semanticTensor().cpu().numpy().astype(np.uint32),
+                          gpu.semanticImage())
+    ptr = gpu.colorCudaBufferDevicePointer()
+    assert ptr == col.data_ptr()
+    dep = gpu.depthTensor()
+    assert gpu.depthCudaBufferDevicePointer() == dep.data_ptr()
+    expected = gpu.colorImage().copy()
+    gpu.close()  # the tensor keeps the renderer's memory alive
+    assert np.array_equal(col.cpu().numpy(), expected)
+
+
+def test_image_into_rectangles(pkg, procedural):
+    wl = procedural.config0(seed=6, envs=4, resolution=48, room_subdiv=8, boxes=3)
+    gpu = procedural.build_renderer(pkg, wl)
+    procedural.set_cameras(gpu, wl, procedural.camera_poses(wl, 0))
+    gpu.draw()
+    full = gpu.colorImage()
+    part = np.empty((20, 30, 4), np.uint8)
+    gpu.colorImageInto(((10, 5), (40, 25)), part)
+    assert np.array_equal(part, full[5:25, 10:40])
+    dpart = np.empty((48, 48), np.float32)
+    gpu.depthImageInto(((48, 48), (96, 96)), dpart)
+    assert np.array_equal(dpart, gpu.depthImage()[48:96, 48:96])
+    with pytest.raises(pkg.GbrError):
+        gpu.colorImageInto(((0, 0), (97, 10)), np.empty((10, 97, 4), np.uint8))
+
+
+def test_unproject_device_matches_host(pkg):
+    import torch
+    p = S.perspective(60.0, 1.0, 0.01, 10.0)
+    u = pkg.calculateDepthUnprojection(p)
+    d = torch.rand(64, 80, device="cuda")
+    d[::7, ::5] = 1.0
+    host = d.cpu().numpy().copy()
+    pkg.unprojectDepthDevice(u, d)
+    torch.cuda.synchronize()
+    pkg.unprojectDepth(u, host)
+    assert np.array_equal(d.cpu().numpy().view(np.uint32), host.view(np.uint32))
+
+
+def test_errors(pkg, procedural):
+    r = gpu_factory(pkg, 0)((32, 32), (1, 1), 0)
+    assert r.addFile("/nonexistent/file.gltf") is False
+    with pytest.raises(pkg.GbrError) as e:
+        r.addNodeHierarchy(0, "nothing")
+    assert e.value.status == 2
+    with pytest.raises(pkg.GbrError) as e:
+        r.addNodeHierarchy(5, "nothing")
+    assert e.value.status == 1
+    with pytest.raises(pkg.GbrError):
+        r.addMesh(np.zeros((3, 3)), indices=np.array([0, 1, 3]))
+    with pytest.raises(pkg.GbrError):
+        r.setTuning(threads=100)
+
+
+def test_config1_full_size_properties(pkg, procedural):
+    """All 1024 envs of the textured-instancing workload in one batched
+    step: every pixel written, ids and depths in range, the batched output
+    equals the per-scene output, and sampled envs equal the oracle."""
+    from oracle.model import OracleRenderer
+    wl = procedural.config1()
+    gpu = procedural.build_renderer(pkg, wl, mode=1)
+    poses = procedural.camera_poses(wl, 3)
+    procedural.set_cameras(gpu, wl, poses)
+    gpu.draw(mode=1, graph=True)
+    col, lin, sem = gpu.colorImage(), gpu.linearDepthImage(), gpu.semanticImage()
+    valid_ids = (sem == 0) | (sem == 1) | ((sem >= 1000) & (sem < 1200))
+    assert valid_ids.all()
+    assert ((lin == 0) | ((lin >= 0.0099) & (lin <= 10.0))).all()
+    assert ((sem == 0) == (lin == 0)).all()
+    gpu.draw(mode=0)
+    assert np.array_equal(col, gpu.colorImage())
+    assert np.array_equal(sem, gpu.semanticImage())
+    sample = [0, 137, 500, 1023]
+    cpu = procedural.build_oracle(OracleRenderer, wl, envs=sample)
+    procedural.set_cameras(cpu, wl, poses, sample)
+    cpu.draw(threads=8)
+    res = []
+    for slot, e in enumerate(sample):
+        _, _, w, h = gpu.sceneViewport(e)
+        for plane, arr in ((pkg.Plane.Color, cpu.color), (pkg.Plane.LinearDepth, cpu.linear_depth),
+                           (pkg.Plane.Semantic, cpu.semantic)):
+            g = gpu.sceneImage(plane, e)
+            c = cpu.scene_image(arr, slot)
+            if plane == pkg.Plane.Color:
+                c = c.view(np.uint8).reshape(g.shape)
+            res.append(np.array_equal(g, c))
+    assert all(res), res
