@@ -1,0 +1,395 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 batch renderer on the textured-instancing workload.
+
+One step renders every env of the workload once: 1024 envs over 4
+procedural scenes (20k-triangle room + 200 textured instances each), 128 x 128
+RGBA8 + FP32 linear depth + uint32 semantic id per env, fresh camera poses
+every step (uploaded from host memory inside the step).
+
+Printed (rank 0, one JSON line):
+  value        frames/s of the batched form (one prepare + one persistent
+               raster launch per step, replayed from a CUDA graph), geometry
+               and textures resident in HBM, L2 flushed before every step
+               (a 256 MiB write outside the timed events); each step timed
+               with CUDA events on the launching stream;
+  plain        the same workload through the plain per-scene path (two
+               launches per env, no graph);
+  e2e          the same metric through the C ABI with host buffers: poses
+               from host arrays, framebuffer (colour, linear depth, ids) read
+               back into pinned host memory by the imageInto calls;
+  roofline     the raster kernel against measured HBM bandwidth, bytes = the
+               framebuffer written plus the unique geometry and textures;
+  cpu_baseline the CPU oracle (the renderer restated in C++) on a bounded
+               sample of the same envs, all host threads;
+  parity       sampled envs of the timed workload against the oracle.
+
+``--impl reference`` times the CPU restatement alone on this workload (the
+reference renderer itself is GL-only and cannot run here)."""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "128² RGBD frames/s on 1 GB300, batched vs plain; p50/p99 ms at ≤1e-4 m depth err"
+WORKLOAD = ("config1 textured instancing: 1024 envs over 4 procedural scenes, each a "
+            "20,172-triangle room shell + 200 instances of 16 prototypes (500-5k tris, 512x512x16 "
+            "RGBA8 noise texture array, bilinear), 128x128 pinhole hfov 90, near 0.01 far 10")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--plain-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--envs", type=int, default=1024)
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ------------------------------------------------------------- workload
+def load_workload(envs):
+    import __graft_entry__ as graft
+    pkg = graft.build()
+    from habitat_sim_gb300 import procedural
+    wl = procedural.config1(envs=envs)
+    return pkg, procedural, wl
+
+
+def algorithmic_bytes(wl):
+    px = sum(w * h for (w, h) in wl.viewports)
+    fb = px * 12   # RGBA8 + FP32 linear depth + uint32 id
+    return fb, wl.geometry_bytes()
+
+
+def cpu_frames_per_s(procedural, wl, seconds, threads):
+    """The oracle on host cores over a growing sample of envs until the time budget."""
+    from oracle.model import OracleRenderer
+    n = 8
+    best = None
+    t_total = 0.0
+    while True:
+        envs = list(range(min(n, wl.envs)))
+        cpu = procedural.build_oracle(OracleRenderer, wl, envs=envs)
+        procedural.set_cameras(cpu, wl, procedural.camera_poses(wl, 0), envs)
+        t0 = time.perf_counter()
+        cpu.draw(threads=threads, window_depth=False)
+        dt = time.perf_counter() - t0
+        t_total += dt
+        best = (len(envs), dt)
+        if dt * 2.5 + t_total > seconds or len(envs) >= wl.envs:
+            break
+        n *= 2
+    return best[0] / best[1], best[0], best[1]
+
+
+def run_reference_impl(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    import __graft_entry__ as graft
+    graft.load_package()
+    from oracle import build as oracle_build
+    oracle_build.build()
+    from habitat_sim_gb300 import procedural
+    from oracle.model import OracleRenderer
+    wl = procedural.config1(envs=args.envs)
+    threads = os.cpu_count() or 1
+    # Size one step so that warmup + steps end within a few minutes.
+    fps, n, dt = cpu_frames_per_s(procedural, wl, min(args.cpu_seconds, 8.0), threads)
+    per_step_envs = max(1, min(wl.envs, int(fps * 4.0)))
+    envs = list(range(per_step_envs))
+    cpu = procedural.build_oracle(OracleRenderer, wl, envs=envs)
+    times = []
+    for i in range(args.warmup + args.steps):
+        procedural.set_cameras(cpu, wl, procedural.camera_poses(wl, i), envs)
+        t0 = time.perf_counter()
+        cpu.draw(threads=threads, window_depth=False)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    value = per_step_envs * len(times) / sum(times)
+    ms = [t * 1e3 for t in times]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(ms), "p50_ms": float(np.percentile(ms, 50)),
+        "p99_ms": float(np.percentile(ms, 99)), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "envs_per_step": per_step_envs,
+                   "sample": f"first {per_step_envs} of {wl.envs} envs per step"},
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": f"{per_step_envs} envs per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": ("the reference renderer is OpenGL-only (no GL, EGL or software rasteriser on "
+                 "this machine); this arm times the C++ restatement of its draw path"),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference_impl(args)
+    rank, local_rank, world = dist_env()
+    import torch
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    pkg, procedural, wl = load_workload(args.envs)
+    planes = pkg.Plane.Color | pkg.Plane.LinearDepth | pkg.Plane.Semantic
+    r = procedural.build_renderer(pkg, wl, mode=pkg.DrawMode.Batched, planes=planes)
+    r.setKernelTiming(True)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    steps = args.warmup + args.steps
+    poses = [procedural.camera_poses(wl, i) for i in range(steps)]
+
+    def batched_step(i, events=None):
+        flush.zero_()
+        r.updateCameras(*poses[i % steps])
+        if events:
+            events[0].record(stream)
+        r.draw(stream=stream, mode=pkg.DrawMode.Batched, graph=True)
+        if events:
+            events[1].record(stream)
+
+    for i in range(args.warmup):
+        batched_step(i)
+    torch.cuda.synchronize()
+
+    # ---- timed batched steps
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms, raster_ms, prepare_ms = [], [], []
+    tri = None
+    for k in range(args.steps):
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        batched_step(args.warmup + k, ev)
+        st = r.lastDrawStats()          # synchronises the stream
+        step_ms.append(ev[0].elapsed_time(ev[1]))
+        raster_ms.append(st["raster_ms"])
+        prepare_ms.append(st["prepare_ms"])
+        tri = st["triangles"]
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    frames = wl.envs * args.steps * world
+    value = frames / (total_ms / 1e3)
+
+    # ---- plain per-scene path
+    plain_ms = []
+    for k in range(args.plain_steps + 1 if args.plain_steps else 0):
+        r.updateCameras(*poses[k % steps])
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r.draw(stream=stream, mode=pkg.DrawMode.PerScene)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if k > 0:
+            plain_ms.append(e0.elapsed_time(e1))
+    plain_fps = wl.envs * len(plain_ms) / (sum(plain_ms) / 1e3) if plain_ms else None
+
+    # ---- end to end through the C ABI with host buffers
+    fbw, fbh = r.framebufferSize()
+    host_color = torch.empty((fbh, fbw, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    host_lin = torch.empty((fbh, fbw), dtype=torch.float32, pin_memory=True).numpy()
+    host_sem = torch.empty((fbh, fbw), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    rect = ((0, 0), (fbw, fbh))
+    e2e_s = []
+    for k in range(args.e2e_steps + 1 if args.e2e_steps else 0):
+        projs, views = poses[k % steps]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.updateCameras(projs, views)
+        r.draw(stream=stream, mode=pkg.DrawMode.Batched, graph=True)
+        r.colorImageInto(rect, host_color)
+        r.linearDepthImageInto(rect, host_lin)
+        r.semanticImageInto(rect, host_sem)
+        t1 = time.perf_counter()
+        if k > 0:
+            e2e_s.append(t1 - t0)
+    e2e_fps = wl.envs * len(e2e_s) / sum(e2e_s) if e2e_s else None
+    h2d = wl.envs * 2 * 64
+    d2h = host_color.nbytes + host_lin.nbytes + host_sem.nbytes
+
+    # ---- parity of sampled envs against the oracle (last e2e step's poses)
+    parity = None
+    if rank == 0 and e2e_s:
+        from oracle.model import OracleRenderer
+        sample = [0, 1, 2, 3, wl.envs // 2 + 1, wl.envs - 1]
+        cpu = procedural.build_oracle(OracleRenderer, wl, envs=sample)
+        procedural.set_cameras(cpu, wl, poses[args.e2e_steps % steps], sample)
+        cpu.draw(threads=os.cpu_count() or 1)
+        mism, max_err, px = 0, 0.0, 0
+        for slot, e in enumerate(sample):
+            off, pitch, w, h = r.sceneViewport(e)
+            y0, x0 = off // pitch, off % pitch
+            g_col = host_color[y0:y0 + h, x0:x0 + w]
+            g_lin = host_lin[y0:y0 + h, x0:x0 + w]
+            g_sem = host_sem[y0:y0 + h, x0:x0 + w]
+            c_col = cpu.scene_image(cpu.color, slot).view(np.uint8).reshape(h, w, 4)
+            c_lin = cpu.scene_image(cpu.linear_depth, slot)
+            c_sem = cpu.scene_image(cpu.semantic, slot)
+            same = (g_col == c_col).all(-1) & (g_sem == c_sem)
+            mism += int((~same).sum())
+            px += same.size
+            if same.any():
+                max_err = max(max_err, float(np.abs(g_lin[same].astype(np.float64) -
+                                                    c_lin[same]).max()))
+        parity = {"envs_checked": len(sample), "pixels": px, "mismatched_pixels": mism,
+                  "max_linear_depth_err_m": max_err, "depth_tolerance_m": 1e-4}
+
+    # ---- roofline of the raster kernel
+    fb_bytes, geo_bytes = algorithmic_bytes(wl)
+    launch_bytes = fb_bytes + geo_bytes
+    raster_avg_ms = statistics.mean(raster_ms)
+    achieved = launch_bytes / (raster_avg_ms / 1e3) / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "raster_kernel_config1.txt")
+    if os.path.exists(tpath):
+        for line in open(tpath):
+            if line.startswith("dram_bytes_per_launch:"):
+                traffic = float(line.split(":")[1])
+
+    cpu_baseline = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        fps, n, dt = cpu_frames_per_s(procedural, wl, args.cpu_seconds, threads)
+        cpu_baseline = {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                        "sample": f"first {n} of {wl.envs} envs, one step, {dt:.2f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.mean(step_ms),
+            "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "envs": wl.envs, "resolution": 128,
+                       "planes": "rgba8 + f32 linear depth + u32 semantic id",
+                       "form": "batched: prepare + persistent raster per step, CUDA graph",
+                       "l2": "flushed with a 256 MiB write before every step (outside timing)",
+                       "triangles_per_step_after_draw_culling": tri,
+                       "triangles_per_step_before_culling": int(wl.triangles_per_env().sum()),
+                       "tuning": r.tuning()},
+            "plain": None if not plain_ms else {
+                "value": plain_fps, "unit": "frames/s", "ms_per_step": statistics.mean(plain_ms),
+                "p50_ms": float(np.percentile(plain_ms, 50)),
+                "p99_ms": float(np.percentile(plain_ms, 99)),
+                "form": "per-scene prepare + raster launches (2 per env), no graph"},
+            "batched_over_plain": value / plain_fps if plain_fps else None,
+            "e2e": None if not e2e_s else {
+                "value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * statistics.mean(e2e_s),
+                "timing": "host clock around updateCameras + draw + 3 imageInto readbacks"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": peak_src, "kernel": "raster_kernel",
+                         "bytes_per_launch": launch_bytes,
+                         "bytes_breakdown": {"framebuffer": fb_bytes, "geometry_textures": geo_bytes},
+                         "avg_launch_ms": raster_avg_ms,
+                         "prepare_avg_ms": statistics.mean(prepare_ms)},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clocks,
+            "parity": parity,
+            "cpu_baseline": cpu_baseline,
+        }
+        print(json.dumps(line))
+    r.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

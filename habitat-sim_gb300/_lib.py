@@ -54,7 +54,8 @@ class Tuning(ctypes.Structure):
 class DrawStats(ctypes.Structure):
     _fields_ = [("scenes", ctypes.c_uint64), ("draws", ctypes.c_uint64),
                 ("visible_draws", ctypes.c_uint64), ("triangles", ctypes.c_uint64),
-                ("kernel_launches", ctypes.c_uint64)]
+                ("kernel_launches", ctypes.c_uint64), ("prepare_ms", ctypes.c_float),
+                ("raster_ms", ctypes.c_float)]
 
 
 _P = ctypes.c_void_p
@@ -101,6 +102,7 @@ PROTOTYPES = {
     "gbr_get_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
     "gbr_set_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
     "gbr_last_draw_stats": (_ST, [_P, ctypes.POINTER(DrawStats)]),
+    "gbr_set_kernel_timing": (_ST, [_P, _I32]),
 }
 
 _lib = None

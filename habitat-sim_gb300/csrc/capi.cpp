@@ -351,4 +351,9 @@ gbr_status gbr_last_draw_stats(gbr_renderer* r, gbr_draw_stats* out) {
   return guarded([&] { return R(r)->last_stats(out); });
 }
 
+gbr_status gbr_set_kernel_timing(gbr_renderer* r, int32_t enabled) {
+  GBR_HANDLE(r);
+  return R(r)->set_kernel_timing(enabled != 0);
+}
+
 }  // extern "C"

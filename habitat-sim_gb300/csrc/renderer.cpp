@@ -227,6 +227,8 @@ Renderer::~Renderer() {
   if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
   if (upload_done_) cudaEventDestroy(upload_done_);
   if (own_stream_) cudaStreamDestroy(own_stream_);
+  for (auto& e : ev_)
+    if (e) cudaEventDestroy(e);
 }
 
 // ----------------------------------------------------------- resources
@@ -800,8 +802,10 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   uint64_t launches = 0;
   if (mode == GBR_DRAW_BATCHED) {
     pp.scene_base = 0;
+    if (timing_) GBR_CUDA(cudaEventRecordWithFlags(ev_[0], stream, cudaEventRecordExternal), "timing event");
     GBR_CUDA(launch_prepare(pp, S, stream), "prepare launch");
     GBR_CUDA(cudaMemsetAsync(d_counter_.ptr, 0, 4, stream), "counter reset");
+    if (timing_) GBR_CUDA(cudaEventRecordWithFlags(ev_[1], stream, cudaEventRecordExternal), "timing event");
     rp.items = d_items_lpt_.as<WorkItem>();
     rp.item_base = 0;
     rp.item_count = item_count_;
@@ -809,6 +813,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
     const uint32_t grid =
         std::min<uint32_t>(item_count_, uint32_t(sm_count_) * uint32_t(ctas_per_sm_));
     GBR_CUDA(launch_raster(rp, tuning_.threads, grid, smem_bytes_, stream), "raster launch");
+    if (timing_) GBR_CUDA(cudaEventRecordWithFlags(ev_[2], stream, cudaEventRecordExternal), "timing event");
     launches = 2;
   } else {
     rp.items = d_items_.as<WorkItem>();
@@ -870,6 +875,7 @@ gbr_status Renderer::draw(cudaStream_t stream, uint32_t mode, bool use_graph) {
   last_stats_.scenes = S;
   last_stats_.draws = total_draws_;
   last_stats_.kernel_launches = launches_;
+  timed_ = timing_ && mode == GBR_DRAW_BATCHED;
   return GBR_OK;
 }
 
@@ -1009,6 +1015,15 @@ gbr_status Renderer::plane_dlpack(uint32_t plane, void** out) {
   return GBR_OK;
 }
 
+gbr_status Renderer::set_kernel_timing(bool on) {
+  cudaSetDevice(device_);
+  for (auto& e : ev_)
+    if (!e) GBR_CUDA(cudaEventCreate(&e), "timing events");
+  if (on != timing_) graph_valid_ = false;
+  timing_ = on;
+  return GBR_OK;
+}
+
 gbr_status Renderer::get_tuning(gbr_tuning* t) const {
   *t = tuning_;
   return GBR_OK;
@@ -1032,6 +1047,11 @@ gbr_status Renderer::last_stats(gbr_draw_stats* out) {
   if (S && d_vis_count_.ptr) {
     GBR_CUDA(cudaMemcpy(cnt.data(), d_vis_count_.ptr, S * 4, cudaMemcpyDeviceToHost), "stats");
     GBR_CUDA(cudaMemcpy(tris.data(), d_vis_tris_.ptr, S * 4, cudaMemcpyDeviceToHost), "stats");
+  }
+  last_stats_.prepare_ms = last_stats_.raster_ms = -1.0f;
+  if (timed_) {
+    GBR_CUDA(cudaEventElapsedTime(&last_stats_.prepare_ms, ev_[0], ev_[1]), "timing");
+    GBR_CUDA(cudaEventElapsedTime(&last_stats_.raster_ms, ev_[1], ev_[2]), "timing");
   }
   last_stats_.visible_draws = std::accumulate(cnt.begin(), cnt.end(), uint64_t(0));
   last_stats_.triangles = std::accumulate(tris.begin(), tris.end(), uint64_t(0));

@@ -102,6 +102,7 @@ class Renderer {
   gbr_status get_tuning(gbr_tuning* t) const;
   gbr_status set_tuning(const gbr_tuning& t);
   gbr_status last_stats(gbr_draw_stats* out);
+  gbr_status set_kernel_timing(bool on);
 
   uint32_t scene_count() const { return uint32_t(scenes_.size()); }
   const gbr_config& config() const { return cfg_; }
@@ -174,6 +175,9 @@ class Renderer {
   bool graph_valid_ = false;
 
   gbr_draw_stats last_stats_{};
+  bool timing_ = false;
+  bool timed_ = false;
+  cudaEvent_t ev_[3] = {nullptr, nullptr, nullptr};
   uint64_t launches_ = 0;
 };
 

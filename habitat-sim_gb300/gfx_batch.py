@@ -364,7 +364,12 @@ class RendererStandalone:
     def lastDrawStats(self):
         s = _lib.DrawStats()
         check(self._lib.gbr_last_draw_stats(self._h, ctypes.byref(s)))
-        return {k: int(getattr(s, k)) for k, _ in _lib.DrawStats._fields_}
+        return {k: getattr(s, k) for k, _ in _lib.DrawStats._fields_}
+
+    def setKernelTiming(self, enabled=True):
+        """CUDA events around the prepare and raster launches of batched
+        draws; read back through lastDrawStats() (prepare_ms, raster_ms)."""
+        check(self._lib.gbr_set_kernel_timing(self._h, 1 if enabled else 0))
 
     def tuning(self):
         t = _lib.Tuning()

@@ -243,7 +243,12 @@ gbr_status gbr_set_tuning(gbr_renderer* r, const gbr_tuning* tuning);
 typedef struct gbr_draw_stats {
   uint64_t scenes, draws, visible_draws, triangles; /* triangles of visible draws */
   uint64_t kernel_launches;
+  float prepare_ms, raster_ms; /* CUDA-event times on the draw's stream when
+                                  kernel timing is on (batched mode), else -1 */
 } gbr_draw_stats;
+/* Records CUDA events around the prepare and raster launches of each
+ * batched draw (also inside a captured graph). */
+gbr_status gbr_set_kernel_timing(gbr_renderer* r, int32_t enabled);
 gbr_status gbr_last_draw_stats(gbr_renderer* r, gbr_draw_stats* out);
 
 #ifdef __cplusplus
