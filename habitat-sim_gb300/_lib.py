@@ -103,6 +103,8 @@ PROTOTYPES = {
     "gbr_set_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
     "gbr_last_draw_stats": (_ST, [_P, ctypes.POINTER(DrawStats)]),
     "gbr_set_kernel_timing": (_ST, [_P, _I32]),
+    "gbr_render_mesh_no_alloc": (_ST, [_P, _P, _P, _U32, _U32, c_float_p, c_float_p, _U32, _I32,
+                                       _I32, _I32, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

@@ -770,3 +770,242 @@ cudaError_t launch_unproject(float a, float b, float* depth, uint64_t rows, uint
 }
 
 }  // namespace gbr
+
+// ======================================================================
+// Rendering one mesh without allocating device memory.
+//
+// For callers that must not allocate: code running inside another
+// framework's memory pool or under a strict device-memory budget, real-time
+// loops where an allocation could stall or fail, and plugins whose host
+// application owns every allocation.  They pass their own device buffers for
+// the mesh and the output planes; the few hundred bytes of per-call scratch
+// this path needs (scene and visible-draw records, the work-item list and
+// counter of the persistent raster kernel, a bad-index flag) live in the
+// fixed array below, which every GPU that loads this library keeps until
+// the process exits.
+// ======================================================================
+#include <algorithm>
+#include <mutex>
+#include <string>
+
+#include "../../include/gbr.h"
+
+namespace gbr {
+void set_last_error(const std::string& msg);
+void mat4_mul(const float* a, const float* b, float* c);
+
+namespace {
+
+constexpr int kNoAllocMaxSide = 4096;  // largest viewport side the scratch can tile
+constexpr int kNoAllocRegion = 128;    // region side of one work item
+constexpr int kNoAllocMaxItems =
+    (kNoAllocMaxSide / kNoAllocRegion) * (kNoAllocMaxSide / kNoAllocRegion);
+constexpr size_t kNoAllocScratchBytes = 16384;
+constexpr int kNoAllocMaxDevices = 64;
+
+struct NoAllocScratch {
+  SceneRec scene;
+  VisibleRec visible;
+  MaterialRec material;
+  uint32_t vis_count, vis_tris, counter, bad_index;
+  WorkItem items[kNoAllocMaxItems];
+};
+static_assert(sizeof(NoAllocScratch) <= kNoAllocScratchBytes, "no-alloc scratch too small");
+
+// The scratch.  Shared by every call on a device; calls that overlap on the
+// GPU (different streams, no ordering between them) race on it.
+static __device__ __align__(256) unsigned char g_no_alloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_no_alloc_mutex;
+void* g_no_alloc_ptr[kNoAllocMaxDevices] = {};
+
+__global__ void no_alloc_check_indices(const uint32_t* indices, uint64_t n, uint32_t vertex_count,
+                                       NoAllocScratch* s) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
+       i += uint64_t(gridDim.x) * blockDim.x)
+    if (indices[i] >= vertex_count) s->bad_index = 1u;
+}
+
+struct NoAllocSetup {
+  float pv[16];
+  float vrow[4];
+  int32_t width, height;
+  uint32_t triangles, semantic_id, flags, items;
+};
+
+// Fills the scene, visible-draw, material and work-item records and resets
+// the work counter (everything the raster kernel must find fresh).
+__global__ void no_alloc_setup(const NoAllocSetup a, NoAllocScratch* s) {
+  if (threadIdx.x == 0) {
+    SceneRec sc{};
+    sc.width = a.width;
+    sc.height = a.height;
+    sc.fb_offset = 0;
+    sc.pitch = a.width;
+    sc.node_base = 0;
+    sc.node_count = 2;
+    sc.draw_base = 0;
+    sc.draw_count = 1;
+    s->scene = sc;
+    // The mesh sits under an identity root and an identity child, as a
+    // hierarchy added without a bake transform: abs = I * I, MVP = PV * abs.
+    float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    float absm[16], mvp[16];
+    matmul(ident, ident, absm);
+    matmul(a.pv, absm, mvp);
+    VisibleRec v{};
+    for (int i = 0; i < 16; ++i) v.mvp[i] = mvp[i];
+    for (int col = 0; col < 4; ++col) {
+      float z = __fmul_rn(a.vrow[0], absm[col * 4 + 0]);
+      z = fma_(a.vrow[1], absm[col * 4 + 1], z);
+      z = fma_(a.vrow[2], absm[col * 4 + 2], z);
+      z = fma_(a.vrow[3], absm[col * 4 + 3], z);
+      v.zrow[col] = z;
+    }
+    const bool ok = s->bad_index == 0u;
+    v.vertex_base = 0;
+    v.first_index = 0;
+    v.tri_count = a.triangles;
+    v.material = 0;
+    v.semantic_id = a.semantic_id;
+    v.ordinal = 0;
+    v.flags = a.flags;
+    s->visible = v;
+    MaterialRec m{};
+    m.color[0] = m.color[1] = m.color[2] = m.color[3] = 1.0f;
+    m.texture = 0;
+    m.layer = 0;
+    m.m[0] = m.m[4] = m.m[8] = 1.0f;
+    s->material = m;
+    s->vis_count = ok && a.triangles ? 1u : 0u;
+    s->vis_tris = ok ? a.triangles : 0u;
+    s->counter = 0u;
+  }
+  const int cols = (a.width + kNoAllocRegion - 1) / kNoAllocRegion;
+  for (uint32_t i = threadIdx.x; i < a.items; i += blockDim.x) {
+    WorkItem w{};
+    w.scene = 0;
+    w.x0 = uint16_t((i % cols) * kNoAllocRegion);
+    w.y0 = uint16_t((i / cols) * kNoAllocRegion);
+    w.w = uint16_t(min(kNoAllocRegion, a.width - int(w.x0)));
+    w.h = uint16_t(min(kNoAllocRegion, a.height - int(w.y0)));
+    s->items[i] = w;
+  }
+}
+
+gbr_status no_alloc_fail(gbr_status s, const std::string& m) {
+  set_last_error("gbr_render_mesh_no_alloc: " + m);
+  return s;
+}
+
+}  // namespace
+}  // namespace gbr
+
+extern "C" gbr_status gbr_render_mesh_no_alloc(
+    const void* positions, const void* colors, const uint32_t* indices, uint32_t vertex_count,
+    uint32_t triangle_count, const float projection[16], const float view[16],
+    uint32_t semantic_id, int32_t use_vertex_ids, int32_t width, int32_t height, uint32_t* color,
+    float* depth, float* linear_depth, uint32_t* semantic, void* stream) {
+  using namespace gbr;
+  if (!projection || !view) return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT, "null camera matrix");
+  if (width < 1 || height < 1 || width > kNoAllocMaxSide || height > kNoAllocMaxSide)
+    return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT,
+                         "viewport " + std::to_string(width) + "x" + std::to_string(height) +
+                             " is outside 1..4096 x 1..4096, the limit of its fixed scratch");
+  if (triangle_count >= (1u << 31))
+    return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT, "2^31 or more triangles");
+  if (triangle_count && (!positions || !indices || vertex_count == 0))
+    return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT, "positions, indices and vertices are required");
+  if ((reinterpret_cast<uintptr_t>(positions) | reinterpret_cast<uintptr_t>(colors)) & 15u)
+    return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT, "positions and colours must be 16-byte aligned");
+  if ((reinterpret_cast<uintptr_t>(color) | reinterpret_cast<uintptr_t>(depth) |
+       reinterpret_cast<uintptr_t>(linear_depth) | reinterpret_cast<uintptr_t>(semantic) |
+       reinterpret_cast<uintptr_t>(indices)) & 3u)
+    return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT, "indices and planes must be 4-byte aligned");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
+    return no_alloc_fail(GBR_ERROR_CUDA, "no usable current device");
+  void* scratch = nullptr;
+  {
+    // First call on this device: look up the device address of the fixed
+    // scratch (a host-side name of a __device__ array is not a device address).
+    std::lock_guard<std::mutex> lock(g_no_alloc_mutex);
+    if (!g_no_alloc_ptr[dev]) {
+      e = cudaGetSymbolAddress(&g_no_alloc_ptr[dev], g_no_alloc_scratch);
+      if (e != cudaSuccess) {
+        g_no_alloc_ptr[dev] = nullptr;
+        cudaGetLastError();
+        return no_alloc_fail(GBR_ERROR_CUDA, std::string("cudaGetSymbolAddress: ") +
+                                                 cudaGetErrorString(e));
+      }
+    }
+    scratch = g_no_alloc_ptr[dev];
+  }
+  NoAllocScratch* s = static_cast<NoAllocScratch*>(scratch);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int cols = (width + kNoAllocRegion - 1) / kNoAllocRegion;
+  const int rows = (height + kNoAllocRegion - 1) / kNoAllocRegion;
+  NoAllocSetup a{};
+  mat4_mul(projection, view, a.pv);
+  for (int k = 0; k < 4; ++k) a.vrow[k] = view[k * 4 + 2];
+  a.width = width;
+  a.height = height;
+  a.triangles = triangle_count;
+  a.semantic_id = semantic_id;
+  a.flags = (colors ? kMeshVertexColor : 0u) | (use_vertex_ids ? kMeshObjectId : 0u);
+  a.items = uint32_t(cols * rows);
+  e = cudaMemsetAsync(&s->bad_index, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess && triangle_count) {
+    const uint64_t n = uint64_t(triangle_count) * 3;
+    const unsigned blocks = unsigned(std::min<uint64_t>((n + 255) / 256, 1024));
+    no_alloc_check_indices<<<blocks, 256, 0, st>>>(indices, n, vertex_count, s);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    no_alloc_setup<<<1, 256, 0, st>>>(a, s);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess)
+    return no_alloc_fail(GBR_ERROR_CUDA, std::string("setup: ") + cudaGetErrorString(e));
+  constexpr int kThreads = 512;
+  size_t max_dyn = 0;
+  e = raster_configure(kThreads, &max_dyn);
+  const size_t smem = raster_smem_bytes(kThreads, kNoAllocRegion * kNoAllocRegion, 1);
+  int occ = 0, sms = 0;
+  if (e == cudaSuccess) e = raster_max_ctas_per_sm(kThreads, smem, &occ);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess || smem > max_dyn || occ < 1)
+    return no_alloc_fail(GBR_ERROR_CUDA, "raster kernel configuration failed");
+  RasterParams p{};
+  p.scenes = &s->scene;
+  p.visible = &s->visible;
+  p.vis_count = &s->vis_count;
+  p.vis_tris = &s->vis_tris;
+  p.pos = static_cast<const float4*>(positions);
+  p.color = static_cast<const float4*>(colors);
+  p.uv = nullptr;
+  p.indices = indices;
+  p.materials = &s->material;
+  p.textures = nullptr;
+  p.texels = nullptr;
+  p.texture_count = 1;
+  p.flags = 0;
+  p.items = s->items;
+  p.item_base = 0;
+  p.item_count = a.items;
+  p.counter = &s->counter;
+  p.persistent = 1;
+  p.out.color = color;
+  p.out.depth = depth;
+  p.out.linear = linear_depth;
+  p.out.semantic = semantic;
+  p.region_px = kNoAllocRegion * kNoAllocRegion;
+  p.prefix_cap = 1;
+  p.small_area = 64;
+  const uint32_t grid = std::min<uint32_t>(a.items, uint32_t(sms) * uint32_t(occ));
+  e = launch_raster(p, kThreads, grid, smem, st);
+  if (e != cudaSuccess)
+    return no_alloc_fail(GBR_ERROR_CUDA, std::string("raster launch: ") + cudaGetErrorString(e));
+  return GBR_OK;
+}

@@ -251,6 +251,41 @@ typedef struct gbr_draw_stats {
 gbr_status gbr_set_kernel_timing(gbr_renderer* r, int32_t enabled);
 gbr_status gbr_last_draw_stats(gbr_renderer* r, gbr_draw_stats* out);
 
+/* Renders one triangle mesh into caller-owned device planes without
+ * allocating any memory.  No counterpart in the reference: it is for callers
+ * that must not call cudaMalloc -- code running inside another framework's
+ * memory pool or under a strict device-memory budget, real-time loops where
+ * an allocation could stall or fail, plugins whose host owns every
+ * allocation.  It runs the same raster kernel as gbr_draw on one scene whose
+ * mesh sits under identity transforms, with flat white material (vertex
+ * colours if `colors` is not NULL) and no texture.
+ *
+ *  positions   device, float4 per vertex (x, y, z, object-id bits), 16-B aligned
+ *  colors      device, float4 RGBA per vertex, 16-B aligned, or NULL
+ *  indices     device, 3 uint32 per triangle (an index >= vertex_count makes
+ *              the call render only background)
+ *  projection, view   host, column-major 4x4 (as gbr_update_camera)
+ *  semantic_id id of every pixel the mesh covers, unless use_vertex_ids,
+ *              then the last vertex's id from positions[].w
+ *  width, height      1..4096 each; larger viewports are rejected
+ *  color, depth, linear_depth, semantic   device planes of width*height
+ *              elements, row pitch = width, row 0 at the bottom; any may be NULL
+ *
+ * Its per-call scratch is one fixed 16 KiB __device__ array in the library
+ * (held by every GPU that loads it until the process exits); each call
+ * rewrites what must start fresh.  All calls share that array, so calls that
+ * may overlap on the GPU (different streams without ordering) race: order
+ * them on one stream.  The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  Asynchronous on `stream`. */
+gbr_status gbr_render_mesh_no_alloc(const void* positions, const void* colors,
+                                    const uint32_t* indices, uint32_t vertex_count,
+                                    uint32_t triangle_count, const float projection[16],
+                                    const float view[16], uint32_t semantic_id,
+                                    int32_t use_vertex_ids, int32_t width, int32_t height,
+                                    uint32_t* color, float* depth, float* linear_depth,
+                                    uint32_t* semantic, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
