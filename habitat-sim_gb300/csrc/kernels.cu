@@ -38,6 +38,8 @@ namespace {
 constexpr uint64_t kEmptyKey = ~0ull;
 constexpr uint32_t kBackground = 0xFF1F1F1Fu;
 constexpr int kMaxHierarchyDepth = 64;
+// Chunks tested and compacted per window (must be <= 32 x the smallest CTA).
+constexpr int kChunkWindow = 2048;
 
 __device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
@@ -95,15 +97,43 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
   return out;
 }
 
+// Clip-plane outcode of an object-space point, with a relative margin: a
+// bit is set only when the point is beyond that plane by more than rounding
+// could move it, so every culling decision built on it is conservative.
+__device__ __forceinline__ uint32_t outcode(const float* mvp, float x, float y, float z) {
+  const float cx = mrow(mvp, 0, x, y, z), cy = mrow(mvp, 1, x, y, z), cz = mrow(mvp, 2, x, y, z),
+              cw = mrow(mvp, 3, x, y, z);
+  const float ax = 1e-5f * (fabsf(cx) + fabsf(cw)), ay = 1e-5f * (fabsf(cy) + fabsf(cw)),
+              az = 1e-5f * (fabsf(cz) + fabsf(cw));
+  uint32_t out = 0;
+  out |= (cx - cw > ax) ? 1u : 0u;
+  out |= (-cx - cw > ax) ? 2u : 0u;
+  out |= (cy - cw > ay) ? 4u : 0u;
+  out |= (-cy - cw > ay) ? 8u : 0u;
+  out |= (cz - cw > az) ? 16u : 0u;
+  out |= (-cz - cw > az) ? 32u : 0u;
+  return out;
+}
+
+// True when the point is inside all six clip planes by a relative margin.
+__device__ __forceinline__ bool inside_frustum(const float* mvp, float x, float y, float z) {
+  const float cx = mrow(mvp, 0, x, y, z), cy = mrow(mvp, 1, x, y, z), cz = mrow(mvp, 2, x, y, z),
+              cw = mrow(mvp, 3, x, y, z);
+  const float m = 1e-5f * (fabsf(cx) + fabsf(cy) + fabsf(cz) + fabsf(cw));
+  return cx + m < cw && -cx + m < cw && cy + m < cw && -cy + m < cw && cz + m < cw &&
+         -cz + m < cw;
+}
+
 // ================================================================ prepare
 template <int T>
 __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
-  __shared__ uint32_t s_warp[T / 32], s_total, s_count, s_tris;
+  __shared__ uint32_t s_warp[T / 32], s_total, s_count, s_tris, s_chunks;
   const uint32_t s = p.scene_base + blockIdx.x;
   const SceneRec sc = p.scenes[s];
   if (threadIdx.x == 0) {
     s_count = 0;
     s_tris = 0;
+    s_chunks = 0;
   }
   float pv[16], vrow[4];
 #pragma unroll
@@ -113,7 +143,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
   __syncthreads();
   for (uint32_t base = 0; base < sc.draw_count; base += T) {
     const uint32_t j = base + threadIdx.x;
-    uint32_t vis = 0, tris = 0;
+    uint32_t vis = 0, tris = 0, chunks = 0;
     VisibleRec rec;
     if (j < sc.draw_count) {
       const DrawRec d = p.draws[sc.draw_base + j];
@@ -159,34 +189,28 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
         // eight corners lie beyond the same clip plane by a relative margin,
         // so rounding can never drop a triangle that would cover a pixel.
         uint32_t all_out = 0x3fu;
+        bool inside = true;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           const float x = d.bbox[(c & 1) ? 3 : 0], y = d.bbox[(c & 2) ? 4 : 1],
                       z = d.bbox[(c & 4) ? 5 : 2];
-          const float cx = mrow(rec.mvp, 0, x, y, z), cy = mrow(rec.mvp, 1, x, y, z),
-                      cz = mrow(rec.mvp, 2, x, y, z), cw = mrow(rec.mvp, 3, x, y, z);
-          const float ax = 1e-5f * (fabsf(cx) + fabsf(cw)), ay = 1e-5f * (fabsf(cy) + fabsf(cw)),
-                      az = 1e-5f * (fabsf(cz) + fabsf(cw));
-          uint32_t out = 0;
-          out |= (cx - cw > ax) ? 1u : 0u;
-          out |= (-cx - cw > ax) ? 2u : 0u;
-          out |= (cy - cw > ay) ? 4u : 0u;
-          out |= (-cy - cw > ay) ? 8u : 0u;
-          out |= (cz - cw > az) ? 16u : 0u;
-          out |= (-cz - cw > az) ? 32u : 0u;
-          all_out &= out;
+          all_out &= outcode(rec.mvp, x, y, z);
+          inside = inside && inside_frustum(rec.mvp, x, y, z);
         }
         if (all_out == 0 && d.tri_count > 0) {
           const MeshRec m = p.meshes[d.mesh];
           vis = 1;
           tris = d.tri_count;
+          chunks = d.chunk_count;
           rec.vertex_base = m.vertex_base;
           rec.first_index = d.first_index;
           rec.tri_count = d.tri_count;
           rec.material = d.material;
           rec.semantic_id = d.semantic_id;
-          rec.flags = m.flags;
-          rec.pad = 0;
+          rec.flags = m.flags | (inside ? kDrawInsideFrustum : 0u);
+          rec.box_base = d.box_base;
+          rec.chunk_count = d.chunk_count;
+          rec.pad[0] = rec.pad[1] = 0;
         }
       }
     }
@@ -195,20 +219,26 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
     __syncthreads();
     const uint32_t to = block_exclusive_scan<T>(tris, s_warp, &s_total);
     const uint32_t ttot = s_total;
+    __syncthreads();
+    const uint32_t co = block_exclusive_scan<T>(chunks, s_warp, &s_total);
+    const uint32_t ctot = s_total;
     if (vis) {
       rec.ordinal = s_tris + to;
+      rec.chunk = s_chunks + co;
       p.visible[sc.draw_base + s_count + vo] = rec;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
       s_count += vtot;
       s_tris += ttot;
+      s_chunks += ctot;
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     p.vis_count[s] = s_count;
     p.vis_tris[s] = s_tris;
+    p.vis_chunks[s] = s_chunks;
   }
 }
 
@@ -220,6 +250,23 @@ struct QEntry {
   uint32_t bias;  // bit i: edge i owns its pixels (top-left)
   int16_t x0, y0, x1, y1;
 };
+
+// Dynamic shared-memory layout of raster_kernel; every section starts on a
+// 16-byte boundary.
+struct SmemLayout {
+  size_t queue, qoff, prefix, chunks, total;
+};
+__host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+__host__ __device__ __forceinline__ SmemLayout smem_layout(int threads, int region_px,
+                                                           int prefix_cap) {
+  SmemLayout l;
+  l.queue = align16(size_t(region_px) * 8);
+  l.qoff = align16(l.queue + size_t(threads) * sizeof(QEntry));
+  l.prefix = align16(l.qoff + size_t(threads + 1) * 4);
+  l.chunks = align16(l.prefix + size_t(prefix_cap + 1) * 4);
+  l.total = align16(l.chunks + size_t(kChunkWindow) * sizeof(uint2));
+  return l;
+}
 
 struct Setup {
   int32_t X[3], Y[3];
@@ -564,13 +611,65 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
   sid = (flags & kMeshObjectId) ? __float_as_uint(__ldg(&p.pos[v[2]]).w) : __ldg(&rec->semantic_id);
 }
 
+// False when no triangle of the chunk can cover a pixel of the region: its
+// object-space box is beyond one frustum plane, or, with every corner in
+// front of the camera, its projected bounding rectangle (grown by 2 pixels)
+// misses the region.  Conservative: culling never removes a covered pixel.
+__device__ __forceinline__ bool chunk_visible(const float* mvp, const ChunkBox& b, const Ctx& c,
+                                              bool frustum, bool region) {
+  uint32_t all_out = 0x3fu;
+  bool all_front = true;
+  float x0 = 3.0e38f, x1 = -3.0e38f, y0 = 3.0e38f, y1 = -3.0e38f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float x = (k & 1) ? b.hi[0] : b.lo[0], y = (k & 2) ? b.hi[1] : b.lo[1],
+                z = (k & 4) ? b.hi[2] : b.lo[2];
+    if (frustum) all_out &= outcode(mvp, x, y, z);
+    if (region) {
+      const float cx = mrow(mvp, 0, x, y, z), cy = mrow(mvp, 1, x, y, z),
+                  cw = mrow(mvp, 3, x, y, z);
+      if (cw > 1e-6f) {
+        const float sx = (cx / cw * 0.5f + 0.5f) * float(c.W);
+        const float sy = (cy / cw * 0.5f + 0.5f) * float(c.H);
+        x0 = fminf(x0, sx);
+        x1 = fmaxf(x1, sx);
+        y0 = fminf(y0, sy);
+        y1 = fmaxf(y1, sy);
+      } else {
+        all_front = false;
+      }
+    }
+  }
+  if (frustum && all_out) return false;
+  if (region && all_front &&
+      (x1 + 2.0f < float(c.rx0) || x0 - 2.0f > float(c.rx0 + c.rw) ||
+       y1 + 2.0f < float(c.ry0) || y0 - 2.0f > float(c.ry0 + c.rh)))
+    return false;
+  return true;
+}
+
+// Largest d in [0, n) with vis[d].chunk <= g.
+__device__ __forceinline__ uint32_t find_chunk_draw(const VisibleRec* vis, uint32_t n, uint32_t g) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&vis[mid].chunk) <= g)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
 template <int T>
 __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const SmemLayout L = smem_layout(T, p.region_px, p.prefix_cap);
   uint64_t* keys = reinterpret_cast<uint64_t*>(smem);
-  QEntry* queue = reinterpret_cast<QEntry*>(keys + p.region_px);
-  uint32_t* qoff = reinterpret_cast<uint32_t*>(queue + T);
-  uint32_t* prefix = qoff + (T + 1);
+  QEntry* queue = reinterpret_cast<QEntry*>(smem + L.queue);
+  uint32_t* qoff = reinterpret_cast<uint32_t*>(smem + L.qoff);
+  uint32_t* prefix = reinterpret_cast<uint32_t*>(smem + L.prefix);
+  uint2* chunks = reinterpret_cast<uint2*>(smem + L.chunks);
   __shared__ uint32_t s_item, s_qcount, s_total;
   __shared__ uint32_t s_warp[T / 32];
 
@@ -606,59 +705,106 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
     if (threadIdx.x == 0) s_qcount = 0;
     __syncthreads();
 
-    for (uint32_t base = 0; base < total; base += T) {
-      const uint32_t g = base + threadIdx.x;
-      if (g < total) {
-        const uint32_t di = find_draw(prefix, vis, cached, nvis, g);
-        const VisibleRec* rec = vis + di;
-        const uint32_t t = g - __ldg(&rec->ordinal);
-        float mvp[16];
+    // Visible chunks of the scene, a window of kChunkWindow at a time: each
+    // thread tests a run of consecutive chunks, the CTA compacts the
+    // survivors into a shared list of (draw, chunk in draw), then rounds of
+    // T threads set up one triangle each from that list.
+    const uint32_t nchunks = p.vis_chunks[wi.scene];
+    const bool whole = c.rw == c.W && c.rh == c.H;
+    (void)total;
+    for (uint32_t w0 = 0; w0 < nchunks; w0 += kChunkWindow) {
+      const uint32_t wn = min(uint32_t(kChunkWindow), nchunks - w0);
+      const uint32_t per = (wn + T - 1) / T;
+      const uint32_t my0 = w0 + min(wn, threadIdx.x * per), my1 = w0 + min(wn, (threadIdx.x + 1) * per);
+      uint32_t mask = 0, count = 0;  // per <= 32 because kChunkWindow <= 32 * T
+      if (my0 < my1) {
+        uint32_t di = find_chunk_draw(vis, nvis, my0);
+        for (uint32_t gc = my0; gc < my1; ++gc) {
+          while (di + 1 < nvis && __ldg(&vis[di + 1].chunk) <= gc) ++di;
+          const VisibleRec* rec = vis + di;
+          const bool inside = __ldg(&rec->flags) & kDrawInsideFrustum;
+          bool keep = true;
+          if (p.boxes && !(inside && whole)) {
+            float mvp[16];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) mvp[i] = __ldg(&rec->mvp[i]);
-        const uint32_t vb = __ldg(&rec->vertex_base);
-        const uint32_t fi = __ldg(&rec->first_index) + 3u * t;
-        float4 cv[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const float4 q = __ldg(&p.pos[vb + __ldg(&p.indices[fi + k])]);
-          cv[k] = make_float4(mrow(mvp, 0, q.x, q.y, q.z), mrow(mvp, 1, q.x, q.y, q.z),
-                              mrow(mvp, 2, q.x, q.y, q.z), mrow(mvp, 3, q.x, q.y, q.z));
-        }
-        triangle(cv, g, c);
-      }
-      __syncthreads();
-      const uint32_t nq = min(s_qcount, uint32_t(T));
-      __syncthreads();
-      if (nq > 0) {
-        if (threadIdx.x == 0) s_qcount = 0;
-        uint32_t area = 0;
-        if (threadIdx.x < nq) {
-          const QEntry& e = queue[threadIdx.x];
-          area = uint32_t(e.x1 - e.x0 + 1) * uint32_t(e.y1 - e.y0 + 1);
-        }
-        const uint32_t off = block_exclusive_scan<T>(area, s_warp, &s_total);
-        const uint32_t tot = s_total;
-        if (threadIdx.x < nq) qoff[threadIdx.x] = off;
-        __syncthreads();
-        for (uint32_t q = threadIdx.x; q < tot; q += T) {
-          uint32_t lo = 0, hi = nq;
-          while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (qoff[mid] <= q)
-              lo = mid;
-            else
-              hi = mid;
+            for (int i = 0; i < 16; ++i) mvp[i] = __ldg(&rec->mvp[i]);
+            keep = chunk_visible(mvp, p.boxes[__ldg(&rec->box_base) + (gc - __ldg(&rec->chunk))], c,
+                                 !inside, !whole);
           }
-          const QEntry& e = queue[lo];
-          const int w = e.x1 - e.x0 + 1;
-          const int local = int(q - qoff[lo]);
-          const int px = e.x0 + local % w, py = e.y0 + local / w;
-          float z;
-          if (cover(e.X, e.Y, e.bias, e.zw0, e.d1, e.d2, e.inva, px, py, z))
-            depth_write(keys, (py - c.ry0) * c.rw + (px - c.rx0), z, e.ordinal);
+          if (keep) {
+            mask |= 1u << (gc - my0);
+            ++count;
+          }
+        }
+      }
+      uint32_t pos = block_exclusive_scan<T>(count, s_warp, &s_total);
+      const uint32_t nvc = s_total;
+      if (count) {
+        uint32_t di = find_chunk_draw(vis, nvis, my0);
+        for (uint32_t gc = my0; gc < my1; ++gc) {
+          while (di + 1 < nvis && __ldg(&vis[di + 1].chunk) <= gc) ++di;
+          if (mask & (1u << (gc - my0))) chunks[pos++] = make_uint2(di, gc - __ldg(&vis[di].chunk));
+        }
+      }
+      __syncthreads();
+      const uint32_t ntri = nvc * kChunkTris;
+      for (uint32_t base = 0; base < ntri; base += T) {
+        const uint32_t g = base + threadIdx.x;
+        if (g < ntri) {
+          const uint2 ch = chunks[g / kChunkTris];
+          const VisibleRec* rec = vis + ch.x;
+          const uint32_t t = ch.y * kChunkTris + (g % kChunkTris);
+          if (t < __ldg(&rec->tri_count)) {
+            float mvp[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) mvp[i] = __ldg(&rec->mvp[i]);
+            const uint32_t vb = __ldg(&rec->vertex_base);
+            const uint32_t fi = __ldg(&rec->first_index) + 3u * t;
+            float4 cv[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              const float4 q = __ldg(&p.pos[vb + __ldg(&p.indices[fi + k])]);
+              cv[k] = make_float4(mrow(mvp, 0, q.x, q.y, q.z), mrow(mvp, 1, q.x, q.y, q.z),
+                                  mrow(mvp, 2, q.x, q.y, q.z), mrow(mvp, 3, q.x, q.y, q.z));
+            }
+            triangle(cv, __ldg(&rec->ordinal) + t, c);
+          }
         }
         __syncthreads();
+        const uint32_t nq = min(s_qcount, uint32_t(T));
+        __syncthreads();
+        if (nq > 0) {
+          if (threadIdx.x == 0) s_qcount = 0;
+          uint32_t area = 0;
+          if (threadIdx.x < nq) {
+            const QEntry& e = queue[threadIdx.x];
+            area = uint32_t(e.x1 - e.x0 + 1) * uint32_t(e.y1 - e.y0 + 1);
+          }
+          const uint32_t off = block_exclusive_scan<T>(area, s_warp, &s_total);
+          const uint32_t tot = s_total;
+          if (threadIdx.x < nq) qoff[threadIdx.x] = off;
+          __syncthreads();
+          for (uint32_t q = threadIdx.x; q < tot; q += T) {
+            uint32_t lo = 0, hi = nq;
+            while (hi - lo > 1) {
+              const uint32_t mid = (lo + hi) >> 1;
+              if (qoff[mid] <= q)
+                lo = mid;
+              else
+                hi = mid;
+            }
+            const QEntry& e = queue[lo];
+            const int w = e.x1 - e.x0 + 1;
+            const int local = int(q - qoff[lo]);
+            const int px = e.x0 + local % w, py = e.y0 + local / w;
+            float z;
+            if (cover(e.X, e.Y, e.bias, e.zw0, e.d1, e.d2, e.inva, px, py, z))
+              depth_write(keys, (py - c.ry0) * c.rw + (px - c.rx0), z, e.ordinal);
+          }
+          __syncthreads();
+        }
       }
+      __syncthreads();
     }
     __syncthreads();
 
@@ -704,9 +850,7 @@ cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStr
 }
 
 size_t raster_smem_bytes(int threads, int region_px, int prefix_cap) {
-  size_t b = size_t(region_px) * 8 + size_t(threads) * sizeof(QEntry) +
-             size_t(threads + 1) * 4 + size_t(prefix_cap + 1) * 4;
-  return (b + 15) & ~size_t(15);
+  return smem_layout(threads, region_px, prefix_cap).total;
 }
 
 #define GBR_RASTER_SWITCH(threads, F) \
@@ -723,16 +867,16 @@ cudaError_t raster_configure(int threads, size_t* max_dynamic) {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-#define GBR_CFG(T)                                                                            \
-  {                                                                                           \
-    cudaFuncAttributes fa;                                                                    \
-    e = cudaFuncGetAttributes(&fa, raster_kernel<T>);                                         \
-    if (e != cudaSuccess) return e;                                                           \
+#define GBR_CFG(T)                                                                             \
+  {                                                                                            \
+    cudaFuncAttributes fa;                                                                     \
+    e = cudaFuncGetAttributes(&fa, raster_kernel<T>);                                          \
+    if (e != cudaSuccess) return e;                                                            \
     const size_t dyn = size_t(optin) > fa.sharedSizeBytes ? size_t(optin) - fa.sharedSizeBytes : 0; \
-    e = cudaFuncSetAttribute(raster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
-                             int(dyn));                                                       \
-    if (e != cudaSuccess) return e;                                                           \
-    *max_dynamic = dyn;                                                                       \
+    e = cudaFuncSetAttribute(raster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                             int(dyn));                                                        \
+    if (e != cudaSuccess) return e;                                                            \
+    *max_dynamic = dyn;                                                                        \
   }
   GBR_RASTER_SWITCH(threads, GBR_CFG)
 #undef GBR_CFG
@@ -740,10 +884,10 @@ cudaError_t raster_configure(int threads, size_t* max_dynamic) {
 }
 
 cudaError_t raster_max_ctas_per_sm(int threads, size_t smem, int* out) {
-#define GBR_OCC(T)                                                                         \
-  {                                                                                        \
+#define GBR_OCC(T)                                                                                \
+  {                                                                                               \
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, raster_kernel<T>, T, smem); \
-    if (e != cudaSuccess) return e;                                                        \
+    if (e != cudaSuccess) return e;                                                               \
   }
   GBR_RASTER_SWITCH(threads, GBR_OCC)
 #undef GBR_OCC
@@ -807,7 +951,7 @@ struct NoAllocScratch {
   SceneRec scene;
   VisibleRec visible;
   MaterialRec material;
-  uint32_t vis_count, vis_tris, counter, bad_index;
+  uint32_t vis_count, vis_tris, vis_chunks, counter, bad_index;
   WorkItem items[kNoAllocMaxItems];
 };
 static_assert(sizeof(NoAllocScratch) <= kNoAllocScratchBytes, "no-alloc scratch too small");
@@ -870,6 +1014,8 @@ __global__ void no_alloc_setup(const NoAllocSetup a, NoAllocScratch* s) {
     v.semantic_id = a.semantic_id;
     v.ordinal = 0;
     v.flags = a.flags;
+    v.chunk = 0;
+    v.box_base = 0;
     s->visible = v;
     MaterialRec m{};
     m.color[0] = m.color[1] = m.color[2] = m.color[3] = 1.0f;
@@ -879,6 +1025,7 @@ __global__ void no_alloc_setup(const NoAllocSetup a, NoAllocScratch* s) {
     s->material = m;
     s->vis_count = ok && a.triangles ? 1u : 0u;
     s->vis_tris = ok ? a.triangles : 0u;
+    s->vis_chunks = ok ? (a.triangles + kChunkTris - 1) / kChunkTris : 0u;
     s->counter = 0u;
   }
   const int cols = (a.width + kNoAllocRegion - 1) / kNoAllocRegion;
@@ -968,7 +1115,7 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
   }
   if (e != cudaSuccess)
     return no_alloc_fail(GBR_ERROR_CUDA, std::string("setup: ") + cudaGetErrorString(e));
-  constexpr int kThreads = 512;
+  constexpr int kThreads = 1024;
   size_t max_dyn = 0;
   e = raster_configure(kThreads, &max_dyn);
   const size_t smem = raster_smem_bytes(kThreads, kNoAllocRegion * kNoAllocRegion, 1);
@@ -982,6 +1129,8 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
   p.visible = &s->visible;
   p.vis_count = &s->vis_count;
   p.vis_tris = &s->vis_tris;
+  p.vis_chunks = &s->vis_chunks;
+  p.boxes = nullptr;
   p.pos = static_cast<const float4*>(positions);
   p.color = static_cast<const float4*>(colors);
   p.uv = nullptr;
@@ -1002,7 +1151,7 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
   p.out.semantic = semantic;
   p.region_px = kNoAllocRegion * kNoAllocRegion;
   p.prefix_cap = 1;
-  p.small_area = 64;
+  p.small_area = 1;
   const uint32_t grid = std::min<uint32_t>(a.items, uint32_t(sms) * uint32_t(occ));
   e = launch_raster(p, kThreads, grid, smem, st);
   if (e != cudaSuccess)

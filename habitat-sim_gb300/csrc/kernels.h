@@ -29,17 +29,22 @@ struct PrepareParams {
   VisibleRec* visible;
   uint32_t* vis_count;
   uint32_t* vis_tris;
+  uint32_t* vis_chunks;
   uint32_t* status;
   uint32_t scene_base;
 };
 
-// Raster: per work item (scene, region), triangle setup + clipping +
-// shared-memory (depth, ordinal) z-buffer + deferred shading + plane writes.
+// Raster: per work item (scene, region), warps take 32-triangle chunks,
+// cull them by bounding box, set up + clip + rasterise their triangles into a
+// shared-memory (depth, ordinal) z-buffer; then deferred shading and plane
+// writes.
 struct RasterParams {
   const SceneRec* scenes;
   const VisibleRec* visible;
   const uint32_t* vis_count;
   const uint32_t* vis_tris;
+  const uint32_t* vis_chunks;
+  const ChunkBox* boxes;      // box per 32-triangle chunk (null: no chunk culling)
   const float4* pos;
   const float4* color;
   const float2* uv;
@@ -57,7 +62,7 @@ struct RasterParams {
   Planes out;
   int32_t region_px;   // capacity of the shared z-buffer, pixels
   int32_t prefix_cap;  // visible draws whose ordinals are cached in shared memory
-  int32_t small_area;
+  int32_t small_area;  // boxes up to this many pixels are rasterised by one lane
 };
 
 cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStream_t stream);

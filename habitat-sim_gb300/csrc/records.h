@@ -8,9 +8,10 @@
 //   textures   texel[t]  uint32 RGBA8, layer-major, row 0 bottom
 //   tables     MeshRec, MaterialRec, TextureRec
 //   scenes     SceneRec[s]; per node parent (int32) + local 4x4 (64 B);
-//              DrawRec[] in draw-batch order; CameraRec[s] (80 B)
+//              DrawRec[] (64 B) in draw-batch order; CameraRec[s] (80 B)
 //   per step   VisibleRec[] (128 B, written by the prepare kernel),
-//              vis_count[s], vis_tris[s]; WorkItem[] + one counter
+//              vis_count[s], vis_tris[s], vis_chunks[s]; WorkItem[] + one counter
+//   views      ChunkBox[] (32 B per 32 triangles of every mesh view)
 //   output     colour u32, window depth f32, linear depth f32, id u32
 //              planes, one element per framebuffer pixel.
 #pragma once
@@ -19,6 +20,8 @@
 namespace gbr {
 
 enum : uint32_t { kMeshVertexColor = 1u, kMeshObjectId = 2u, kMeshTexcoords = 4u };
+// VisibleRec::flags bit: the draw's bounding box lies inside the frustum.
+constexpr uint32_t kDrawInsideFrustum = 0x100u;
 
 struct MeshRec {
   uint32_t vertex_base;
@@ -60,6 +63,9 @@ struct DrawRec {
   uint32_t material;
   uint32_t semantic_id;
   float bbox[6];         // object-space min xyz, max xyz of the view
+  uint32_t box_base;     // first chunk box of the view
+  uint32_t chunk_count;  // 32-triangle chunks of the view
+  uint32_t pad[2];
 };
 
 struct CameraRec {
@@ -67,7 +73,8 @@ struct CameraRec {
   float vrow[4];    // row 2 of the view matrix
 };
 
-struct VisibleRec {
+// 16-byte aligned: the raster kernel reads the matrix with float4 loads.
+struct alignas(16) VisibleRec {
   float mvp[16];
   float zrow[4];       // row 2 of view * model
   uint32_t vertex_base;
@@ -77,9 +84,22 @@ struct VisibleRec {
   uint32_t semantic_id;
   uint32_t ordinal;    // index of this draw's first triangle in the scene
   uint32_t flags;      // mesh flags
-  uint32_t pad;
+  uint32_t chunk;      // index of this draw's first chunk in the scene
+  uint32_t box_base;   // first chunk box of the draw's view
+  uint32_t chunk_count;
+  uint32_t pad[2];
 };
-static_assert(sizeof(VisibleRec) == 112, "VisibleRec layout");
+static_assert(sizeof(VisibleRec) == 128, "VisibleRec layout");
+
+// Triangles per chunk: the unit of work a warp takes and of bounding-box culling.
+constexpr uint32_t kChunkTris = 32;
+
+// Object-space bounding box of one chunk of a mesh view.
+struct ChunkBox {
+  float lo[4];
+  float hi[4];
+};
+
 
 struct WorkItem {
   uint32_t scene;

@@ -367,10 +367,37 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
       mv.bbox[c] = lo[c];
       mv.bbox[3 + c] = hi[c];
     }
+    mv.box_base = uint32_t(boxes_.size());
+    build_chunk_boxes(m, v.index_offset, v.index_count);
+    mv.chunk_count = uint32_t(boxes_.size()) - mv.box_base;
     views_.push_back(mv);
   }
   names_[name] = {begin, uint32_t(views_.size())};
+  tables_dirty_ = true;
+  graph_valid_ = false;
   return GBR_OK;
+}
+
+// Object-space bounding box of every kChunkTris consecutive triangles of a view.
+void Renderer::build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count) {
+  const uint32_t tris = index_count / 3;
+  const uint32_t* idx = &host_indices_[size_t(m.index_base) + index_offset];
+  for (uint32_t t0 = 0; t0 < tris; t0 += kChunkTris) {
+    ChunkBox b{};
+    for (int k = 0; k < 3; ++k) {
+      b.lo[k] = INFINITY;
+      b.hi[k] = -INFINITY;
+    }
+    const uint32_t t1 = std::min(tris, t0 + kChunkTris);
+    for (uint32_t k = t0 * 3; k < t1 * 3; ++k) {
+      const float* p = &host_pos_[(size_t(m.vertex_base) + idx[k]) * 3];
+      for (int c = 0; c < 3; ++c) {
+        b.lo[c] = std::min(b.lo[c], p[c]);
+        b.hi[c] = std::max(b.hi[c], p[c]);
+      }
+    }
+    boxes_.push_back(b);
+  }
 }
 
 gbr_status Renderer::add_file(const char* filename, uint32_t flags, const char* name) {
@@ -469,7 +496,8 @@ gbr_status Renderer::add_node_hierarchy(uint32_t scene, const char* name, const 
              sc.batches[batch].texture == key.texture))
       ++batch;
     if (batch == sc.batches.size()) sc.batches.push_back(key);
-    HostDraw d{batch, nid, top, v.mesh, v.index_offset, v.index_count, v.material, 0u, {}};
+    HostDraw d{batch, nid, top, v.mesh, v.index_offset, v.index_count, v.material, 0u, {},
+               v.box_base, v.chunk_count};
     std::memcpy(d.bbox, v.bbox, 24);
     sc.draws.push_back(d);
   }
@@ -567,8 +595,12 @@ gbr_status Renderer::upload_tables() {
   if (!tables_dirty_) return GBR_OK;
   if (!d_meshes_.reserve(std::max<size_t>(1, meshes_.size()) * sizeof(MeshRec), false) ||
       !d_materials_.reserve(materials_.size() * sizeof(MaterialRec), false) ||
-      !d_textures_.reserve(textures_.size() * sizeof(TextureRec), false))
+      !d_textures_.reserve(textures_.size() * sizeof(TextureRec), false) ||
+      !d_boxes_.reserve(std::max<size_t>(1, boxes_.size()) * sizeof(ChunkBox), false))
     return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of device memory for tables");
+  if (!boxes_.empty())
+    GBR_CUDA(cudaMemcpy(d_boxes_.ptr, boxes_.data(), boxes_.size() * sizeof(ChunkBox),
+                        cudaMemcpyHostToDevice), "table upload");
   if (!meshes_.empty())
     GBR_CUDA(cudaMemcpy(d_meshes_.ptr, meshes_.data(), meshes_.size() * sizeof(MeshRec),
                         cudaMemcpyHostToDevice), "table upload");
@@ -623,6 +655,8 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
       dr.material = d.material;
       dr.semantic_id = d.semantic;
       std::memcpy(dr.bbox, d.bbox, 24);
+      dr.box_base = d.box_base;
+      dr.chunk_count = d.chunk_count;
       draws.push_back(dr);
       tris += dr.tri_count;
     }
@@ -634,15 +668,15 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
   total_draws_ = uint32_t(draws.size());
   total_tris_ = std::accumulate(cost.begin(), cost.end(), uint64_t(0));
 
-  // Work items: each scene's viewport cut into regions of at most
-  // region_width x region_height pixels.
-  std::vector<WorkItem> items;
-  std::vector<uint64_t> item_cost;
+  // Work items: each scene's viewport cut into regions.  The per-scene form
+  // uses small regions so that one scene spreads over several CTAs; the
+  // batched form uses large ones (fewer redundant triangle setups) ordered
+  // longest-processing-time first for the persistent grid.
+  std::vector<WorkItem> items, batched;
+  std::vector<uint64_t> batched_cost;
   scene_item_base_.assign(S, 0);
   scene_item_count_.assign(S, 0);
-  const int rwm = tuning_.region_width, rhm = tuning_.region_height;
-  for (uint32_t s = 0; s < S; ++s) {
-    scene_item_base_[s] = uint32_t(items.size());
+  auto tile = [&](uint32_t s, int rwm, int rhm, std::vector<WorkItem>& out) {
     const SceneState& sc = scenes_[s];
     for (int y = 0; y < sc.height; y += rhm)
       for (int x = 0; x < sc.width; x += rwm) {
@@ -652,19 +686,28 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
         it.y0 = uint16_t(y);
         it.w = uint16_t(std::min(rwm, sc.width - x));
         it.h = uint16_t(std::min(rhm, sc.height - y));
-        items.push_back(it);
-        item_cost.push_back(cost[s] + 1);
+        out.push_back(it);
       }
+  };
+  for (uint32_t s = 0; s < S; ++s) {
+    scene_item_base_[s] = uint32_t(items.size());
+    tile(s, tuning_.plain_region_width, tuning_.plain_region_height, items);
     scene_item_count_[s] = uint32_t(items.size()) - scene_item_base_[s];
+    const size_t before = batched.size();
+    tile(s, tuning_.region_width, tuning_.region_height, batched);
+    const SceneState& sc = scenes_[s];
+    for (size_t k = before; k < batched.size(); ++k)
+      batched_cost.push_back((cost[s] + 1) * uint64_t(batched[k].w) * batched[k].h /
+                             (uint64_t(sc.width) * sc.height) + cost[s] / 4);
   }
   item_count_ = uint32_t(items.size());
-  // Longest-processing-time-first order for the persistent grid.
-  std::vector<uint32_t> perm(items.size());
+  lpt_count_ = uint32_t(batched.size());
+  std::vector<uint32_t> perm(batched.size());
   std::iota(perm.begin(), perm.end(), 0u);
   std::stable_sort(perm.begin(), perm.end(),
-                   [&](uint32_t a, uint32_t b) { return item_cost[a] > item_cost[b]; });
-  std::vector<WorkItem> lpt(items.size());
-  for (size_t i = 0; i < perm.size(); ++i) lpt[i] = items[perm[i]];
+                   [&](uint32_t a, uint32_t b) { return batched_cost[a] > batched_cost[b]; });
+  std::vector<WorkItem> lpt(batched.size());
+  for (size_t i = 0; i < perm.size(); ++i) lpt[i] = batched[perm[i]];
 
   cudaSetDevice(device_);
   if (gbr_status st = upload_tables()) return st;
@@ -676,9 +719,10 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
       !d_cameras_.reserve(S1 * kCameraBytes, false) ||
       !d_visible_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(VisibleRec), false) ||
       !d_vis_count_.reserve(S1 * 4, false) || !d_vis_tris_.reserve(S1 * 4, false) ||
+      !d_vis_chunks_.reserve(S1 * 4, false) ||
       !d_status_.reserve(4, false) || !d_counter_.reserve(4, false) ||
       !d_items_.reserve(std::max<size_t>(items.size(), 1) * sizeof(WorkItem), false) ||
-      !d_items_lpt_.reserve(std::max<size_t>(items.size(), 1) * sizeof(WorkItem), false) ||
+      !d_items_lpt_.reserve(std::max<size_t>(lpt.size(), 1) * sizeof(WorkItem), false) ||
       !h_stage_.reserve(S1 * kCameraBytes + std::max<size_t>(nodes, 1) * 64))
     return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of memory for scene data");
   GBR_CUDA(cudaMemcpy(d_scenes_.ptr, recs.data(), S * sizeof(SceneRec), cudaMemcpyHostToDevice),
@@ -689,12 +733,12 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
   if (!draws.empty())
     GBR_CUDA(cudaMemcpy(d_draws_.ptr, draws.data(), draws.size() * sizeof(DrawRec),
                         cudaMemcpyHostToDevice), "scene upload");
-  if (!items.empty()) {
+  if (!items.empty())
     GBR_CUDA(cudaMemcpy(d_items_.ptr, items.data(), items.size() * sizeof(WorkItem),
                         cudaMemcpyHostToDevice), "scene upload");
+  if (!lpt.empty())
     GBR_CUDA(cudaMemcpy(d_items_lpt_.ptr, lpt.data(), lpt.size() * sizeof(WorkItem),
                         cudaMemcpyHostToDevice), "scene upload");
-  }
   GBR_CUDA(cudaMemset(d_status_.ptr, 0, 4), "scene upload");
   for (auto& sc : scenes_) sc.transforms_dirty = true;
   structure_dirty_ = false;
@@ -705,21 +749,24 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
 gbr_status Renderer::ensure_raster_config() {
   if (raster_configured_) return GBR_OK;
   const int region_px = tuning_.region_width * tuning_.region_height;
+  const int plain_px = tuning_.plain_region_width * tuning_.plain_region_height;
   size_t max_dyn = 0;
   GBR_CUDA(raster_configure(tuning_.threads, &max_dyn), "raster configure");
   int cap = kPrefixCapMax;
-  size_t smem = raster_smem_bytes(tuning_.threads, region_px, cap);
+  size_t smem = raster_smem_bytes(tuning_.threads, std::max(region_px, plain_px), cap);
   while (smem > max_dyn && cap > 64) {
     cap /= 2;
-    smem = raster_smem_bytes(tuning_.threads, region_px, cap);
+    smem = raster_smem_bytes(tuning_.threads, std::max(region_px, plain_px), cap);
   }
   if (smem > max_dyn)
     return fail(GBR_ERROR_INVALID_ARGUMENT, "tuning: region does not fit in shared memory");
+  smem = raster_smem_bytes(tuning_.threads, region_px, cap);
   int occ = 0;
   GBR_CUDA(raster_max_ctas_per_sm(tuning_.threads, smem, &occ), "raster occupancy");
   if (occ < 1) return fail(GBR_ERROR_INVALID_ARGUMENT, "tuning: raster kernel cannot be resident");
   ctas_per_sm_ = std::min(occ, std::max(1, tuning_.ctas_per_sm));
   smem_bytes_ = smem;
+  smem_plain_ = raster_smem_bytes(tuning_.threads, plain_px, cap);
   prefix_cap_ = cap;
   raster_configured_ = true;
   return GBR_OK;
@@ -776,12 +823,15 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   pp.visible = d_visible_.as<VisibleRec>();
   pp.vis_count = d_vis_count_.as<uint32_t>();
   pp.vis_tris = d_vis_tris_.as<uint32_t>();
+  pp.vis_chunks = d_vis_chunks_.as<uint32_t>();
   pp.status = d_status_.as<uint32_t>();
   RasterParams rp{};
   rp.scenes = pp.scenes;
   rp.visible = pp.visible;
   rp.vis_count = pp.vis_count;
   rp.vis_tris = pp.vis_tris;
+  rp.vis_chunks = pp.vis_chunks;
+  rp.boxes = d_boxes_.as<ChunkBox>();
   rp.pos = d_pos_.as<float4>();
   rp.color = d_color_.as<float4>();
   rp.uv = d_uv_.as<float2>();
@@ -796,7 +846,6 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   rp.out.depth = (cfg_.planes & GBR_PLANE_DEPTH) ? d_planes_[1].as<float>() : nullptr;
   rp.out.linear = (cfg_.planes & GBR_PLANE_LINEAR_DEPTH) ? d_planes_[2].as<float>() : nullptr;
   rp.out.semantic = (cfg_.planes & GBR_PLANE_SEMANTIC) ? d_planes_[3].as<uint32_t>() : nullptr;
-  rp.region_px = tuning_.region_width * tuning_.region_height;
   rp.prefix_cap = prefix_cap_;
   rp.small_area = tuning_.small_area;
   uint64_t launches = 0;
@@ -808,22 +857,24 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
     if (timing_) GBR_CUDA(cudaEventRecordWithFlags(ev_[1], stream, cudaEventRecordExternal), "timing event");
     rp.items = d_items_lpt_.as<WorkItem>();
     rp.item_base = 0;
-    rp.item_count = item_count_;
+    rp.item_count = lpt_count_;
     rp.persistent = 1;
+    rp.region_px = tuning_.region_width * tuning_.region_height;
     const uint32_t grid =
-        std::min<uint32_t>(item_count_, uint32_t(sm_count_) * uint32_t(ctas_per_sm_));
+        std::min<uint32_t>(lpt_count_, uint32_t(sm_count_) * uint32_t(ctas_per_sm_));
     GBR_CUDA(launch_raster(rp, tuning_.threads, grid, smem_bytes_, stream), "raster launch");
     if (timing_) GBR_CUDA(cudaEventRecordWithFlags(ev_[2], stream, cudaEventRecordExternal), "timing event");
     launches = 2;
   } else {
     rp.items = d_items_.as<WorkItem>();
     rp.persistent = 0;
+    rp.region_px = tuning_.plain_region_width * tuning_.plain_region_height;
     for (uint32_t s = 0; s < S; ++s) {
       pp.scene_base = s;
       GBR_CUDA(launch_prepare(pp, 1, stream), "prepare launch");
       rp.item_base = scene_item_base_[s];
       rp.item_count = scene_item_count_[s];
-      GBR_CUDA(launch_raster(rp, tuning_.threads, scene_item_count_[s], smem_bytes_, stream),
+      GBR_CUDA(launch_raster(rp, tuning_.threads, scene_item_count_[s], smem_plain_, stream),
                "raster launch");
       launches += 2;
     }
@@ -1032,7 +1083,9 @@ gbr_status Renderer::get_tuning(gbr_tuning* t) const {
 gbr_status Renderer::set_tuning(const gbr_tuning& t) {
   if ((t.threads != 256 && t.threads != 512 && t.threads != 1024) || t.region_width < 4 ||
       t.region_height < 1 || t.region_width > 1024 || t.region_height > 1024 ||
-      t.region_width * t.region_height > 32768 || t.small_area < 1 || t.ctas_per_sm < 1)
+      t.region_width * t.region_height > 32768 || t.small_area < 1 || t.ctas_per_sm < 1 ||
+      t.plain_region_width < 4 || t.plain_region_height < 1 || t.plain_region_width > 1024 ||
+      t.plain_region_height > 1024 || t.plain_region_width * t.plain_region_height > 32768)
     return fail(GBR_ERROR_INVALID_ARGUMENT, "setTuning: out of range");
   tuning_ = t;
   raster_configured_ = false;

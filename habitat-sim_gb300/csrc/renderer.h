@@ -37,11 +37,14 @@ struct MeshView {
   uint32_t mesh, index_offset, index_count, material;
   float transform[16];
   float bbox[6];
+  uint32_t box_base;     // first chunk box of this view
+  uint32_t chunk_count;  // 32-triangle chunks of this view
 };
 
 struct HostDraw {
   uint32_t batch, node, top, mesh, index_offset, index_count, material, semantic;
   float bbox[6];
+  uint32_t box_base, chunk_count;
 };
 
 struct BatchKey {
@@ -121,6 +124,7 @@ class Renderer {
   gbr_status upload_step(cudaStream_t stream);
   gbr_status enqueue_step(cudaStream_t stream, uint32_t mode);
   gbr_status ensure_raster_config();
+  void build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count);
   void* plane_ptr(uint32_t plane, size_t* elem) const;
   gbr_status sync_and_check();
 
@@ -139,6 +143,7 @@ class Renderer {
   uint64_t texel_count_ = 0;
   std::vector<MaterialRec> materials_;
   std::vector<MeshView> views_;
+  std::vector<ChunkBox> boxes_;
   std::unordered_map<std::string, std::pair<uint32_t, uint32_t>> names_;
   uint32_t vertex_count_ = 0, index_count_ = 0;
   bool tables_dirty_ = true;
@@ -148,9 +153,10 @@ class Renderer {
 
   // device
   DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_;
-  DeviceBuffer d_meshes_, d_materials_, d_textures_;
+  DeviceBuffer d_meshes_, d_materials_, d_textures_, d_boxes_;
   DeviceBuffer d_scenes_, d_parents_, d_local_, d_draws_, d_cameras_;
-  DeviceBuffer d_visible_, d_vis_count_, d_vis_tris_, d_status_, d_items_, d_items_lpt_, d_counter_;
+  DeviceBuffer d_visible_, d_vis_count_, d_vis_tris_, d_vis_chunks_, d_status_, d_items_,
+      d_items_lpt_, d_counter_;
   DeviceBuffer d_planes_[4];
   PinnedBuffer h_stage_;
   cudaEvent_t upload_done_ = nullptr;
@@ -161,10 +167,10 @@ class Renderer {
   uint32_t total_nodes_ = 0, total_draws_ = 0;
   uint64_t total_tris_ = 0;
   std::vector<uint32_t> scene_item_base_, scene_item_count_;
-  uint32_t item_count_ = 0;
+  uint32_t item_count_ = 0, lpt_count_ = 0;
 
-  gbr_tuning tuning_{512, 128, 128, 64, 1};
-  size_t smem_bytes_ = 0;
+  gbr_tuning tuning_{1024, 128, 128, 8, 1, 32, 32};
+  size_t smem_bytes_ = 0, smem_plain_ = 0;
   int prefix_cap_ = 0;
   bool raster_configured_ = false;
   int ctas_per_sm_ = 1;

@@ -229,12 +229,15 @@ gbr_status gbr_unproject_depth_device(const float unprojection[2], float* depth,
 /* Tuning of the raster kernel (chosen by the autotuner). */
 typedef struct gbr_tuning {
   int32_t threads;        /* threads per CTA: 256, 512 or 1024              */
-  int32_t region_width;   /* max pixels per CTA region, x (multiple of 4)   */
-  int32_t region_height;  /* max pixels per CTA region, y                   */
+  int32_t region_width;   /* batched form: max pixels per CTA region, x     */
+  int32_t region_height;  /* batched form: max pixels per CTA region, y     */
   int32_t small_area;     /* bounding boxes up to this many pixels are
-                             rasterised by one thread, larger ones by the
-                             whole CTA from a shared-memory bin            */
-  int32_t ctas_per_sm;    /* persistent grid = SMs x this                   */
+                             rasterised by one lane, larger ones by the
+                             whole warp                                    */
+  int32_t ctas_per_sm;    /* persistent grid = SMs x this (capped by
+                             occupancy)                                    */
+  int32_t plain_region_width;  /* per-scene form: region size, so that one */
+  int32_t plain_region_height; /* scene spreads over several CTAs          */
 } gbr_tuning;
 gbr_status gbr_get_tuning(gbr_renderer* r, gbr_tuning* out);
 gbr_status gbr_set_tuning(gbr_renderer* r, const gbr_tuning* tuning);
