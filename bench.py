@@ -218,6 +218,11 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     steps = args.warmup + args.steps
     poses = [procedural.camera_poses(wl, i) for i in range(steps)]
+    # Launch shape chosen by the autotuner (cached per GPU and workload).
+    from habitat_sim_gb300 import autotune
+    tuned, tune_report = autotune.tune(r, [procedural.camera_poses(wl, 1000 + i) for i in range(3)],
+                                       int(wl.triangles_per_env().sum()),
+                                       cache=os.path.join(ROOT, "gpurun_out", "autotune.json"))
 
     def batched_step(i, events=None):
         flush.zero_()
@@ -361,7 +366,9 @@ def main():
                        "l2": "flushed with a 256 MiB write before every step (outside timing)",
                        "triangles_per_step_after_draw_culling": tri,
                        "triangles_per_step_before_culling": int(wl.triangles_per_env().sum()),
-                       "tuning": r.tuning()},
+                       "tuning": r.tuning(),
+                       "autotune": {"cached": tune_report["cached"],
+                                    "candidates": len(tune_report.get("trials", []))}},
             "plain": None if not plain_ms else {
                 "value": plain_fps, "unit": "frames/s", "ms_per_step": statistics.mean(plain_ms),
                 "p50_ms": float(np.percentile(plain_ms, 50)),

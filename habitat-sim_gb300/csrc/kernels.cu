@@ -756,8 +756,15 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
           const uint32_t t = ch.y * kChunkTris + (g % kChunkTris);
           if (t < __ldg(&rec->tri_count)) {
             float mvp[16];
+            const float4* m4 = reinterpret_cast<const float4*>(rec->mvp);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) mvp[i] = __ldg(&rec->mvp[i]);
+            for (int i = 0; i < 4; ++i) {
+              const float4 v = __ldg(m4 + i);
+              mvp[4 * i] = v.x;
+              mvp[4 * i + 1] = v.y;
+              mvp[4 * i + 2] = v.z;
+              mvp[4 * i + 3] = v.w;
+            }
             const uint32_t vb = __ldg(&rec->vertex_base);
             const uint32_t fi = __ldg(&rec->first_index) + 3u * t;
             float4 cv[3];

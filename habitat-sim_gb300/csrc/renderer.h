@@ -169,7 +169,7 @@ class Renderer {
   std::vector<uint32_t> scene_item_base_, scene_item_count_;
   uint32_t item_count_ = 0, lpt_count_ = 0;
 
-  gbr_tuning tuning_{1024, 128, 128, 8, 1, 32, 32};
+  gbr_tuning tuning_{1024, 128, 128, 1, 1, 16, 32};
   size_t smem_bytes_ = 0, smem_plain_ = 0;
   int prefix_cap_ = 0;
   bool raster_configured_ = false;
