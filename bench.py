@@ -21,7 +21,10 @@ Printed (rank 0, one JSON line):
                framebuffer written plus the unique geometry and textures;
   cpu_baseline the CPU oracle (the renderer restated in C++) on a bounded
                sample of the same envs, all host threads;
-  parity       sampled envs of the timed workload against the oracle.
+  parity       sampled envs of the timed workload against the oracle;
+  serving      request serving over 256 scenes (continuous batching, LRU
+               device budget): saturation requests/s, p50/p99 latency under
+               Poisson arrivals, an eviction run with a small budget.
 
 ``--impl reference`` times the CPU restatement alone on this workload (the
 reference renderer itself is GL-only and cannot run here)."""
@@ -56,6 +59,9 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--envs", type=int, default=1024)
+    p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--serving-scenes", type=int, default=256)
+    p.add_argument("--serving-requests", type=int, default=20000)
     return p.parse_args()
 
 
@@ -152,6 +158,61 @@ def cpu_frames_per_s(procedural, wl, seconds, threads):
             break
         n *= 2
     return best[0] / best[1], best[0], best[1]
+
+
+def serving_leg(pkg, args):
+    """Request serving over a catalog of procedural scenes (triangles
+    log-uniform in 10k-1M, resolution 64/128/256 with p 0.3/0.5/0.2, 6-DoF
+    poses): continuous batching into 96 + 64 + 16 render slots per step, one
+    graph launch per step, slot rectangles copied back to pinned host memory
+    overlapped with the next step.  A closed-loop run (every request pending
+    at the start) gives the saturation rate; Poisson arrivals at 50 % and
+    80 % of it give latency percentiles (arrival to images in host memory);
+    a run with the device budget at a quarter of the catalog's bytes, Zipf(1)
+    scene popularity and 500 requests/s exercises LRU eviction."""
+    from habitat_sim_gb300 import server
+    slots = {64: 96, 128: 64, 256: 16}
+    cat = server.SceneCatalog(args.serving_scenes, seed=4, tri_range=(1e4, 1e6))
+    t0 = time.perf_counter()
+    assets = [cat.asset(s) for s in range(len(cat))]
+    gen_s = time.perf_counter() - t0
+    total_bytes = sum(a.device_bytes() for a in assets)
+    tris = [a.triangles for a in assets]
+    n = args.serving_requests
+    out = {"workload": ("serving: %d procedural scenes (room shell + 20 boxes, %d-%d triangles, "
+                        "mean %d, log-uniform), requests (scene, 6-DoF pose, 64/128/256 px "
+                        "with p 0.3/0.5/0.2)" % (len(cat), min(tris), max(tris),
+                                                  int(np.mean(tris)))),
+           "slots": slots, "catalog_bytes": total_bytes, "catalog_generation_s": gen_s,
+           "planes": "rgba8 + f32 linear depth + u32 semantic id per request",
+           "latency": "arrival to all three images in host memory"}
+    srv = server.RenderServer(pkg, cat, slots=slots, max_resident=len(cat),
+                              budget_bytes=150 * 10**9)
+    warm = server.random_requests(cat, max(len(cat), 2000), rate=0, seed=100)
+    for s, q in enumerate(warm[:len(cat)]):
+        q.scene = s                       # every scene resident before timing
+    t0 = time.perf_counter()
+    srv.serve(warm, realtime=False)
+    out["warm_load_s"] = time.perf_counter() - t0
+
+    def keep(st):
+        return {k: st[k] for k in ("requests", "requests_per_s", "p50_ms", "p99_ms", "mean_ms",
+                                   "mean_batch", "steps", "loads", "evictions", "elapsed_s")}
+    sat = srv.serve(server.random_requests(cat, n, rate=0, seed=101), realtime=False)
+    out["saturation"] = keep(sat)
+    rate = sat["requests_per_s"]
+    out["open_loop"] = []
+    for k, frac in enumerate((0.5, 0.8)):
+        st = srv.serve(server.random_requests(cat, n // 2, rate=frac * rate, seed=102 + k))
+        out["open_loop"].append(dict(offered_per_s=frac * rate, **keep(st)))
+    srv.close()
+    budget = total_bytes // 4
+    srv = server.RenderServer(pkg, cat, slots=slots, max_resident=len(cat), budget_bytes=budget)
+    st = srv.serve(server.random_requests(cat, 2500, rate=500.0, seed=110, zipf=1.0))
+    out["small_budget"] = dict(budget_bytes=budget, offered_per_s=500.0, popularity="zipf 1.0",
+                               **keep(st))
+    srv.close()
+    return out
 
 
 def run_reference_impl(args):
@@ -345,6 +406,8 @@ def main():
             if line.startswith("dram_bytes_per_launch:"):
                 traffic = float(line.split(":")[1])
 
+    serving = None if args.no_serving else serving_leg(pkg, args)
+
     cpu_baseline = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -390,6 +453,7 @@ def main():
             "clocks": clocks,
             "parity": parity,
             "cpu_baseline": cpu_baseline,
+            "serving": serving,
         }
         print(json.dumps(line))
     r.close()

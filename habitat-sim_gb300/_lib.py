@@ -79,6 +79,12 @@ PROTOTYPES = {
     "gbr_add_texture": (_ST, [_P, ctypes.POINTER(TextureData), ctypes.POINTER(_U32)]),
     "gbr_add_material": (_ST, [_P, ctypes.POINTER(MaterialData), ctypes.POINTER(_U32)]),
     "gbr_add_node_hierarchy_template": (_ST, [_P, ctypes.c_char_p, _U32, ctypes.POINTER(MeshView)]),
+    "gbr_set_scene_sources": (_ST, [_P, _U32, _U32, ctypes.POINTER(_U32)]),
+    "gbr_set_scene_enabled": (_ST, [_P, _U32, _I32]),
+    "gbr_remove_mesh": (_ST, [_P, _U32]),
+    "gbr_remove_texture": (_ST, [_P, _U32]),
+    "gbr_remove_node_hierarchy_template": (_ST, [_P, ctypes.c_char_p]),
+    "gbr_memory_usage": (_ST, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     "gbr_has_node_hierarchy": (_ST, [_P, ctypes.c_char_p, ctypes.POINTER(_I32)]),
     "gbr_add_node_hierarchy": (_ST, [_P, _U32, ctypes.c_char_p, c_float_p, ctypes.POINTER(_U64)]),
     "gbr_add_empty_node": (_ST, [_P, _U32, ctypes.POINTER(_U64)]),

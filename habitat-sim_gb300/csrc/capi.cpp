@@ -165,6 +165,38 @@ gbr_status gbr_add_node_hierarchy_template(gbr_renderer* r, const char* name, ui
   return guarded([&] { return R(r)->add_template(name, count, views); });
 }
 
+gbr_status gbr_set_scene_sources(gbr_renderer* r, uint32_t first, uint32_t count,
+                                 const uint32_t* sources) {
+  GBR_HANDLE(r);
+  return guarded([&] { return R(r)->set_sources(first, count, sources); });
+}
+
+gbr_status gbr_set_scene_enabled(gbr_renderer* r, uint32_t scene, int32_t enabled) {
+  GBR_HANDLE(r);
+  return guarded([&] { return R(r)->set_enabled(scene, enabled != 0); });
+}
+
+gbr_status gbr_remove_mesh(gbr_renderer* r, uint32_t mesh) {
+  GBR_HANDLE(r);
+  return guarded([&] { return R(r)->remove_mesh(mesh); });
+}
+
+gbr_status gbr_remove_texture(gbr_renderer* r, uint32_t texture) {
+  GBR_HANDLE(r);
+  return guarded([&] { return R(r)->remove_texture(texture); });
+}
+
+gbr_status gbr_remove_node_hierarchy_template(gbr_renderer* r, const char* name) {
+  GBR_HANDLE(r);
+  GBR_ARG(name);
+  return guarded([&] { return R(r)->remove_template(name); });
+}
+
+gbr_status gbr_memory_usage(gbr_renderer* r, uint64_t* live_bytes, uint64_t* reserved_bytes) {
+  GBR_HANDLE(r);
+  return guarded([&] { return R(r)->memory_usage(live_bytes, reserved_bytes); });
+}
+
 gbr_status gbr_has_node_hierarchy(gbr_renderer* r, const char* name, int32_t* out) {
   GBR_HANDLE(r);
   GBR_ARG(name);

@@ -129,7 +129,14 @@ template <int T>
 __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
   __shared__ uint32_t s_warp[T / 32], s_total, s_count, s_tris, s_chunks;
   const uint32_t s = p.scene_base + blockIdx.x;
-  const SceneRec sc = p.scenes[s];
+  const CameraRec& cam = p.cameras[s];
+  const uint32_t vis_base = cam.vis_base;
+  if (!cam.enabled) {
+    if (threadIdx.x == 0) p.vis_count[s] = p.vis_tris[s] = p.vis_chunks[s] = 0;
+    return;
+  }
+  // The scene renders the nodes and draws of its source scene.
+  const SceneRec sc = p.scenes[cam.source];
   if (threadIdx.x == 0) {
     s_count = 0;
     s_tris = 0;
@@ -137,9 +144,9 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
   }
   float pv[16], vrow[4];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) pv[i] = p.cameras[s].pv[i];
+  for (int i = 0; i < 16; ++i) pv[i] = cam.pv[i];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) vrow[i] = p.cameras[s].vrow[i];
+  for (int i = 0; i < 4; ++i) vrow[i] = cam.vrow[i];
   __syncthreads();
   for (uint32_t base = 0; base < sc.draw_count; base += T) {
     const uint32_t j = base + threadIdx.x;
@@ -225,7 +232,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
     if (vis) {
       rec.ordinal = s_tris + to;
       rec.chunk = s_chunks + co;
-      p.visible[sc.draw_base + s_count + vo] = rec;
+      p.visible[vis_base + s_count + vo] = rec;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -681,6 +688,8 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
     const uint32_t item = s_item;
     if (item >= p.item_count) return;
     const WorkItem wi = p.items[p.item_base + item];
+    const uint32_t vis_base = p.cameras[wi.scene].vis_base;
+    if (!p.cameras[wi.scene].enabled) continue;  // disabled scene: pixels untouched
     const SceneRec sc = p.scenes[wi.scene];
     Ctx c;
     c.keys = keys;
@@ -698,7 +707,7 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
     for (int i = threadIdx.x; i < npx; i += T) keys[i] = kEmptyKey;
     const uint32_t nvis = p.vis_count[wi.scene];
     const uint32_t total = p.vis_tris[wi.scene];
-    const VisibleRec* vis = p.visible + sc.draw_base;
+    const VisibleRec* vis = p.visible + vis_base;
     const bool cached = nvis <= uint32_t(p.prefix_cap);
     if (cached)
       for (uint32_t i = threadIdx.x; i < nvis; i += T) prefix[i] = vis[i].ordinal;
@@ -955,6 +964,7 @@ constexpr size_t kNoAllocScratchBytes = 16384;
 constexpr int kNoAllocMaxDevices = 64;
 
 struct NoAllocScratch {
+  CameraRec camera;
   SceneRec scene;
   VisibleRec visible;
   MaterialRec material;
@@ -998,6 +1008,13 @@ __global__ void no_alloc_setup(const NoAllocSetup a, NoAllocScratch* s) {
     sc.draw_base = 0;
     sc.draw_count = 1;
     s->scene = sc;
+    CameraRec cam{};
+    for (int i = 0; i < 16; ++i) cam.pv[i] = a.pv[i];
+    for (int i = 0; i < 4; ++i) cam.vrow[i] = a.vrow[i];
+    cam.source = 0;
+    cam.vis_base = 0;
+    cam.enabled = 1;
+    s->camera = cam;
     // The mesh sits under an identity root and an identity child, as a
     // hierarchy added without a bake transform: abs = I * I, MVP = PV * abs.
     float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
@@ -1133,6 +1150,7 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
     return no_alloc_fail(GBR_ERROR_CUDA, "raster kernel configuration failed");
   RasterParams p{};
   p.scenes = &s->scene;
+  p.cameras = &s->camera;
   p.visible = &s->visible;
   p.vis_count = &s->vis_count;
   p.vis_tris = &s->vis_tris;

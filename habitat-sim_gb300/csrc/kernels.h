@@ -40,6 +40,7 @@ struct PrepareParams {
 // writes.
 struct RasterParams {
   const SceneRec* scenes;
+  const CameraRec* cameras;   // binding of each scene (vis_base, enabled)
   const VisibleRec* visible;
   const uint32_t* vis_count;
   const uint32_t* vis_tris;

@@ -68,10 +68,18 @@ struct DrawRec {
   uint32_t pad[2];
 };
 
+// Per-scene state uploaded every step: the camera and the scene's binding
+// (which scene's nodes and draws it renders, where its visible records go,
+// whether it is drawn at all).
 struct CameraRec {
-  float pv[16];     // projection * view
-  float vrow[4];    // row 2 of the view matrix
+  float pv[16];       // projection * view
+  float vrow[4];      // row 2 of the view matrix
+  uint32_t source;    // scene whose nodes and draws are rendered
+  uint32_t vis_base;  // first visible record of this scene
+  uint32_t enabled;   // 0: not drawn, framebuffer rectangle untouched
+  uint32_t pad;
 };
+static_assert(sizeof(CameraRec) == 96, "CameraRec layout");
 
 // 16-byte aligned: the raster kernel reads the matrix with float4 loads.
 struct alignas(16) VisibleRec {

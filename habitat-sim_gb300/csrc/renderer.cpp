@@ -71,6 +71,45 @@ bool DeviceBuffer::reserve(size_t n, bool keep, cudaStream_t stream) {
   return true;
 }
 
+uint64_t RangePool::alloc(uint64_t n) {
+  if (n == 0) return 0;
+  for (auto it = free.begin(); it != free.end(); ++it) {
+    if (it->second < n) continue;
+    const uint64_t off = it->first, rest = it->second - n;
+    free.erase(it);
+    if (rest) free.emplace(off + n, rest);
+    free_total -= n;
+    return off;
+  }
+  const uint64_t off = end;
+  end += n;
+  return off;
+}
+
+void RangePool::release(uint64_t offset, uint64_t n) {
+  if (n == 0) return;
+  auto it = free.emplace(offset, n).first;
+  free_total += n;
+  auto next = std::next(it);
+  if (next != free.end() && it->first + it->second == next->first) {
+    it->second += next->second;
+    free.erase(next);
+  }
+  if (it != free.begin()) {
+    auto prev = std::prev(it);
+    if (prev->first + prev->second == it->first) {
+      prev->second += it->second;
+      free.erase(it);
+      it = prev;
+    }
+  }
+  if (it->first + it->second == end) {  // the tail is free: shrink
+    end = it->first;
+    free_total -= it->second;
+    free.erase(it);
+  }
+}
+
 PinnedBuffer::~PinnedBuffer() {
   if (ptr) cudaFreeHost(ptr);
 }
@@ -187,9 +226,11 @@ Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
       sc.fb_offset = int64_t(y) * th * r->fb_w_ + int64_t(x) * tw;
     }
   }
-  for (auto& sc : r->scenes_) {
+  for (uint32_t s = 0; s < n; ++s) {
+    SceneState& sc = r->scenes_[s];
     std::memcpy(sc.pv, kIdentity, 64);
     std::memcpy(sc.view, kIdentity, 64);
+    sc.source = s;
   }
   for (int i = 0; i < 4; ++i)
     if (r->cfg_.planes & (1u << i))
@@ -235,20 +276,28 @@ Renderer::~Renderer() {
 gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
   if (!m.positions || (m.index_count && !m.indices))
     return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: positions and indices are required");
-  if (uint64_t(vertex_count_) + m.vertex_count > 0xffffffffull ||
-      uint64_t(index_count_) + m.index_count > 0xffffffffull)
-    return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: more than 2^32 vertices or indices");
   for (uint32_t i = 0; i < m.index_count; ++i)
     if (m.indices[i] >= m.vertex_count)
       return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: index " + std::to_string(i) +
                                                   " out of range for " +
                                                   std::to_string(m.vertex_count) + " vertices");
   cudaSetDevice(device_);
-  const size_t nv = m.vertex_count, vb = vertex_count_;
-  if (!d_pos_.reserve((vb + nv) * 16, true) || !d_color_.reserve((vb + nv) * 16, true) ||
-      !d_uv_.reserve((vb + nv) * 8, true) ||
-      !d_indices_.reserve((size_t(index_count_) + m.index_count) * 4, true))
+  const size_t nv = m.vertex_count;
+  const uint64_t vb = vertex_pool_.alloc(nv), ib = index_pool_.alloc(m.index_count);
+  auto undo = [&]() {
+    vertex_pool_.release(vb, nv);
+    index_pool_.release(ib, m.index_count);
+  };
+  if (vb + nv > 0xffffffffull || ib + m.index_count > 0xffffffffull) {
+    undo();
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: more than 2^32 vertices or indices");
+  }
+  const size_t ve = vertex_pool_.end, ie = index_pool_.end;
+  if (!d_pos_.reserve(ve * 16, true) || !d_color_.reserve(ve * 16, true) ||
+      !d_uv_.reserve(ve * 8, true) || !d_indices_.reserve(std::max<size_t>(ie, 1) * 4, true)) {
+    undo();
     return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of device memory");
+  }
   std::vector<float> pos(nv * 4), col(nv * 4), uv(nv * 2, 0.0f);
   for (size_t v = 0; v < nv; ++v) {
     pos[v * 4 + 0] = m.positions[v * 3 + 0];
@@ -269,21 +318,22 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
   GBR_CUDA(cudaMemcpy(d_uv_.as<char>() + vb * 8, uv.data(), nv * 8, cudaMemcpyHostToDevice),
            "addMesh upload");
   if (m.index_count)
-    GBR_CUDA(cudaMemcpy(d_indices_.as<char>() + size_t(index_count_) * 4, m.indices,
+    GBR_CUDA(cudaMemcpy(d_indices_.as<char>() + size_t(ib) * 4, m.indices,
                         size_t(m.index_count) * 4, cudaMemcpyHostToDevice),
              "addMesh upload");
   MeshRec rec{};
-  rec.vertex_base = vertex_count_;
+  rec.vertex_base = uint32_t(vb);
   rec.vertex_count = m.vertex_count;
-  rec.index_base = index_count_;
+  rec.index_base = uint32_t(ib);
   rec.index_count = m.index_count;
   rec.flags = (m.colors ? kMeshVertexColor : 0u) | (m.object_ids ? kMeshObjectId : 0u) |
               (m.texcoords ? kMeshTexcoords : 0u);
   meshes_.push_back(rec);
-  host_pos_.insert(host_pos_.end(), m.positions, m.positions + nv * 3);
-  host_indices_.insert(host_indices_.end(), m.indices, m.indices + m.index_count);
-  vertex_count_ += m.vertex_count;
-  index_count_ += m.index_count;
+  mesh_live_.push_back(true);
+  if (host_pos_.size() < ve * 3) host_pos_.resize(ve * 3);
+  if (host_indices_.size() < ie) host_indices_.resize(ie);
+  std::copy(m.positions, m.positions + nv * 3, host_pos_.begin() + vb * 3);
+  std::copy(m.indices, m.indices + m.index_count, host_indices_.begin() + ib);
   tables_dirty_ = true;
   graph_valid_ = false;
   *id = uint32_t(meshes_.size() - 1);
@@ -297,13 +347,15 @@ gbr_status Renderer::add_texture(const gbr_texture_data& t, uint32_t* id) {
     return fail(GBR_ERROR_INVALID_ARGUMENT, "addTexture: bad filter or wrap mode");
   cudaSetDevice(device_);
   const size_t n = size_t(t.width) * t.height * t.layers;
-  if (!d_texels_.reserve((texel_count_ + n) * 4, true))
+  const uint64_t off = texel_pool_.alloc(n);
+  if (!d_texels_.reserve(texel_pool_.end * 4, true)) {
+    texel_pool_.release(off, n);
     return fail(GBR_ERROR_OUT_OF_MEMORY, "addTexture: out of device memory");
-  GBR_CUDA(cudaMemcpy(d_texels_.as<char>() + texel_count_ * 4, t.rgba8, n * 4,
-                      cudaMemcpyHostToDevice),
+  }
+  GBR_CUDA(cudaMemcpy(d_texels_.as<char>() + off * 4, t.rgba8, n * 4, cudaMemcpyHostToDevice),
            "addTexture upload");
   TextureRec rec{};
-  rec.offset = texel_count_;
+  rec.offset = off;
   rec.width = t.width;
   rec.height = t.height;
   rec.layers = t.layers;
@@ -311,7 +363,7 @@ gbr_status Renderer::add_texture(const gbr_texture_data& t, uint32_t* id) {
   rec.wrap_s = t.wrap_s;
   rec.wrap_t = t.wrap_t;
   textures_.push_back(rec);
-  texel_count_ += n;
+  texture_live_.push_back(true);
   tables_dirty_ = true;
   graph_valid_ = false;
   *id = uint32_t(textures_.size() - 1);
@@ -341,6 +393,9 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
     const gbr_mesh_view& v = views[i];
     if (v.mesh >= meshes_.size() || v.material >= materials_.size())
       return fail(GBR_ERROR_INVALID_ARGUMENT, "addNodeHierarchyTemplate: bad mesh or material id");
+    if (!mesh_live_[v.mesh])
+      return fail(GBR_ERROR_STATE, "addNodeHierarchyTemplate: mesh " + std::to_string(v.mesh) +
+                                       " was removed");
     const MeshRec& m = meshes_[v.mesh];
     if (uint64_t(v.index_offset) + v.index_count > m.index_count)
       return fail(GBR_ERROR_INVALID_ARGUMENT, "addNodeHierarchyTemplate: index range out of mesh");
@@ -367,9 +422,11 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
       mv.bbox[c] = lo[c];
       mv.bbox[3 + c] = hi[c];
     }
-    mv.box_base = uint32_t(boxes_.size());
-    build_chunk_boxes(m, v.index_offset, v.index_count);
-    mv.chunk_count = uint32_t(boxes_.size()) - mv.box_base;
+    mv.chunk_count = (v.index_count / 3 + kChunkTris - 1) / kChunkTris;
+    mv.box_base = uint32_t(box_pool_.alloc(mv.chunk_count));
+    if (boxes_.size() < box_pool_.end) boxes_.resize(box_pool_.end);
+    build_chunk_boxes(m, v.index_offset, v.index_count, mv.box_base);
+    mv.live = true;
     views_.push_back(mv);
   }
   names_[name] = {begin, uint32_t(views_.size())};
@@ -379,7 +436,8 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
 }
 
 // Object-space bounding box of every kChunkTris consecutive triangles of a view.
-void Renderer::build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count) {
+void Renderer::build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count,
+                                 uint32_t box_base) {
   const uint32_t tris = index_count / 3;
   const uint32_t* idx = &host_indices_[size_t(m.index_base) + index_offset];
   for (uint32_t t0 = 0; t0 < tris; t0 += kChunkTris) {
@@ -396,7 +454,7 @@ void Renderer::build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32
         b.hi[c] = std::max(b.hi[c], p[c]);
       }
     }
-    boxes_.push_back(b);
+    boxes_[box_base + t0 / kChunkTris] = b;
   }
 }
 
@@ -476,6 +534,12 @@ gbr_status Renderer::add_node_hierarchy(uint32_t scene, const char* name, const 
   if (found == names_.end())
     return fail(GBR_ERROR_NOT_FOUND,
                 std::string("Renderer::add(): name ") + (name ? name : "") + " not found");
+  for (uint32_t i = found->second.first; i < found->second.second; ++i) {
+    const MeshView& v = views_[i];
+    if (!mesh_live_[v.mesh] || texture_removed(uint32_t(materials_[v.material].texture)))
+      return fail(GBR_ERROR_STATE, std::string("Renderer::add(): ") + name +
+                                       " uses a removed mesh or texture");
+  }
   SceneState& sc = scenes_[scene];
   const uint32_t top = uint32_t(sc.parents.size());
   sc.parents.push_back(-1);
@@ -497,7 +561,7 @@ gbr_status Renderer::add_node_hierarchy(uint32_t scene, const char* name, const 
       ++batch;
     if (batch == sc.batches.size()) sc.batches.push_back(key);
     HostDraw d{batch, nid, top, v.mesh, v.index_offset, v.index_count, v.material, 0u, {},
-               v.box_base, v.chunk_count};
+               v.box_base, v.chunk_count, i};
     std::memcpy(d.bbox, v.bbox, 24);
     sc.draws.push_back(d);
   }
@@ -590,6 +654,97 @@ gbr_status Renderer::stats(uint32_t scene, gbr_scene_stats_info* out) const {
   return GBR_OK;
 }
 
+gbr_status Renderer::set_sources(uint32_t first, uint32_t count, const uint32_t* sources) {
+  if (uint64_t(first) + count > scenes_.size())
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "setSceneSources: scene range out of bounds");
+  if (count && !sources) return fail(GBR_ERROR_INVALID_ARGUMENT, "setSceneSources: null sources");
+  for (uint32_t i = 0; i < count; ++i)
+    if (sources[i] >= scenes_.size())
+      return fail(GBR_ERROR_INVALID_ARGUMENT, "setSceneSources: source " +
+                                                  std::to_string(sources[i]) + " out of range");
+  for (uint32_t i = 0; i < count; ++i)
+    if (scenes_[first + i].source != sources[i]) {
+      scenes_[first + i].source = sources[i];
+      bindings_dirty_ = true;
+    }
+  return GBR_OK;
+}
+
+gbr_status Renderer::set_enabled(uint32_t scene, bool enabled) {
+  if (gbr_status s = check_scene(scene, "setSceneEnabled()")) return s;
+  if (scenes_[scene].enabled != enabled) {
+    scenes_[scene].enabled = enabled;
+    bindings_dirty_ = true;
+  }
+  return GBR_OK;
+}
+
+// ------------------------------------------------------------- removal
+// Device ranges of a removed resource are reused by later adds, so nothing
+// the GPU may still be reading (the last draw) can be released early.
+gbr_status Renderer::quiesce() {
+  if (upload_pending_) {  // upload_done_ follows the whole last step on its stream
+    cudaSetDevice(device_);
+    GBR_CUDA(cudaEventSynchronize(upload_done_), "synchronise before removal");
+    upload_pending_ = false;
+  }
+  return GBR_OK;
+}
+
+gbr_status Renderer::remove_mesh(uint32_t mesh) {
+  if (mesh >= meshes_.size() || !mesh_live_[mesh])
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "removeMesh: no mesh " + std::to_string(mesh));
+  if (gbr_status s = quiesce()) return s;
+  const MeshRec& m = meshes_[mesh];
+  vertex_pool_.release(m.vertex_base, m.vertex_count);
+  index_pool_.release(m.index_base, m.index_count);
+  mesh_live_[mesh] = false;
+  structure_dirty_ = true;  // the next draw checks that no scene uses it
+  return GBR_OK;
+}
+
+gbr_status Renderer::remove_texture(uint32_t texture) {
+  if (texture == 0)
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "removeTexture: texture 0 is reserved");
+  if (texture >= textures_.size() || !texture_live_[texture])
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "removeTexture: no texture " + std::to_string(texture));
+  if (gbr_status s = quiesce()) return s;
+  const TextureRec& t = textures_[texture];
+  texel_pool_.release(t.offset, uint64_t(t.width) * t.height * t.layers);
+  texture_live_[texture] = false;
+  structure_dirty_ = true;
+  return GBR_OK;
+}
+
+gbr_status Renderer::remove_template(const char* name) {
+  auto found = names_.find(name ? name : "");
+  if (found == names_.end())
+    return fail(GBR_ERROR_NOT_FOUND,
+                std::string("removeNodeHierarchyTemplate: name ") + (name ? name : "") + " not found");
+  if (gbr_status s = quiesce()) return s;
+  for (uint32_t i = found->second.first; i < found->second.second; ++i) {
+    MeshView& v = views_[i];
+    box_pool_.release(v.box_base, v.chunk_count);
+    v.live = false;
+  }
+  names_.erase(found);
+  structure_dirty_ = true;
+  return GBR_OK;
+}
+
+gbr_status Renderer::memory_usage(uint64_t* live, uint64_t* reserved) const {
+  // Bytes per element: vertices 16 position + 16 colour + 8 texcoord,
+  // indices and texels 4, chunk boxes 32.
+  constexpr uint64_t kV = 40, kI = 4, kT = 4, kB = sizeof(ChunkBox);
+  if (live)
+    *live = vertex_pool_.live() * kV + index_pool_.live() * kI + texel_pool_.live() * kT +
+            box_pool_.live() * kB;
+  if (reserved)
+    *reserved = vertex_pool_.end * kV + index_pool_.end * kI + texel_pool_.end * kT +
+                box_pool_.end * kB;
+  return GBR_OK;
+}
+
 // -------------------------------------------------------------- drawing
 gbr_status Renderer::upload_tables() {
   if (!tables_dirty_) return GBR_OK;
@@ -647,6 +802,11 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
     uint64_t tris = 0;
     for (uint32_t k : order) {
       const HostDraw& d = sc.draws[k];
+      if (!mesh_live_[d.mesh] || !views_[d.view].live ||
+          texture_removed(uint32_t(materials_[d.material].texture)))
+        return fail(GBR_ERROR_STATE, "draw: scene " + std::to_string(s) +
+                                         " uses a removed mesh, texture or hierarchy template;"
+                                         " clear it first");
       DrawRec dr{};
       dr.node = d.node;
       dr.mesh = d.mesh;
@@ -663,6 +823,8 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
     if (tris >= (1ull << 31))
       return fail(GBR_ERROR_INVALID_ARGUMENT, "draw: 2^31 or more triangles in one scene");
     cost[s] = tris;
+    sc.draw_count = r.draw_count;
+    sc.tris = tris;
   }
   total_nodes_ = nodes;
   total_draws_ = uint32_t(draws.size());
@@ -670,10 +832,9 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
 
   // Work items: each scene's viewport cut into regions.  The per-scene form
   // uses small regions so that one scene spreads over several CTAs; the
-  // batched form uses large ones (fewer redundant triangle setups) ordered
-  // longest-processing-time first for the persistent grid.
+  // batched form uses large ones (fewer redundant triangle setups), ordered
+  // longest-processing-time first for the persistent grid by order_items().
   std::vector<WorkItem> items, batched;
-  std::vector<uint64_t> batched_cost;
   scene_item_base_.assign(S, 0);
   scene_item_count_.assign(S, 0);
   auto tile = [&](uint32_t s, int rwm, int rhm, std::vector<WorkItem>& out) {
@@ -693,21 +854,11 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
     scene_item_base_[s] = uint32_t(items.size());
     tile(s, tuning_.plain_region_width, tuning_.plain_region_height, items);
     scene_item_count_[s] = uint32_t(items.size()) - scene_item_base_[s];
-    const size_t before = batched.size();
     tile(s, tuning_.region_width, tuning_.region_height, batched);
-    const SceneState& sc = scenes_[s];
-    for (size_t k = before; k < batched.size(); ++k)
-      batched_cost.push_back((cost[s] + 1) * uint64_t(batched[k].w) * batched[k].h /
-                             (uint64_t(sc.width) * sc.height) + cost[s] / 4);
   }
   item_count_ = uint32_t(items.size());
   lpt_count_ = uint32_t(batched.size());
-  std::vector<uint32_t> perm(batched.size());
-  std::iota(perm.begin(), perm.end(), 0u);
-  std::stable_sort(perm.begin(), perm.end(),
-                   [&](uint32_t a, uint32_t b) { return batched_cost[a] > batched_cost[b]; });
-  std::vector<WorkItem> lpt(batched.size());
-  for (size_t i = 0; i < perm.size(); ++i) lpt[i] = batched[perm[i]];
+  batched_items_ = std::move(batched);
 
   cudaSetDevice(device_);
   if (gbr_status st = upload_tables()) return st;
@@ -722,8 +873,9 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
       !d_vis_chunks_.reserve(S1 * 4, false) ||
       !d_status_.reserve(4, false) || !d_counter_.reserve(4, false) ||
       !d_items_.reserve(std::max<size_t>(items.size(), 1) * sizeof(WorkItem), false) ||
-      !d_items_lpt_.reserve(std::max<size_t>(lpt.size(), 1) * sizeof(WorkItem), false) ||
-      !h_stage_.reserve(S1 * kCameraBytes + std::max<size_t>(nodes, 1) * 64))
+      !d_items_lpt_.reserve(std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem), false) ||
+      !h_stage_.reserve(S1 * kCameraBytes + std::max<size_t>(nodes, 1) * 64 +
+                        std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem)))
     return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of memory for scene data");
   GBR_CUDA(cudaMemcpy(d_scenes_.ptr, recs.data(), S * sizeof(SceneRec), cudaMemcpyHostToDevice),
            "scene upload");
@@ -736,12 +888,10 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
   if (!items.empty())
     GBR_CUDA(cudaMemcpy(d_items_.ptr, items.data(), items.size() * sizeof(WorkItem),
                         cudaMemcpyHostToDevice), "scene upload");
-  if (!lpt.empty())
-    GBR_CUDA(cudaMemcpy(d_items_lpt_.ptr, lpt.data(), lpt.size() * sizeof(WorkItem),
-                        cudaMemcpyHostToDevice), "scene upload");
   GBR_CUDA(cudaMemset(d_status_.ptr, 0, 4), "scene upload");
   for (auto& sc : scenes_) sc.transforms_dirty = true;
   structure_dirty_ = false;
+  bindings_dirty_ = true;  // item order and visible-record bases follow the new draws
   graph_valid_ = false;
   return GBR_OK;
 }
@@ -780,10 +930,39 @@ gbr_status Renderer::upload_step(cudaStream_t stream) {
     upload_pending_ = false;
   }
   char* stage = static_cast<char*>(h_stage_.ptr);
+  if (bindings_dirty_) {
+    // Visible records: each enabled scene gets room for its source's draws.
+    uint64_t base = 0;
+    for (uint32_t s = 0; s < S; ++s) {
+      SceneState& sc = scenes_[s];
+      sc.vis_base = uint32_t(base);
+      if (sc.enabled) base += scenes_[sc.source].draw_count;
+      if (base > 0xffffffffull) return fail(GBR_ERROR_INVALID_ARGUMENT, "draw: too many draws");
+    }
+    vis_needed_ = base;
+    void* before = d_visible_.ptr;
+    if (!d_visible_.reserve(std::max<uint64_t>(base, 1) * sizeof(VisibleRec), false))
+      return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of device memory for visible draws");
+    if (d_visible_.ptr != before) graph_valid_ = false;
+    order_items();
+    bindings_dirty_ = false;
+  }
   CameraRec* cams = reinterpret_cast<CameraRec*>(stage);
   for (uint32_t s = 0; s < S; ++s) {
-    std::memcpy(cams[s].pv, scenes_[s].pv, 64);
-    for (int k = 0; k < 4; ++k) cams[s].vrow[k] = scenes_[s].view[k * 4 + 2];
+    const SceneState& sc = scenes_[s];
+    std::memcpy(cams[s].pv, sc.pv, 64);
+    for (int k = 0; k < 4; ++k) cams[s].vrow[k] = sc.view[k * 4 + 2];
+    cams[s].source = sc.source;
+    cams[s].vis_base = sc.vis_base;
+    cams[s].enabled = sc.enabled ? 1u : 0u;
+    cams[s].pad = 0;
+  }
+  if (items_staged_) {
+    WorkItem* istage = reinterpret_cast<WorkItem*>(stage + size_t(S) * kCameraBytes +
+                                                   size_t(total_nodes_) * 64);
+    GBR_CUDA(cudaMemcpyAsync(d_items_lpt_.ptr, istage, size_t(lpt_count_) * sizeof(WorkItem),
+                             cudaMemcpyHostToDevice, stream), "work item upload");
+    items_staged_ = false;
   }
   float* tstage = reinterpret_cast<float*>(stage + size_t(S) * kCameraBytes);
   // Coalesce runs of dirty scenes into single copies.
@@ -811,6 +990,34 @@ gbr_status Renderer::upload_step(cudaStream_t stream) {
   return GBR_OK;
 }
 
+// Longest-processing-time order of the batched form's regions for the
+// persistent grid: a region's cost is its share of the source scene's
+// triangles plus a per-region setup term; disabled scenes go last.  Staged
+// for upload_step().
+void Renderer::order_items() {
+  const size_t n = batched_items_.size();
+  std::vector<uint64_t> cost(n);
+  std::vector<uint8_t> on(n);
+  for (size_t k = 0; k < n; ++k) {
+    const WorkItem& it = batched_items_[k];
+    const SceneState& sc = scenes_[it.scene];
+    const uint64_t tris = scenes_[sc.source].tris;
+    on[k] = sc.enabled;
+    cost[k] = (tris + 1) * uint64_t(it.w) * it.h / (uint64_t(sc.width) * sc.height) + tris / 4;
+  }
+  std::vector<uint32_t> perm(n);
+  std::iota(perm.begin(), perm.end(), 0u);
+  std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
+    if (on[a] != on[b]) return on[a] > on[b];
+    return cost[a] > cost[b];
+  });
+  WorkItem* istage = reinterpret_cast<WorkItem*>(static_cast<char*>(h_stage_.ptr) +
+                                                 scenes_.size() * kCameraBytes +
+                                                 size_t(total_nodes_) * 64);
+  for (size_t i = 0; i < n; ++i) istage[i] = batched_items_[perm[i]];
+  items_staged_ = n != 0;
+}
+
 gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   const uint32_t S = uint32_t(scenes_.size());
   PrepareParams pp{};
@@ -827,6 +1034,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   pp.status = d_status_.as<uint32_t>();
   RasterParams rp{};
   rp.scenes = pp.scenes;
+  rp.cameras = pp.cameras;
   rp.visible = pp.visible;
   rp.vis_count = pp.vis_count;
   rp.vis_tris = pp.vis_tris;
@@ -870,6 +1078,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
     rp.persistent = 0;
     rp.region_px = tuning_.plain_region_width * tuning_.plain_region_height;
     for (uint32_t s = 0; s < S; ++s) {
+      if (!scenes_[s].enabled) continue;
       pp.scene_base = s;
       GBR_CUDA(launch_prepare(pp, 1, stream), "prepare launch");
       rp.item_base = scene_item_base_[s];

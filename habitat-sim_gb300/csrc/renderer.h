@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <map>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -33,18 +34,31 @@ struct PinnedBuffer {
   bool reserve(size_t n);
 };
 
+// Offsets into one of the device arrays (vertices, indices, texels, chunk
+// boxes): first-fit reuse of released ranges, else growth at the end.
+struct RangePool {
+  uint64_t end = 0;                   // one past the highest range ever handed out
+  uint64_t free_total = 0;
+  std::map<uint64_t, uint64_t> free;  // offset -> size, coalesced
+  uint64_t alloc(uint64_t n);
+  void release(uint64_t offset, uint64_t n);
+  uint64_t live() const { return end - free_total; }
+};
+
 struct MeshView {
   uint32_t mesh, index_offset, index_count, material;
   float transform[16];
   float bbox[6];
   uint32_t box_base;     // first chunk box of this view
   uint32_t chunk_count;  // 32-triangle chunks of this view
+  bool live;             // false once its template was removed
 };
 
 struct HostDraw {
   uint32_t batch, node, top, mesh, index_offset, index_count, material, semantic;
   float bbox[6];
   uint32_t box_base, chunk_count;
+  uint32_t view;  // index into the renderer's mesh views
 };
 
 struct BatchKey {
@@ -63,6 +77,11 @@ struct SceneState {
   int64_t fb_offset = 0, pitch = 0;
   bool transforms_dirty = true;
   uint32_t node_base = 0;  // in the flattened device arrays
+  uint32_t draw_count = 0; // draws in the flattened device arrays (at the last rebuild)
+  uint64_t tris = 0;       // triangles of those draws
+  uint32_t source = 0;     // scene whose nodes and draws this scene renders
+  uint32_t vis_base = 0;   // first visible record (from the current bindings)
+  bool enabled = true;
 };
 
 class Renderer {
@@ -82,6 +101,10 @@ class Renderer {
   gbr_status add_texture(const gbr_texture_data& t, uint32_t* id);
   gbr_status add_material(const gbr_material_data& m, uint32_t* id);
   gbr_status add_template(const char* name, uint32_t count, const gbr_mesh_view* views);
+  gbr_status remove_mesh(uint32_t mesh);
+  gbr_status remove_texture(uint32_t texture);
+  gbr_status remove_template(const char* name);
+  gbr_status memory_usage(uint64_t* live, uint64_t* reserved) const;
 
   // -- scenes
   bool has_hierarchy(const char* name) const { return names_.count(name) != 0; }
@@ -95,6 +118,8 @@ class Renderer {
   gbr_status unprojection(uint32_t scene, float* out) const;
   gbr_status transformations(uint32_t scene, float** out, uint64_t* count);
   gbr_status stats(uint32_t scene, gbr_scene_stats_info* out) const;
+  gbr_status set_sources(uint32_t first, uint32_t count, const uint32_t* sources);
+  gbr_status set_enabled(uint32_t scene, bool enabled);
 
   // -- drawing
   gbr_status draw(cudaStream_t stream, uint32_t mode, bool use_graph);
@@ -124,9 +149,13 @@ class Renderer {
   gbr_status upload_step(cudaStream_t stream);
   gbr_status enqueue_step(cudaStream_t stream, uint32_t mode);
   gbr_status ensure_raster_config();
-  void build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count);
+  void build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count,
+                         uint32_t box_base);
   void* plane_ptr(uint32_t plane, size_t* elem) const;
   gbr_status sync_and_check();
+  gbr_status quiesce();
+  bool texture_removed(uint32_t t) const { return t < texture_live_.size() && !texture_live_[t]; }
+  void order_items();
 
   gbr_config cfg_{};
   std::vector<int32_t> viewports_;
@@ -137,15 +166,16 @@ class Renderer {
 
   // resources (host mirrors)
   std::vector<MeshRec> meshes_;
+  std::vector<bool> mesh_live_;
   std::vector<float> host_pos_;                    // xyz per vertex, for view bounding boxes
   std::vector<uint32_t> host_indices_;
   std::vector<TextureRec> textures_;
-  uint64_t texel_count_ = 0;
+  std::vector<bool> texture_live_;
   std::vector<MaterialRec> materials_;
   std::vector<MeshView> views_;
   std::vector<ChunkBox> boxes_;
   std::unordered_map<std::string, std::pair<uint32_t, uint32_t>> names_;
-  uint32_t vertex_count_ = 0, index_count_ = 0;
+  RangePool vertex_pool_, index_pool_, texel_pool_, box_pool_;
   bool tables_dirty_ = true;
 
   std::vector<SceneState> scenes_;
@@ -168,6 +198,10 @@ class Renderer {
   uint64_t total_tris_ = 0;
   std::vector<uint32_t> scene_item_base_, scene_item_count_;
   uint32_t item_count_ = 0, lpt_count_ = 0;
+  std::vector<WorkItem> batched_items_;  // regions of the batched form, scene order
+  bool bindings_dirty_ = true;           // sources or enabled flags changed
+  bool items_staged_ = false;            // a new item order waits in the staging buffer
+  uint64_t vis_needed_ = 0;              // visible records the current bindings need
 
   gbr_tuning tuning_{1024, 128, 128, 1, 1, 16, 32};
   size_t smem_bytes_ = 0, smem_plain_ = 0;

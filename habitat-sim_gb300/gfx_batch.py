@@ -350,6 +350,33 @@ class RendererStandalone:
         check(self._lib.gbr_scene_stats(self._h, sceneId, ctypes.byref(s)))
         return SceneStats(s.node_count, s.draw_count, s.draw_batch_count)
 
+    # ------------------------------------------- serving extensions (new)
+    def setSceneSources(self, sources, first=0):
+        """Scene ``first + i`` renders the nodes and draws of scene
+        ``sources[i]`` with its own camera and viewport, from the next draw."""
+        src = np.ascontiguousarray(sources, np.uint32).reshape(-1)
+        check(self._lib.gbr_set_scene_sources(self._h, first, len(src),
+                                              src.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+
+    def setSceneEnabled(self, sceneId, enabled):
+        """A disabled scene is not drawn; its framebuffer rectangle keeps its pixels."""
+        check(self._lib.gbr_set_scene_enabled(self._h, sceneId, 1 if enabled else 0))
+
+    def removeMesh(self, meshId):
+        check(self._lib.gbr_remove_mesh(self._h, meshId))
+
+    def removeTexture(self, textureId):
+        check(self._lib.gbr_remove_texture(self._h, textureId))
+
+    def removeNodeHierarchyTemplate(self, name):
+        check(self._lib.gbr_remove_node_hierarchy_template(self._h, name.encode()))
+
+    def memoryUsage(self):
+        """(live, reserved) device bytes of geometry, textures and chunk boxes."""
+        live, reserved = ctypes.c_uint64(), ctypes.c_uint64()
+        check(self._lib.gbr_memory_usage(self._h, ctypes.byref(live), ctypes.byref(reserved)))
+        return live.value, reserved.value
+
     # -------------------------------------------------------------- draw
     def draw(self, stream=None, mode=None, graph=False):
         """Render every scene into the framebuffer, asynchronously on

@@ -1,0 +1,454 @@
+"""Request serving over the batch renderer: continuous batching, a device
+memory budget with least-recently-used eviction, latency percentiles.
+
+A serving process keeps a catalog of scenes in host memory (as if read from
+disk), a bounded set of them resident on the GPU, and answers requests --
+(scene, 6-DoF camera pose, resolution) -- with RGBA8 colour, linear depth in
+metres and uint32 semantic ids.  Each step packs pending requests into
+render slots: fixed square viewports of each resolution class, laid out at
+the start of one ragged framebuffer.  Every used slot is pointed at its
+request's resident scene (``setSceneSources``), unused slots are disabled,
+all slots are drawn by one batched launch (a CUDA graph), and the used slot
+rectangles are copied to pinned host memory while the host prepares the next
+step.  Scenes are loaded on first use into "content" scenes (1 x 1 viewports
+that are never drawn themselves) and evicted least-recently-used when the
+device budget or the number of content scenes would be exceeded; eviction
+returns their device ranges to the renderer's free lists.
+
+habitat-sim's batch renderer draws a fixed set of environments per call
+(src/esp/gfx_batch/Renderer.cpp:1292-1353) and its callers own the request
+loop (src/esp/sim/BatchReplayRenderer.cpp:117-151); this module is that loop
+for a request-driven caller of the same draw path.
+"""
+import collections
+import dataclasses
+import math
+import time
+
+import numpy as np
+
+from . import procedural
+
+CLASSES = (64, 128, 256)
+CLASS_P = (0.3, 0.5, 0.2)
+ROOM_LO = np.array([-6.0, 0.0, -6.0])
+ROOM_HI = np.array([6.0, 3.0, 6.0])
+
+
+# ------------------------------------------------------------------ catalog
+@dataclasses.dataclass
+class SceneAsset:
+    positions: np.ndarray   # [V, 3] float32
+    colors: np.ndarray      # [V, 4] float32
+    texcoords: np.ndarray   # [V, 2] float32
+    object_ids: np.ndarray  # [V] uint32
+    indices: np.ndarray     # [3T] uint32
+    texture: np.ndarray     # [h, w, 4] uint8
+
+    @property
+    def triangles(self):
+        return len(self.indices) // 3
+
+    def device_bytes(self):
+        """Bytes the renderer keeps on the device for this scene: 40 per
+        vertex (position, colour, texcoord), 4 per index, 4 per texel, 32 per
+        32-triangle chunk box."""
+        chunks = (self.triangles + 31) // 32
+        return len(self.positions) * 40 + len(self.indices) * 4 + self.texture.size + chunks * 32
+
+
+def serving_scene(seed, triangles, texture_size=64):
+    """One catalog scene of about ``triangles`` triangles: a 12 x 3 x 12 m
+    room shell (80 % of the budget) and 20 boxes (20 %), random RGB per
+    vertex, object id 1 for the shell and 2..21 for the boxes, planar
+    texcoords into one noise texture."""
+    rng = np.random.default_rng([seed, 104729])
+    n = max(2, int(round(math.sqrt(0.8 * triangles / 12.0))))
+    m = max(1, int(round(math.sqrt(0.2 * triangles / (20 * 12.0)))))
+    parts = [procedural.box_faces(ROOM_LO, ROOM_HI, n, inward=True)]
+    ids = [np.full(len(parts[0][0]), 1, np.uint32)]
+    for b in range(20):
+        size = rng.uniform(0.3, 1.5, size=3)
+        c = rng.uniform(ROOM_LO[[0, 2]] + 1.0, ROOM_HI[[0, 2]] - 1.0)
+        lo = np.array([c[0] - size[0] / 2, 0.0, c[1] - size[2] / 2])
+        parts.append(procedural.box_faces(lo, lo + size, m, inward=False))
+        ids.append(np.full(len(parts[-1][0]), 2 + b, np.uint32))
+    pos, idx, base = [], [], 0
+    for p, t in parts:
+        pos.append(p)
+        idx.append(t + base)
+        base += len(p)
+    pos = np.concatenate(pos).astype(np.float32)
+    col = np.ones((len(pos), 4), np.float32)
+    col[:, :3] = rng.integers(0, 256, size=(len(pos), 3)).astype(np.float32) / np.float32(255.0)
+    uv = np.stack([pos[:, 0] + pos[:, 1], pos[:, 2] + pos[:, 1]], 1).astype(np.float32) / 2.0
+    tex = rng.integers(0, 256, size=(texture_size, texture_size, 4), dtype=np.uint8)
+    tex[..., 3] = 255
+    return SceneAsset(pos, col, uv, np.concatenate(ids),
+                      np.concatenate(idx).astype(np.uint32).reshape(-1), tex)
+
+
+class SceneCatalog:
+    """``count`` scenes with triangle counts log-uniform in ``tri_range``,
+    generated on first use from (seed, scene) and kept in host memory."""
+
+    def __init__(self, count, seed=0, tri_range=(1e4, 1e6)):
+        rng = np.random.default_rng([seed, 31337])
+        self.seed = seed
+        self.targets = np.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1]), count))
+        self._assets = {}
+
+    def __len__(self):
+        return len(self.targets)
+
+    def asset(self, scene):
+        a = self._assets.get(scene)
+        if a is None:
+            a = self._assets[scene] = serving_scene(self.seed * 100003 + scene,
+                                                    int(self.targets[scene]))
+        return a
+
+
+# ----------------------------------------------------------------- requests
+@dataclasses.dataclass
+class Request:
+    scene: int
+    resolution: int
+    view: np.ndarray          # world -> camera, [col][row] float32
+    hfov: float = 90.0
+    arrival: float = 0.0      # seconds after the start of serving
+    rid: int = -1
+    done: float = math.nan    # seconds after the start of serving
+    color: np.ndarray = None     # [res, res, 4] uint8, row 0 = bottom
+    depth: np.ndarray = None     # [res, res] float32 metres, 0 = nothing drawn
+    semantic: np.ndarray = None  # [res, res] uint32
+
+    @property
+    def latency(self):
+        return self.done - self.arrival
+
+
+def pose_view(x, y, z, yaw, pitch, roll):
+    """World -> camera matrix ([col][row]) of a camera at (x, y, z) rotated
+    by yaw (about +y), then pitch (about +x), then roll (about -z)."""
+    def rot(axis, a):
+        c, s = math.cos(a), math.sin(a)
+        m = np.eye(3)
+        i, j = [(1, 2), (2, 0), (0, 1)][axis]
+        m[i, i] = c
+        m[i, j] = -s
+        m[j, i] = s
+        m[j, j] = c
+        return m
+    cam = np.eye(4)
+    cam[:3, :3] = rot(1, yaw) @ rot(0, pitch) @ rot(2, roll)
+    cam[:3, 3] = [x, y, z]
+    return np.linalg.inv(cam).T.astype(np.float32)
+
+
+def random_requests(catalog, count, rate, seed=0, classes=CLASSES, p=CLASS_P, zipf=None):
+    """Poisson arrivals at ``rate`` per second; scene uniform over the
+    catalog (or Zipf with exponent ``zipf``); resolution from ``classes``
+    with probabilities ``p``; 6-DoF pose inside the room: position uniform
+    (0.5 m from the walls, 0.5-2.5 m high), yaw uniform, pitch U(-30, 30)
+    deg, roll U(-10, 10) deg; hfov 90 deg."""
+    rng = np.random.default_rng([seed, 7])
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count)) if rate else np.zeros(count)
+    if zipf:
+        w = 1.0 / np.arange(1, len(catalog) + 1) ** zipf
+        scenes = rng.choice(len(catalog), size=count, p=w / w.sum())
+    else:
+        scenes = rng.integers(0, len(catalog), count)
+    res = rng.choice(classes, size=count, p=p)
+    out = []
+    for i in range(count):
+        x, z = rng.uniform(ROOM_LO[[0, 2]] + 0.5, ROOM_HI[[0, 2]] - 0.5)
+        y = rng.uniform(0.5, 2.5)
+        view = pose_view(x, y, z, rng.uniform(0, 2 * math.pi), math.radians(rng.uniform(-30, 30)),
+                         math.radians(rng.uniform(-10, 10)))
+        out.append(Request(int(scenes[i]), int(res[i]), view, 90.0, float(arrivals[i]), i))
+    return out
+
+
+# ------------------------------------------------------------ host policies
+class Residency:
+    """Which catalog scenes are resident, in least-recently-used order, under
+    a byte budget and a count limit (pure bookkeeping; no device calls)."""
+
+    def __init__(self, budget_bytes, capacity):
+        self.budget = budget_bytes
+        self.capacity = capacity
+        self.lru = collections.OrderedDict()  # scene -> (slot, bytes)
+        self.free_slots = list(range(capacity - 1, -1, -1))
+        self.bytes = 0
+
+    def touch(self, scene):
+        """The scene's content slot if resident (now most recently used), else None."""
+        e = self.lru.get(scene)
+        if e is None:
+            return None
+        self.lru.move_to_end(scene)
+        return e[0]
+
+    def plan(self, need, pinned):
+        """Scenes to evict, oldest first, so that ``need`` more bytes and one
+        more slot fit; scenes in ``pinned`` stay.  Raises if impossible."""
+        if need > self.budget:
+            raise MemoryError(f"a scene of {need} bytes exceeds the budget of {self.budget}")
+        out, freed, slots = [], 0, len(self.free_slots)
+        for scene, (_, b) in self.lru.items():
+            if self.bytes - freed + need <= self.budget and slots > 0:
+                break
+            if scene in pinned:
+                continue
+            out.append(scene)
+            freed += b
+            slots += 1
+        if self.bytes - freed + need > self.budget or slots == 0:
+            raise MemoryError("budget too small for the scenes one step needs")
+        return out
+
+    def remove(self, scene):
+        slot, b = self.lru.pop(scene)
+        self.bytes -= b
+        self.free_slots.append(slot)
+        return slot
+
+    def add(self, scene, nbytes):
+        slot = self.free_slots.pop()
+        self.lru[scene] = (slot, nbytes)
+        self.bytes += nbytes
+        return slot
+
+
+def take_batch(queues, slots):
+    """Continuous batching: up to ``slots[c]`` oldest requests of each
+    resolution class ``c`` (FIFO per class)."""
+    batch = {}
+    for c, q in queues.items():
+        k = min(len(q), slots.get(c, 0))
+        if k:
+            batch[c] = [q.popleft() for _ in range(k)]
+    return batch
+
+
+def percentiles(latencies_s):
+    lat = np.sort(np.asarray(latencies_s, np.float64)) * 1e3
+    if not len(lat):
+        return dict(p50_ms=None, p99_ms=None, mean_ms=None)
+    return dict(p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)),
+                mean_ms=float(lat.mean()))
+
+
+# ------------------------------------------------------------------ server
+class RenderServer:
+    """Serves requests for the scenes of ``catalog`` on one GPU.
+
+    ``slots`` maps each square resolution to its number of render slots (the
+    largest batch of that class one step takes); ``max_resident`` bounds the
+    resident scenes; ``budget_bytes`` bounds their device bytes (geometry,
+    textures, chunk boxes; default: no limit); ``max_loads_per_step`` bounds
+    the scene loads one step may wait for (requests beyond it wait for a
+    later step, so that requests for resident scenes are not held up)."""
+
+    def __init__(self, pkg, catalog, slots=None, max_resident=64, budget_bytes=None, graph=True,
+                 device=0, max_loads_per_step=8):
+        import torch
+
+        self.torch = torch
+        self.pkg = pkg
+        self.catalog = catalog
+        self.slots = dict(slots or {64: 96, 128: 64, 256: 16})
+        self.graph = graph
+        viewports, self.slot_base, self.class_offset = [], {}, {}
+        px = 0
+        for c in sorted(self.slots):
+            self.slot_base[c] = len(viewports)
+            self.class_offset[c] = px
+            viewports += [(c, c)] * self.slots[c]
+            px += c * c * self.slots[c]
+        self.slot_px = px
+        self.n_slots = len(viewports)
+        self.content_base = len(viewports)
+        viewports += [(1, 1)] * max_resident
+        cfg = pkg.RendererConfiguration().setViewports(viewports).setDrawMode(pkg.DrawMode.Batched)
+        self.r = pkg.RendererStandalone(cfg, pkg.RendererStandaloneConfiguration().setCudaDevice(
+            device).setFlags(pkg.RendererStandaloneFlags.QuietLog))
+        for s in range(len(viewports)):
+            self.r.setSceneEnabled(s, False)
+        self.enabled = np.zeros(self.n_slots, bool)
+        self.sources = np.arange(len(viewports), dtype=np.uint32)
+        self.residency = Residency(budget_bytes if budget_bytes is not None else 1 << 62,
+                                   max_resident)
+        self.handles = {}  # scene -> (mesh, texture, template name)
+        self.loads = self.evictions = 0
+        self.max_loads_per_step = max_loads_per_step
+        self.device = torch.device("cuda", device)
+        self.stream = torch.cuda.Stream(device=self.device)
+        planes = (pkg.Plane.Color, pkg.Plane.LinearDepth, pkg.Plane.Semantic)
+        self.planes = [self.r.deviceTensor(p) for p in planes]
+        self.host = [[torch.empty((self.slot_px,) + tuple(t.shape[1:]), dtype=t.dtype,
+                                  pin_memory=True) for t in self.planes] for _ in range(2)]
+        self._proj = {}
+        self._step = 0
+
+    def close(self):
+        self.torch.cuda.synchronize(self.device)
+        self.planes = None
+        self.r.close()
+
+    # -- residency
+    def _load(self, scene, pinned):
+        a = self.catalog.asset(scene)
+        need = a.device_bytes()
+        for victim in self.residency.plan(need, pinned):
+            self._evict(victim)
+        r = self.r
+        live0 = r.memoryUsage()[0]
+        tex = r.addTexture(a.texture, filter=0)
+        mesh = r.addMesh(a.positions, a.colors, a.texcoords, a.object_ids, a.indices)
+        mat = r.addMaterial((1, 1, 1, 1), tex, 0)
+        name = f"serving/{scene}"
+        r.addNodeHierarchyTemplate(name, [(mesh, 0, len(a.indices), mat, None)])
+        nbytes = r.memoryUsage()[0] - live0
+        slot = self.residency.add(scene, nbytes)
+        r.addNodeHierarchy(self.content_base + slot, name)
+        self.handles[scene] = (mesh, tex, name)
+        self.loads += 1
+        return slot
+
+    def _evict(self, scene):
+        slot = self.residency.remove(scene)
+        mesh, tex, name = self.handles.pop(scene)
+        self.r.clear(self.content_base + slot)
+        self.r.removeNodeHierarchyTemplate(name)
+        self.r.removeMesh(mesh)
+        self.r.removeTexture(tex)
+        self.evictions += 1
+
+    def _projection(self, hfov, c):
+        key = (hfov, c)
+        p = self._proj.get(key)
+        if p is None:
+            p = self._proj[key] = procedural.projection(hfov, c, c)
+        return p
+
+    # -- one step
+    def _admit(self, batch):
+        """Make the batch's scenes resident, oldest request first; a request
+        whose scene cannot be loaded next to the scenes already taken (budget
+        or resident-scene limit), or would exceed this step's loads, is
+        deferred to a later step."""
+        taken, deferred, pinned = {}, [], set()
+        loads = 0
+        for c in sorted(batch):
+            for req in batch[c]:
+                if self.residency.touch(req.scene) is None:
+                    if self.catalog.asset(req.scene).device_bytes() > self.residency.budget:
+                        raise MemoryError(f"scene {req.scene} exceeds the device budget")
+                    if loads >= self.max_loads_per_step:
+                        deferred.append(req)
+                        continue
+                    try:
+                        self._load(req.scene, pinned)
+                    except MemoryError:
+                        deferred.append(req)
+                        continue
+                    loads += 1
+                pinned.add(req.scene)
+                taken.setdefault(c, []).append(req)
+        return taken, deferred
+
+    def launch(self, batch):
+        """Bind, draw and start the copy-back of one step.  Returns a handle
+        for ``finish`` and the requests deferred to a later step."""
+        torch = self.torch
+        batch, deferred = self._admit(batch)
+        want = np.zeros(self.n_slots, bool)
+        for c, reqs in batch.items():
+            base = self.slot_base[c]
+            projs = np.empty((len(reqs), 4, 4), np.float32)
+            views = np.empty((len(reqs), 4, 4), np.float32)
+            for i, req in enumerate(reqs):
+                slot = self.residency.touch(req.scene)
+                self.sources[base + i] = self.content_base + slot
+                want[base + i] = True
+                projs[i] = self._projection(req.hfov, c)
+                views[i] = req.view
+            self.r.updateCameras(projs, views, first=base)
+        for s in np.nonzero(want != self.enabled)[0]:
+            self.r.setSceneEnabled(int(s), bool(want[s]))
+        self.enabled = want
+        self.r.setSceneSources(self.sources[:self.n_slots])
+        self.r.draw(self.stream, graph=self.graph)
+        buf = self.host[self._step % 2]
+        self._step += 1
+        with torch.cuda.stream(self.stream):
+            for c, reqs in batch.items():
+                o, n = self.class_offset[c], len(reqs) * c * c
+                for dst, src in zip(buf, self.planes):
+                    dst[o:o + n].copy_(src[o:o + n], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(self.stream)
+        return (batch, buf, ev), deferred
+
+    def finish(self, handle, clock=None):
+        """Wait for a launched step and hand each request its images."""
+        batch, buf, ev = handle
+        ev.synchronize()
+        now = clock() if clock else math.nan
+        color, depth, sem = (t.numpy() for t in buf)
+        for c, reqs in batch.items():
+            o = self.class_offset[c]
+            for i, req in enumerate(reqs):
+                a, b = o + i * c * c, o + (i + 1) * c * c
+                req.color = color[a:b].reshape(c, c, 4).copy()
+                req.depth = depth[a:b].reshape(c, c).copy()
+                req.semantic = sem[a:b].reshape(c, c).view(np.uint32).copy()
+                req.done = now
+        return batch
+
+    # -- the request loop
+    def serve(self, requests, realtime=True):
+        """Serve ``requests`` (sorted by arrival).  With ``realtime`` a request
+        is admitted once the wall clock passes its arrival time; otherwise
+        all are pending from the start (a closed-loop saturation run).
+        Returns statistics; each request gets its images and ``done``."""
+        queues = {c: collections.deque() for c in self.slots}
+        pending = collections.deque(sorted(requests, key=lambda q: q.arrival))
+        for req in pending:
+            if req.resolution not in self.slots:
+                raise ValueError(f"no render slots for resolution {req.resolution}")
+        t0 = time.perf_counter()
+        clock = lambda: time.perf_counter() - t0
+        if not realtime:
+            for req in pending:
+                req.arrival = 0.0
+        inflight = collections.deque()
+        steps = batched = 0
+        loads0, ev0 = self.loads, self.evictions
+        while pending or inflight or any(queues.values()):
+            now = clock()
+            while pending and pending[0].arrival <= now:
+                req = pending.popleft()
+                queues[req.resolution].append(req)
+            batch = take_batch(queues, self.slots)
+            if batch:
+                handle, deferred = self.launch(batch)
+                for req in reversed(deferred):
+                    queues[req.resolution].appendleft(req)
+                inflight.append(handle)
+                steps += 1
+                batched += sum(len(v) for v in handle[0].values())
+            if inflight and (len(inflight) >= 2 or not batch):
+                self.finish(inflight.popleft(), clock)
+            elif not batch and pending:
+                time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.002)))
+        elapsed = clock()
+        lat = [q.latency for q in requests]
+        stats = dict(requests=len(requests), steps=steps, elapsed_s=elapsed,
+                     requests_per_s=len(requests) / elapsed if elapsed > 0 else None,
+                     mean_batch=batched / steps if steps else 0.0,
+                     loads=self.loads - loads0, evictions=self.evictions - ev0)
+        stats.update(percentiles(lat))
+        return stats

@@ -186,6 +186,28 @@ gbr_status gbr_draw(gbr_renderer* r, void* stream);
  * stream stay the same. */
 gbr_status gbr_draw_mode(gbr_renderer* r, void* stream, uint32_t mode, int32_t use_graph);
 
+/* Serving and batching extensions (no counterpart in the reference).
+ * gbr_set_scene_sources: scene first+i renders the nodes and draws of scene
+ * sources[i] with its own camera and viewport (by default every scene is its
+ * own source).  Cheap: re-binding takes effect at the next draw without
+ * rebuilding the scene records, so a request loop can point render slots at
+ * resident scenes every step. */
+gbr_status gbr_set_scene_sources(gbr_renderer* r, uint32_t first, uint32_t count,
+                                 const uint32_t* sources);
+/* A disabled scene is not drawn (its framebuffer rectangle keeps its
+ * contents); use it for scenes that only hold content for other scenes. */
+gbr_status gbr_set_scene_enabled(gbr_renderer* r, uint32_t scene, int32_t enabled);
+/* Release a mesh, a texture or a hierarchy template: their device ranges go
+ * back to a free list reused by later adds.  A draw that still uses a
+ * removed mesh or texture fails with GBR_ERROR_STATE; clear those scenes
+ * first. */
+gbr_status gbr_remove_mesh(gbr_renderer* r, uint32_t mesh);
+gbr_status gbr_remove_texture(gbr_renderer* r, uint32_t texture);
+gbr_status gbr_remove_node_hierarchy_template(gbr_renderer* r, const char* name);
+/* Device bytes of live geometry, textures and chunk boxes, and the bytes
+ * currently reserved for them (live + free ranges). */
+gbr_status gbr_memory_usage(gbr_renderer* r, uint64_t* live_bytes, uint64_t* reserved_bytes);
+
 /* Renderer::sceneStats (Renderer.cpp:1356-1375). */
 typedef struct gbr_scene_stats_info {
   uint64_t node_count, draw_count, draw_batch_count;
