@@ -60,6 +60,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--envs", type=int, default=1024)
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--serving-scenes", type=int, default=256)
     p.add_argument("--serving-requests", type=int, default=20000)
     return p.parse_args()
@@ -279,11 +280,14 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     steps = args.warmup + args.steps
     poses = [procedural.camera_poses(wl, i) for i in range(steps)]
-    # Launch shape chosen by the autotuner (cached per GPU and workload).
-    from habitat_sim_gb300 import autotune
-    tuned, tune_report = autotune.tune(r, [procedural.camera_poses(wl, 1000 + i) for i in range(3)],
-                                       int(wl.triangles_per_env().sum()),
-                                       cache=os.path.join(ROOT, "gpurun_out", "autotune.json"))
+    # Launch shape chosen by the autotuner (cached per GPU and workload), or
+    # the library's default shape with --no-autotune.
+    tune_report = {"cached": None, "trials": []}
+    if not args.no_autotune:
+        from habitat_sim_gb300 import autotune
+        autotune.tune(r, [procedural.camera_poses(wl, 1000 + i) for i in range(3)],
+                      int(wl.triangles_per_env().sum()),
+                      cache=os.path.join(ROOT, "habitat-sim_gb300", "_build", "autotune.json"))
 
     def batched_step(i, events=None):
         flush.zero_()
@@ -430,8 +434,9 @@ def main():
                        "triangles_per_step_after_draw_culling": tri,
                        "triangles_per_step_before_culling": int(wl.triangles_per_env().sum()),
                        "tuning": r.tuning(),
-                       "autotune": {"cached": tune_report["cached"],
-                                    "candidates": len(tune_report.get("trials", []))}},
+                       "autotune": None if args.no_autotune else {
+                           "cached": tune_report["cached"],
+                           "candidates": len(tune_report.get("trials", []))}},
             "plain": None if not plain_ms else {
                 "value": plain_fps, "unit": "frames/s", "ms_per_step": statistics.mean(plain_ms),
                 "p50_ms": float(np.percentile(plain_ms, 50)),

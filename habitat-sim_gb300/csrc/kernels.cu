@@ -38,8 +38,9 @@ namespace {
 constexpr uint64_t kEmptyKey = ~0ull;
 constexpr uint32_t kBackground = 0xFF1F1F1Fu;
 constexpr int kMaxHierarchyDepth = 64;
-// Chunks tested and compacted per window (must be <= 32 x the smallest CTA).
-constexpr int kChunkWindow = 2048;
+// Capacity of the raster kernel's ring of chunks that passed culling (a
+// power of two >= 31 + the largest CTA).
+constexpr uint32_t kRing = 2048;
 
 __device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
@@ -125,9 +126,15 @@ __device__ __forceinline__ bool inside_frustum(const float* mvp, float x, float 
 }
 
 // ================================================================ prepare
+// Scenes with at most this many visible draws get a nearest-first
+// processing order; larger ones keep the draw order.
+constexpr uint32_t kSortCap = 2048;
+
 template <int T>
 __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
   __shared__ uint32_t s_warp[T / 32], s_total, s_count, s_tris, s_chunks;
+  __shared__ float s_key[kSortCap];
+  __shared__ uint16_t s_idx[kSortCap];
   const uint32_t s = p.scene_base + blockIdx.x;
   const CameraRec& cam = p.cameras[s];
   const uint32_t vis_base = cam.vis_base;
@@ -151,6 +158,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
   for (uint32_t base = 0; base < sc.draw_count; base += T) {
     const uint32_t j = base + threadIdx.x;
     uint32_t vis = 0, tris = 0, chunks = 0;
+    float far = 0.0f;  // distance of the bounding box's farthest corner along the view axis
     VisibleRec rec;
     if (j < sc.draw_count) {
       const DrawRec d = p.draws[sc.draw_base + j];
@@ -203,6 +211,8 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
                       z = d.bbox[(c & 4) ? 5 : 2];
           all_out &= outcode(rec.mvp, x, y, z);
           inside = inside && inside_frustum(rec.mvp, x, y, z);
+          float ze = fma_(rec.zrow[2], z, fma_(rec.zrow[1], y, fma_(rec.zrow[0], x, rec.zrow[3])));
+          far = fmaxf(far, -ze);
         }
         if (all_out == 0 && d.tri_count > 0) {
           const MeshRec m = p.meshes[d.mesh];
@@ -233,6 +243,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
       rec.ordinal = s_tris + to;
       rec.chunk = s_chunks + co;
       p.visible[vis_base + s_count + vo] = rec;
+      if (s_count + vo < kSortCap) s_key[s_count + vo] = far == far ? far : INFINITY;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -246,6 +257,54 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
     p.vis_count[s] = s_count;
     p.vis_tris[s] = s_tris;
     p.vis_chunks[s] = s_chunks;
+  }
+
+  // Processing order: visible draws by the distance of their farthest
+  // corner, nearest first (a draw around the camera, like a room shell,
+  // goes last); ties by draw order.  The raster kernel's results do not
+  // depend on this order, only how much it can cull.
+  if (!p.order) return;
+  const uint32_t n = s_count;
+  uint2* order = p.order + vis_base;
+  const VisibleRec* visible = p.visible + vis_base;  // written above by this CTA: plain loads
+  if (n > kSortCap) {
+    for (uint32_t k = threadIdx.x; k < n; k += T) order[k] = make_uint2(k, visible[k].chunk);
+    return;
+  }
+  uint32_t m = 1;
+  while (m < n) m <<= 1;
+  for (uint32_t i = threadIdx.x; i < m; i += T) {
+    if (i >= n) s_key[i] = INFINITY;
+    s_idx[i] = uint16_t(i);
+  }
+  __syncthreads();
+  for (uint32_t k = 2; k <= m; k <<= 1)
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < m; i += T) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const float ki = s_key[i], kl = s_key[l];
+          const uint16_t ii = s_idx[i], il = s_idx[l];
+          const bool greater = ki > kl || (ki == kl && ii > il);
+          if (greater == ((i & k) == 0)) {
+            s_key[i] = kl;
+            s_key[l] = ki;
+            s_idx[i] = il;
+            s_idx[l] = ii;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  uint32_t running = 0;
+  for (uint32_t base = 0; base < n; base += T) {
+    const uint32_t k = base + threadIdx.x;
+    const uint32_t d = k < n ? s_idx[k] : 0u;
+    const uint32_t cnt = k < n ? visible[d].chunk_count : 0u;
+    const uint32_t off = block_exclusive_scan<T>(cnt, s_warp, &s_total);
+    if (k < n) order[k] = make_uint2(d, running + off);
+    running += s_total;
+    __syncthreads();
   }
 }
 
@@ -261,8 +320,16 @@ struct QEntry {
 // Dynamic shared-memory layout of raster_kernel; every section starts on a
 // 16-byte boundary.
 struct SmemLayout {
-  size_t queue, qoff, prefix, chunks, total;
+  size_t queue, qoff, prefix, chunks, tiles, coarse, total;
 };
+
+// Depth tiles of the occlusion test: kTile x kTile pixels of the region,
+// and coarse tiles of kCoarse x kCoarse tiles.
+constexpr int kTile = 8, kCoarse = 4;
+__host__ __device__ __forceinline__ int tile_capacity(int region_px, int side) {
+  // ceil(w / s) * ceil(h / s) <= w h / s^2 + (w + h) / s + 1 with w, h <= 1024
+  return region_px / (side * side) + 2 * 1024 / side + 1;
+}
 __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 __host__ __device__ __forceinline__ SmemLayout smem_layout(int threads, int region_px,
                                                            int prefix_cap) {
@@ -271,7 +338,9 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int threads, int regi
   l.qoff = align16(l.queue + size_t(threads) * sizeof(QEntry));
   l.prefix = align16(l.qoff + size_t(threads + 1) * 4);
   l.chunks = align16(l.prefix + size_t(prefix_cap + 1) * 4);
-  l.total = align16(l.chunks + size_t(kChunkWindow) * sizeof(uint2));
+  l.tiles = align16(l.chunks + size_t(kRing) * sizeof(uint2));
+  l.coarse = align16(l.tiles + size_t(tile_capacity(region_px, kTile)) * 4);
+  l.total = align16(l.coarse + size_t(tile_capacity(region_px, kTile * kCoarse)) * 4);
   return l;
 }
 
@@ -290,12 +359,23 @@ struct Ctx {
   int rx0, ry0, rw, rh;  // region
   int W, H;              // viewport
   int small_area;
+  float hw, hh;          // half the viewport size
+  float gx, gy;          // guard band in NDC: 32768 / W, 32768 / H
 };
+
+__device__ __forceinline__ void set_viewport(Ctx& c, int W, int H) {
+  c.W = W;
+  c.H = H;
+  c.hw = __fmul_rn(0.5f, float(W));
+  c.hh = __fmul_rn(0.5f, float(H));
+  c.gx = __fdiv_rn(32768.0f, float(W));
+  c.gy = __fdiv_rn(32768.0f, float(H));
+}
 
 // Project, snap, orient and bound one (sub)triangle.  False if it covers
 // no pixel centre of the region.
 __device__ __forceinline__ bool setup_sub(const float4* q, const Ctx& c, Setup& st) {
-  const float hw = __fmul_rn(0.5f, float(c.W)), hh = __fmul_rn(0.5f, float(c.H));
+  const float hw = c.hw, hh = c.hh;
   float zw[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -446,7 +526,7 @@ __device__ __forceinline__ void triangle(const float4* cv, uint32_t ordinal, con
       (cv[0].z > cv[0].w && cv[1].z > cv[1].w && cv[2].z > cv[2].w) ||
       (cv[0].z < -cv[0].w && cv[1].z < -cv[1].w && cv[2].z < -cv[2].w))
     return;
-  const float gx = __fdiv_rn(32768.0f, float(c.W)), gy = __fdiv_rn(32768.0f, float(c.H));
+  const float gx = c.gx, gy = c.gy;
   bool need_clip = false;
 #pragma unroll
   for (int i = 0; i < 3; ++i)
@@ -618,54 +698,96 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
   sid = (flags & kMeshObjectId) ? __float_as_uint(__ldg(&p.pos[v[2]]).w) : __ldg(&rec->semantic_id);
 }
 
-// False when no triangle of the chunk can cover a pixel of the region: its
-// object-space box is beyond one frustum plane, or, with every corner in
-// front of the camera, its projected bounding rectangle (grown by 2 pixels)
-// misses the region.  Conservative: culling never removes a covered pixel.
-__device__ __forceinline__ bool chunk_visible(const float* mvp, const ChunkBox& b, const Ctx& c,
-                                              bool frustum, bool region) {
-  uint32_t all_out = 0x3fu;
-  bool all_front = true;
-  float x0 = 3.0e38f, x1 = -3.0e38f, y0 = 3.0e38f, y1 = -3.0e38f;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const float x = (k & 1) ? b.hi[0] : b.lo[0], y = (k & 2) ? b.hi[1] : b.lo[1],
-                z = (k & 4) ? b.hi[2] : b.lo[2];
-    if (frustum) all_out &= outcode(mvp, x, y, z);
-    if (region) {
-      const float cx = mrow(mvp, 0, x, y, z), cy = mrow(mvp, 1, x, y, z),
-                  cw = mrow(mvp, 3, x, y, z);
-      if (cw > 1e-6f) {
-        const float sx = (cx / cw * 0.5f + 0.5f) * float(c.W);
-        const float sy = (cy / cw * 0.5f + 0.5f) * float(c.H);
-        x0 = fminf(x0, sx);
-        x1 = fmaxf(x1, sx);
-        y0 = fminf(y0, sy);
-        y1 = fmaxf(y1, sy);
-      } else {
-        all_front = false;
-      }
-    }
-  }
-  if (frustum && all_out) return false;
-  if (region && all_front &&
-      (x1 + 2.0f < float(c.rx0) || x0 - 2.0f > float(c.rx0 + c.rw) ||
-       y1 + 2.0f < float(c.ry0) || y0 - 2.0f > float(c.ry0 + c.rh)))
-    return false;
-  return true;
-}
-
-// Largest d in [0, n) with vis[d].chunk <= g.
-__device__ __forceinline__ uint32_t find_chunk_draw(const VisibleRec* vis, uint32_t n, uint32_t g) {
+// Largest k in [0, n) with order[k].y (first chunk in processing order) <= g.
+__device__ __forceinline__ uint32_t find_chunk_draw(const uint2* order, uint32_t n, uint32_t g) {
   uint32_t lo = 0, hi = n;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
-    if (__ldg(&vis[mid].chunk) <= g)
+    if (__ldg(&order[mid].y) <= g)
       lo = mid;
     else
       hi = mid;
   }
   return lo;
+}
+
+// Culling of one 32-triangle chunk by its object-space box, decided by the
+// thread that owns the chunk.  Rejected when
+//  * frustum: all eight corners lie beyond one clip plane (outcode margins);
+//  * region: the box projects (two pixels of margin) outside the region;
+//  * occlusion: every fragment it could produce loses the depth test against
+//    what the z-buffer already holds -- the box lies in front of the camera,
+//    and its nearest window depth, minus a margin far above the rounding of
+//    either computation, is beyond the deepest value of every depth tile its
+//    projection (plus one pixel) touches.  Depths only decrease, so the
+//    chunk stays hidden.
+// Every test is conservative: a rejected chunk has no fragment in the final
+// image.
+__device__ __forceinline__ bool chunk_keep(const float* mvp, const ChunkBox& b, const Ctx& c,
+                                           bool frustum, bool region, const uint32_t* tiles,
+                                           const uint32_t* coarse, int tcols, int ccols) {
+  uint32_t all_out = 0x3fu;
+  bool all_w = true, front = true;
+  float x0 = 3.0e38f, x1 = -3.0e38f, y0 = 3.0e38f, y1 = -3.0e38f, zmin = 3.0e38f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float x = (k & 1) ? b.hi[0] : b.lo[0], y = (k & 2) ? b.hi[1] : b.lo[1],
+                z = (k & 4) ? b.hi[2] : b.lo[2];
+    const float cx = mrow(mvp, 0, x, y, z), cy = mrow(mvp, 1, x, y, z), cz = mrow(mvp, 2, x, y, z),
+                cw = mrow(mvp, 3, x, y, z);
+    const float ax = 1e-5f * (fabsf(cx) + fabsf(cw)), ay = 1e-5f * (fabsf(cy) + fabsf(cw)),
+                az = 1e-5f * (fabsf(cz) + fabsf(cw));
+    uint32_t out = 0;
+    out |= (cx - cw > ax) ? 1u : 0u;
+    out |= (-cx - cw > ax) ? 2u : 0u;
+    out |= (cy - cw > ay) ? 4u : 0u;
+    out |= (-cy - cw > ay) ? 8u : 0u;
+    out |= (cz - cw > az) ? 16u : 0u;
+    out |= (-cz - cw > az) ? 32u : 0u;
+    all_out &= out;
+    if (cw > 1e-6f) {
+      const float iw = 1.0f / cw;
+      const float sx = (cx * iw * 0.5f + 0.5f) * float(c.W);
+      const float sy = (cy * iw * 0.5f + 0.5f) * float(c.H);
+      x0 = fminf(x0, sx);
+      x1 = fmaxf(x1, sx);
+      y0 = fminf(y0, sy);
+      y1 = fmaxf(y1, sy);
+      zmin = fminf(zmin, cz * iw * 0.5f + 0.5f);
+      front = front && cz >= -cw;
+    } else {
+      all_w = false;
+    }
+  }
+  if (frustum && all_out) return false;
+  if (!all_w) return true;
+  if (region && (x1 + 2.0f < float(c.rx0) || x0 - 2.0f > float(c.rx0 + c.rw) ||
+                 y1 + 2.0f < float(c.ry0) || y0 - 2.0f > float(c.ry0 + c.rh)))
+    return false;
+  if (!tiles || !front) return true;
+  zmin -= 4e-6f;
+  if (!(zmin > 0.0f)) return true;
+  // Pixel range of the box in region coordinates, one pixel of margin.
+  const float fx0 = fmaxf(x0 - 1.0f - float(c.rx0), 0.0f), fy0 = fmaxf(y0 - 1.0f - float(c.ry0), 0.0f);
+  const float fx1 = fminf(x1 + 1.0f - float(c.rx0), float(c.rw - 1));
+  const float fy1 = fminf(y1 + 1.0f - float(c.ry0), float(c.rh - 1));
+  if (!(fx0 <= fx1 && fy0 <= fy1)) return false;  // no pixel of the region
+  const uint32_t zbits = __float_as_uint(zmin);
+  int tx0 = int(fx0) / kTile, tx1 = int(fx1) / kTile, ty0 = int(fy0) / kTile, ty1 = int(fy1) / kTile;
+  const uint32_t* t = tiles;
+  int cols = tcols;
+  if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > 16) {  // large footprint: coarse tiles
+    tx0 /= kCoarse;
+    tx1 /= kCoarse;
+    ty0 /= kCoarse;
+    ty1 /= kCoarse;
+    t = coarse;
+    cols = ccols;
+  }
+  for (int ty = ty0; ty <= ty1; ++ty)
+    for (int tx = tx0; tx <= tx1; ++tx)
+      if (t[ty * cols + tx] >= zbits) return true;
+  return false;
 }
 
 template <int T>
@@ -677,7 +799,9 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
   uint32_t* qoff = reinterpret_cast<uint32_t*>(smem + L.qoff);
   uint32_t* prefix = reinterpret_cast<uint32_t*>(smem + L.prefix);
   uint2* chunks = reinterpret_cast<uint2*>(smem + L.chunks);
-  __shared__ uint32_t s_item, s_qcount, s_total;
+  uint32_t* tiles = reinterpret_cast<uint32_t*>(smem + L.tiles);
+  uint32_t* coarse = reinterpret_cast<uint32_t*>(smem + L.coarse);
+  __shared__ uint32_t s_item, s_qcount, s_total, s_rd, s_wr, s_next;
   __shared__ uint32_t s_warp[T / 32];
 
   for (uint32_t iter = 0;; ++iter) {
@@ -700,8 +824,7 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
     c.ry0 = wi.y0;
     c.rw = wi.w;
     c.rh = wi.h;
-    c.W = sc.width;
-    c.H = sc.height;
+    set_viewport(c, sc.width, sc.height);
     c.small_area = p.small_area;
     const int npx = c.rw * c.rh;
     for (int i = threadIdx.x; i < npx; i += T) keys[i] = kEmptyKey;
@@ -714,56 +837,66 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
     if (threadIdx.x == 0) s_qcount = 0;
     __syncthreads();
 
-    // Visible chunks of the scene, a window of kChunkWindow at a time: each
-    // thread tests a run of consecutive chunks, the CTA compacts the
-    // survivors into a shared list of (draw, chunk in draw), then rounds of
-    // T threads set up one triangle each from that list.
+    // Chunks of the visible draws, in processing order (nearest draws
+    // first).  Cull passes: each thread tests one chunk (chunk_keep:
+    // frustum, region, occlusion against the depth tiles) and the survivors
+    // are appended to a ring.  Rounds: each warp takes one chunk of the ring
+    // and its lanes set up one triangle each; triangles covering more than
+    // small_area pixels are queued and rasterised by the whole CTA.  A cull
+    // pass runs whenever fewer chunks than warps wait in the ring, after the
+    // depth tiles are refreshed from the z-buffer.
     const uint32_t nchunks = p.vis_chunks[wi.scene];
+    const uint2* order = p.order + vis_base;
     const bool whole = c.rw == c.W && c.rh == c.H;
+    const bool occlusion = p.occlusion && p.boxes;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tcols = (c.rw + kTile - 1) / kTile, trows = (c.rh + kTile - 1) / kTile;
+    const int ccols = (tcols + kCoarse - 1) / kCoarse, crows = (trows + kCoarse - 1) / kCoarse;
+    if (threadIdx.x == 0) {
+      s_rd = s_wr = s_next = 0;
+    }
     (void)total;
-    for (uint32_t w0 = 0; w0 < nchunks; w0 += kChunkWindow) {
-      const uint32_t wn = min(uint32_t(kChunkWindow), nchunks - w0);
-      const uint32_t per = (wn + T - 1) / T;
-      const uint32_t my0 = w0 + min(wn, threadIdx.x * per), my1 = w0 + min(wn, (threadIdx.x + 1) * per);
-      uint32_t mask = 0, count = 0;  // per <= 32 because kChunkWindow <= 32 * T
-      if (my0 < my1) {
-        uint32_t di = find_chunk_draw(vis, nvis, my0);
-        for (uint32_t gc = my0; gc < my1; ++gc) {
-          while (di + 1 < nvis && __ldg(&vis[di + 1].chunk) <= gc) ++di;
-          const VisibleRec* rec = vis + di;
+    bool tiles_stale = true;  // uniform: the z-buffer changed since the last refresh
+    __syncthreads();
+    for (;;) {
+      const uint32_t rd = s_rd, wr = s_wr, next = s_next;
+      __syncthreads();  // everyone has read the counters
+      if (wr - rd < uint32_t(T / 32) && next < nchunks) {
+        // ---- cull pass
+        if (occlusion && tiles_stale) {
+          // Deepest depth (as ordered bits; empty pixels are all ones) of
+          // each tile; pixels outside the region count as 0.
+          for (int t = warp; t < tcols * trows; t += T / 32) {
+            const int tx = (t % tcols) * kTile + (lane & 7), ty = (t / tcols) * kTile + (lane >> 3);
+            uint32_t m = 0;
+            if (tx < c.rw) {
+              if (ty < c.rh) m = uint32_t(keys[ty * c.rw + tx] >> 32);
+              if (ty + 4 < c.rh) m = max(m, uint32_t(keys[(ty + 4) * c.rw + tx] >> 32));
+            }
+            m = __reduce_max_sync(0xffffffffu, m);
+            if (lane == 0) tiles[t] = m;
+          }
+          __syncthreads();
+          for (int t = threadIdx.x; t < ccols * crows; t += T) {
+            const int cx0 = (t % ccols) * kCoarse, cy0 = (t / ccols) * kCoarse;
+            uint32_t m = 0;
+            for (int y = cy0; y < min(cy0 + kCoarse, trows); ++y)
+              for (int x = cx0; x < min(cx0 + kCoarse, tcols); ++x) m = max(m, tiles[y * tcols + x]);
+            coarse[t] = m;
+          }
+          __syncthreads();
+          tiles_stale = false;
+        }
+        const uint32_t g = next + threadIdx.x;
+        bool keep = false;
+        uint2 od = make_uint2(0u, 0u);
+        if (g < nchunks) {
+          const uint32_t k = find_chunk_draw(order, nvis, g);
+          od = __ldg(&order[k]);
+          const VisibleRec* rec = vis + od.x;
           const bool inside = __ldg(&rec->flags) & kDrawInsideFrustum;
-          bool keep = true;
-          if (p.boxes && !(inside && whole)) {
-            float mvp[16];
-#pragma unroll
-            for (int i = 0; i < 16; ++i) mvp[i] = __ldg(&rec->mvp[i]);
-            keep = chunk_visible(mvp, p.boxes[__ldg(&rec->box_base) + (gc - __ldg(&rec->chunk))], c,
-                                 !inside, !whole);
-          }
-          if (keep) {
-            mask |= 1u << (gc - my0);
-            ++count;
-          }
-        }
-      }
-      uint32_t pos = block_exclusive_scan<T>(count, s_warp, &s_total);
-      const uint32_t nvc = s_total;
-      if (count) {
-        uint32_t di = find_chunk_draw(vis, nvis, my0);
-        for (uint32_t gc = my0; gc < my1; ++gc) {
-          while (di + 1 < nvis && __ldg(&vis[di + 1].chunk) <= gc) ++di;
-          if (mask & (1u << (gc - my0))) chunks[pos++] = make_uint2(di, gc - __ldg(&vis[di].chunk));
-        }
-      }
-      __syncthreads();
-      const uint32_t ntri = nvc * kChunkTris;
-      for (uint32_t base = 0; base < ntri; base += T) {
-        const uint32_t g = base + threadIdx.x;
-        if (g < ntri) {
-          const uint2 ch = chunks[g / kChunkTris];
-          const VisibleRec* rec = vis + ch.x;
-          const uint32_t t = ch.y * kChunkTris + (g % kChunkTris);
-          if (t < __ldg(&rec->tri_count)) {
+          keep = true;
+          if (p.boxes && (occlusion || !(inside && whole))) {
             float mvp[16];
             const float4* m4 = reinterpret_cast<const float4*>(rec->mvp);
 #pragma unroll
@@ -774,52 +907,84 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
               mvp[4 * i + 2] = v.z;
               mvp[4 * i + 3] = v.w;
             }
-            const uint32_t vb = __ldg(&rec->vertex_base);
-            const uint32_t fi = __ldg(&rec->first_index) + 3u * t;
-            float4 cv[3];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-              const float4 q = __ldg(&p.pos[vb + __ldg(&p.indices[fi + k])]);
-              cv[k] = make_float4(mrow(mvp, 0, q.x, q.y, q.z), mrow(mvp, 1, q.x, q.y, q.z),
-                                  mrow(mvp, 2, q.x, q.y, q.z), mrow(mvp, 3, q.x, q.y, q.z));
-            }
-            triangle(cv, __ldg(&rec->ordinal) + t, c);
+            keep = chunk_keep(mvp, p.boxes[__ldg(&rec->box_base) + (g - od.y)], c, !inside, !whole,
+                              occlusion ? tiles : nullptr, coarse, tcols, ccols);
           }
         }
+        const uint32_t pos = block_exclusive_scan<T>(keep ? 1u : 0u, s_warp, &s_total);
+        if (keep) chunks[(wr + pos) & (kRing - 1)] = make_uint2(od.x, g - od.y);
+        if (threadIdx.x == 0) {
+          s_wr = wr + s_total;
+          s_next = next + T;
+        }
         __syncthreads();
-        const uint32_t nq = min(s_qcount, uint32_t(T));
-        __syncthreads();
-        if (nq > 0) {
-          if (threadIdx.x == 0) s_qcount = 0;
-          uint32_t area = 0;
-          if (threadIdx.x < nq) {
-            const QEntry& e = queue[threadIdx.x];
-            area = uint32_t(e.x1 - e.x0 + 1) * uint32_t(e.y1 - e.y0 + 1);
+        continue;
+      }
+      if (wr == rd) break;  // every chunk culled or drawn
+
+      // ---- round: one chunk per warp
+      const uint32_t n = min(wr - rd, uint32_t(T / 32));
+      if (uint32_t(warp) < n) {
+        const uint2 ch = chunks[(rd + warp) & (kRing - 1)];
+        const VisibleRec* rec = vis + ch.x;
+        const uint32_t t = ch.y * kChunkTris + lane;
+        if (t < __ldg(&rec->tri_count)) {
+          float mvp[16];
+          const float4* m4 = reinterpret_cast<const float4*>(rec->mvp);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float4 v = __ldg(m4 + i);
+            mvp[4 * i] = v.x;
+            mvp[4 * i + 1] = v.y;
+            mvp[4 * i + 2] = v.z;
+            mvp[4 * i + 3] = v.w;
           }
-          const uint32_t off = block_exclusive_scan<T>(area, s_warp, &s_total);
-          const uint32_t tot = s_total;
-          if (threadIdx.x < nq) qoff[threadIdx.x] = off;
-          __syncthreads();
-          for (uint32_t q = threadIdx.x; q < tot; q += T) {
-            uint32_t lo = 0, hi = nq;
-            while (hi - lo > 1) {
-              const uint32_t mid = (lo + hi) >> 1;
-              if (qoff[mid] <= q)
-                lo = mid;
-              else
-                hi = mid;
-            }
-            const QEntry& e = queue[lo];
-            const int w = e.x1 - e.x0 + 1;
-            const int local = int(q - qoff[lo]);
-            const int px = e.x0 + local % w, py = e.y0 + local / w;
-            float z;
-            if (cover(e.X, e.Y, e.bias, e.zw0, e.d1, e.d2, e.inva, px, py, z))
-              depth_write(keys, (py - c.ry0) * c.rw + (px - c.rx0), z, e.ordinal);
+          const uint32_t vb = __ldg(&rec->vertex_base);
+          const uint32_t fi = __ldg(&rec->first_index) + 3u * t;
+          float4 cv[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const float4 q = __ldg(&p.pos[vb + __ldg(&p.indices[fi + k])]);
+            cv[k] = make_float4(mrow(mvp, 0, q.x, q.y, q.z), mrow(mvp, 1, q.x, q.y, q.z),
+                                mrow(mvp, 2, q.x, q.y, q.z), mrow(mvp, 3, q.x, q.y, q.z));
           }
-          __syncthreads();
+          triangle(cv, __ldg(&rec->ordinal) + t, c);
         }
       }
+      __syncthreads();
+      const uint32_t nq = min(s_qcount, uint32_t(T));
+      if (threadIdx.x == 0) s_rd = rd + n;
+      __syncthreads();
+      if (nq > 0) {
+        if (threadIdx.x == 0) s_qcount = 0;
+        uint32_t area = 0;
+        if (threadIdx.x < nq) {
+          const QEntry& e = queue[threadIdx.x];
+          area = uint32_t(e.x1 - e.x0 + 1) * uint32_t(e.y1 - e.y0 + 1);
+        }
+        const uint32_t off = block_exclusive_scan<T>(area, s_warp, &s_total);
+        const uint32_t tot = s_total;
+        if (threadIdx.x < nq) qoff[threadIdx.x] = off;
+        __syncthreads();
+        for (uint32_t q = threadIdx.x; q < tot; q += T) {
+          uint32_t lo = 0, hi = nq;
+          while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (qoff[mid] <= q)
+              lo = mid;
+            else
+              hi = mid;
+          }
+          const QEntry& e = queue[lo];
+          const int w = e.x1 - e.x0 + 1;
+          const int local = int(q - qoff[lo]);
+          const int px = e.x0 + local % w, py = e.y0 + local / w;
+          float z;
+          if (cover(e.X, e.Y, e.bias, e.zw0, e.d1, e.d2, e.inva, px, py, z))
+            depth_write(keys, (py - c.ry0) * c.rw + (px - c.rx0), z, e.ordinal);
+        }
+      }
+      tiles_stale = true;
       __syncthreads();
     }
     __syncthreads();
@@ -965,6 +1130,7 @@ constexpr int kNoAllocMaxDevices = 64;
 
 struct NoAllocScratch {
   CameraRec camera;
+  uint2 order;
   SceneRec scene;
   VisibleRec visible;
   MaterialRec material;
@@ -1015,6 +1181,7 @@ __global__ void no_alloc_setup(const NoAllocSetup a, NoAllocScratch* s) {
     cam.vis_base = 0;
     cam.enabled = 1;
     s->camera = cam;
+    s->order = make_uint2(0u, 0u);
     // The mesh sits under an identity root and an identity child, as a
     // hierarchy added without a bake transform: abs = I * I, MVP = PV * abs.
     float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
@@ -1151,6 +1318,7 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
   RasterParams p{};
   p.scenes = &s->scene;
   p.cameras = &s->camera;
+  p.order = &s->order;
   p.visible = &s->visible;
   p.vis_count = &s->vis_count;
   p.vis_tris = &s->vis_tris;

@@ -18,7 +18,9 @@ struct Planes {
 
 // Prepare: per scene, absolute node transforms, per-draw MVP and view-z row,
 // frustum culling of each draw's bounding box, compaction of the visible
-// draws with the running triangle ordinal.  One CTA per scene.
+// draws with the running triangle ordinal, and the order in which the
+// raster kernel walks them (nearest first, so that near geometry hides the
+// chunks behind it early).  One CTA per scene.
 struct PrepareParams {
   const SceneRec* scenes;
   const CameraRec* cameras;
@@ -27,6 +29,7 @@ struct PrepareParams {
   const float* local;
   const MeshRec* meshes;
   VisibleRec* visible;
+  uint2* order;        // per visible draw: (draw, first chunk) in processing order
   uint32_t* vis_count;
   uint32_t* vis_tris;
   uint32_t* vis_chunks;
@@ -42,6 +45,7 @@ struct RasterParams {
   const SceneRec* scenes;
   const CameraRec* cameras;   // binding of each scene (vis_base, enabled)
   const VisibleRec* visible;
+  const uint2* order;         // processing order of the visible draws (see PrepareParams)
   const uint32_t* vis_count;
   const uint32_t* vis_tris;
   const uint32_t* vis_chunks;
@@ -64,6 +68,7 @@ struct RasterParams {
   int32_t region_px;   // capacity of the shared z-buffer, pixels
   int32_t prefix_cap;  // visible draws whose ordinals are cached in shared memory
   int32_t small_area;  // boxes up to this many pixels are rasterised by one lane
+  int32_t occlusion;   // skip chunks hidden behind the depths written so far
 };
 
 cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStream_t stream);

@@ -869,6 +869,7 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
       !d_draws_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(DrawRec), false) ||
       !d_cameras_.reserve(S1 * kCameraBytes, false) ||
       !d_visible_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(VisibleRec), false) ||
+      !d_order_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(uint2), false) ||
       !d_vis_count_.reserve(S1 * 4, false) || !d_vis_tris_.reserve(S1 * 4, false) ||
       !d_vis_chunks_.reserve(S1 * 4, false) ||
       !d_status_.reserve(4, false) || !d_counter_.reserve(4, false) ||
@@ -941,9 +942,11 @@ gbr_status Renderer::upload_step(cudaStream_t stream) {
     }
     vis_needed_ = base;
     void* before = d_visible_.ptr;
-    if (!d_visible_.reserve(std::max<uint64_t>(base, 1) * sizeof(VisibleRec), false))
+    void* before_order = d_order_.ptr;
+    if (!d_visible_.reserve(std::max<uint64_t>(base, 1) * sizeof(VisibleRec), false) ||
+        !d_order_.reserve(std::max<uint64_t>(base, 1) * sizeof(uint2), false))
       return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of device memory for visible draws");
-    if (d_visible_.ptr != before) graph_valid_ = false;
+    if (d_visible_.ptr != before || d_order_.ptr != before_order) graph_valid_ = false;
     order_items();
     bindings_dirty_ = false;
   }
@@ -1028,6 +1031,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   pp.local = d_local_.as<float>();
   pp.meshes = d_meshes_.as<MeshRec>();
   pp.visible = d_visible_.as<VisibleRec>();
+  pp.order = d_order_.as<uint2>();
   pp.vis_count = d_vis_count_.as<uint32_t>();
   pp.vis_tris = d_vis_tris_.as<uint32_t>();
   pp.vis_chunks = d_vis_chunks_.as<uint32_t>();
@@ -1036,6 +1040,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   rp.scenes = pp.scenes;
   rp.cameras = pp.cameras;
   rp.visible = pp.visible;
+  rp.order = pp.order;
   rp.vis_count = pp.vis_count;
   rp.vis_tris = pp.vis_tris;
   rp.vis_chunks = pp.vis_chunks;
@@ -1056,6 +1061,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   rp.out.semantic = (cfg_.planes & GBR_PLANE_SEMANTIC) ? d_planes_[3].as<uint32_t>() : nullptr;
   rp.prefix_cap = prefix_cap_;
   rp.small_area = tuning_.small_area;
+  rp.occlusion = tuning_.occlusion_culling;
   uint64_t launches = 0;
   if (mode == GBR_DRAW_BATCHED) {
     pp.scene_base = 0;
@@ -1294,7 +1300,8 @@ gbr_status Renderer::set_tuning(const gbr_tuning& t) {
       t.region_height < 1 || t.region_width > 1024 || t.region_height > 1024 ||
       t.region_width * t.region_height > 32768 || t.small_area < 1 || t.ctas_per_sm < 1 ||
       t.plain_region_width < 4 || t.plain_region_height < 1 || t.plain_region_width > 1024 ||
-      t.plain_region_height > 1024 || t.plain_region_width * t.plain_region_height > 32768)
+      t.plain_region_height > 1024 || t.plain_region_width * t.plain_region_height > 32768 ||
+      t.occlusion_culling < 0 || t.occlusion_culling > 1)
     return fail(GBR_ERROR_INVALID_ARGUMENT, "setTuning: out of range");
   tuning_ = t;
   raster_configured_ = false;

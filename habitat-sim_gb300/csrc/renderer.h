@@ -185,7 +185,7 @@ class Renderer {
   DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_;
   DeviceBuffer d_meshes_, d_materials_, d_textures_, d_boxes_;
   DeviceBuffer d_scenes_, d_parents_, d_local_, d_draws_, d_cameras_;
-  DeviceBuffer d_visible_, d_vis_count_, d_vis_tris_, d_vis_chunks_, d_status_, d_items_,
+  DeviceBuffer d_visible_, d_order_, d_vis_count_, d_vis_tris_, d_vis_chunks_, d_status_, d_items_,
       d_items_lpt_, d_counter_;
   DeviceBuffer d_planes_[4];
   PinnedBuffer h_stage_;
@@ -203,7 +203,7 @@ class Renderer {
   bool items_staged_ = false;            // a new item order waits in the staging buffer
   uint64_t vis_needed_ = 0;              // visible records the current bindings need
 
-  gbr_tuning tuning_{1024, 128, 128, 1, 1, 16, 32};
+  gbr_tuning tuning_{1024, 128, 128, 1, 1, 16, 32, 1};
   size_t smem_bytes_ = 0, smem_plain_ = 0;
   int prefix_cap_ = 0;
   bool raster_configured_ = false;

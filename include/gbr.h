@@ -260,6 +260,9 @@ typedef struct gbr_tuning {
                              occupancy)                                    */
   int32_t plain_region_width;  /* per-scene form: region size, so that one */
   int32_t plain_region_height; /* scene spreads over several CTAs          */
+  int32_t occlusion_culling;   /* 1: skip 32-triangle chunks hidden behind
+                                  the depths already written (exact: the
+                                  output does not change); 0: off           */
 } gbr_tuning;
 gbr_status gbr_get_tuning(gbr_renderer* r, gbr_tuning* out);
 gbr_status gbr_set_tuning(gbr_renderer* r, const gbr_tuning* tuning);

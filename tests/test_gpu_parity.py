@@ -295,6 +295,15 @@ def test_config1_full_size_properties(pkg, procedural):
     gpu.draw(mode=0)
     assert np.array_equal(col, gpu.colorImage())
     assert np.array_equal(sem, gpu.semanticImage())
+    # Occlusion culling of chunks is exact: switching it off changes no pixel.
+    dep = gpu.depthImage()
+    gpu.setTuning(occlusion_culling=0)
+    gpu.draw(mode=1, graph=True)
+    assert np.array_equal(col, gpu.colorImage())
+    assert np.array_equal(dep.view(np.uint32), gpu.depthImage().view(np.uint32))
+    assert np.array_equal(lin.view(np.uint32), gpu.linearDepthImage().view(np.uint32))
+    assert np.array_equal(sem, gpu.semanticImage())
+    gpu.setTuning(occlusion_culling=1)
     sample = [0, 137, 500, 1023]
     cpu = procedural.build_oracle(OracleRenderer, wl, envs=sample)
     procedural.set_cameras(cpu, wl, poses, sample)
