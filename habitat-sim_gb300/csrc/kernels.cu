@@ -572,12 +572,14 @@ __device__ __forceinline__ float clampc(float f) {
   return f;
 }
 
-__device__ __forceinline__ float chan(uint32_t t, int c) {
-  return __fdiv_rn(float((t >> (8 * c)) & 255u), 255.0f);
+// Channel c of an RGBA8 texel as a float: unorm[v] = v / 255 (correctly
+// rounded), a table in shared memory filled at kernel start.
+__device__ __forceinline__ float chan(uint32_t t, int c, const float* unorm) {
+  return unorm[(t >> (8 * c)) & 255u];
 }
 
 __device__ void sample(const TextureRec& t, const uint32_t* texels, int layer, float s, float u,
-                       float out[4]) {
+                       const float* unorm, float out[4]) {
   const int L = layer < 0 ? 0 : (layer >= t.layers ? t.layers - 1 : layer);
   const float fw = float(t.width), fh = float(t.height);
   const uint32_t* base = texels + t.offset + size_t(L) * t.height * t.width;
@@ -586,7 +588,7 @@ __device__ void sample(const TextureRec& t, const uint32_t* texels, int layer, f
     const int y = wrap(int(floorf(clampc(__fmul_rn(u, fh)))), t.height, t.wrap_t);
     const uint32_t v = __ldg(base + size_t(y) * t.width + x);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) out[c] = chan(v, c);
+    for (int c = 0; c < 4; ++c) out[c] = chan(v, c, unorm);
     return;
   }
   const float fx = clampc(__fsub_rn(__fmul_rn(s, fw), 0.5f));
@@ -601,7 +603,8 @@ __device__ void sample(const TextureRec& t, const uint32_t* texels, int layer, f
   const uint32_t v11 = __ldg(base + size_t(y1) * t.width + x1);
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    const float t00 = chan(v00, c), t10 = chan(v10, c), t01 = chan(v01, c), t11 = chan(v11, c);
+    const float t00 = chan(v00, c, unorm), t10 = chan(v10, c, unorm), t01 = chan(v01, c, unorm),
+                t11 = chan(v11, c, unorm);
     const float lo = fma_(a, __fsub_rn(t10, t00), t00);
     const float hi = fma_(a, __fsub_rn(t11, t01), t01);
     out[c] = fma_(b, __fsub_rn(hi, lo), lo);
@@ -618,7 +621,8 @@ __device__ __forceinline__ uint32_t unorm8(float c) {
 
 // Shade the winning triangle `t` of visible draw `rec` at pixel (px, py).
 __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec, uint32_t t,
-                      int px, int py, uint32_t& color, float& lin, uint32_t& sid) {
+                      int px, int py, const float* unorm, uint32_t& color, float& lin,
+                      uint32_t& sid) {
   float mvp[16], zr[4];
 #pragma unroll
   for (int i = 0; i < 16; ++i) mvp[i] = __ldg(&rec->mvp[i]);
@@ -685,7 +689,7 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
     float tt = mat.m[7];
     tt = fma_(mat.m[1], u, tt);
     tt = fma_(mat.m[4], w, tt);
-    sample(p.textures[tex], p.texels, mat.layer, ts, tt, tc);
+    sample(p.textures[tex], p.texels, mat.layer, ts, tt, unorm, tc);
   }
 #undef GBR_INTERP
   uint32_t packed = 0;
@@ -802,6 +806,8 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
   uint32_t* tiles = reinterpret_cast<uint32_t*>(smem + L.tiles);
   uint32_t* coarse = reinterpret_cast<uint32_t*>(smem + L.coarse);
   __shared__ uint32_t s_item, s_qcount, s_total, s_rd, s_wr, s_next;
+  __shared__ float s_unorm[256];
+  for (int i = threadIdx.x; i < 256; i += T) s_unorm[i] = __fdiv_rn(float(i), 255.0f);
   __shared__ uint32_t s_warp[T / 32];
 
   for (uint32_t iter = 0;; ++iter) {
@@ -842,9 +848,10 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
     // frustum, region, occlusion against the depth tiles) and the survivors
     // are appended to a ring.  Rounds: each warp takes one chunk of the ring
     // and its lanes set up one triangle each; triangles covering more than
-    // small_area pixels are queued and rasterised by the whole CTA.  A cull
-    // pass runs whenever fewer chunks than warps wait in the ring, after the
-    // depth tiles are refreshed from the z-buffer.
+    // small_area pixels are queued.  The queue is rasterised by the whole
+    // CTA (flush) once it is half full, before a cull pass and at the end.
+    // A cull pass runs whenever fewer chunks than warps wait in the ring,
+    // after the depth tiles are refreshed from the z-buffer.
     const uint32_t nchunks = p.vis_chunks[wi.scene];
     const uint2* order = p.order + vis_base;
     const bool whole = c.rw == c.W && c.rh == c.H;
@@ -859,9 +866,61 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
     bool tiles_stale = true;  // uniform: the z-buffer changed since the last refresh
     __syncthreads();
     for (;;) {
-      const uint32_t rd = s_rd, wr = s_wr, next = s_next;
+      const uint32_t rd = s_rd, wr = s_wr, next = s_next, nq = min(s_qcount, uint32_t(T));
       __syncthreads();  // everyone has read the counters
-      if (wr - rd < uint32_t(T / 32) && next < nchunks) {
+      const bool need_cull = wr - rd < uint32_t(T / 32) && next < nchunks;
+      if (nq > 0 && (nq >= uint32_t(T / 2) || need_cull || wr == rd)) {
+        // ---- flush: every thread takes a contiguous run of the queued
+        // triangles' bounding-box pixels.
+        uint32_t area = 0;
+        if (threadIdx.x < nq) {
+          const QEntry& e = queue[threadIdx.x];
+          area = uint32_t(e.x1 - e.x0 + 1) * uint32_t(e.y1 - e.y0 + 1);
+        }
+        const uint32_t off = block_exclusive_scan<T>(area, s_warp, &s_total);
+        const uint32_t tot = s_total;
+        if (threadIdx.x < nq) qoff[threadIdx.x] = off;
+        if (threadIdx.x == 0) qoff[nq] = tot;
+        __syncthreads();
+        const uint32_t per = (tot + T - 1) / T;
+        const uint32_t q0 = min(tot, threadIdx.x * per), q1 = min(tot, q0 + per);
+        if (q0 < q1) {
+          uint32_t lo = 0, hi = nq;  // entry holding pixel q0: qoff[lo] <= q0 < qoff[lo + 1]
+          while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (qoff[mid] <= q0)
+              lo = mid;
+            else
+              hi = mid;
+          }
+          const QEntry* e = &queue[lo];
+          int w = e->x1 - e->x0 + 1;
+          int px = e->x0 + int(q0 - qoff[lo]) % w, py = e->y0 + int(q0 - qoff[lo]) / w;
+          uint32_t end = qoff[lo + 1];
+          for (uint32_t q = q0; q < q1; ++q) {
+            if (q == end) {  // next entry (areas are >= 1, so one step)
+              ++lo;
+              e = &queue[lo];
+              w = e->x1 - e->x0 + 1;
+              px = e->x0;
+              py = e->y0;
+              end = qoff[lo + 1];
+            }
+            float z;
+            if (cover(e->X, e->Y, e->bias, e->zw0, e->d1, e->d2, e->inva, px, py, z))
+              depth_write(keys, (py - c.ry0) * c.rw + (px - c.rx0), z, e->ordinal);
+            if (++px > e->x1) {
+              px = e->x0;
+              ++py;
+            }
+          }
+        }
+        if (threadIdx.x == 0) s_qcount = 0;
+        tiles_stale = true;
+        __syncthreads();
+        continue;
+      }
+      if (need_cull) {
         // ---- cull pass
         if (occlusion && tiles_stale) {
           // Deepest depth (as ordered bits; empty pixels are all ones) of
@@ -951,39 +1010,7 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
           triangle(cv, __ldg(&rec->ordinal) + t, c);
         }
       }
-      __syncthreads();
-      const uint32_t nq = min(s_qcount, uint32_t(T));
       if (threadIdx.x == 0) s_rd = rd + n;
-      __syncthreads();
-      if (nq > 0) {
-        if (threadIdx.x == 0) s_qcount = 0;
-        uint32_t area = 0;
-        if (threadIdx.x < nq) {
-          const QEntry& e = queue[threadIdx.x];
-          area = uint32_t(e.x1 - e.x0 + 1) * uint32_t(e.y1 - e.y0 + 1);
-        }
-        const uint32_t off = block_exclusive_scan<T>(area, s_warp, &s_total);
-        const uint32_t tot = s_total;
-        if (threadIdx.x < nq) qoff[threadIdx.x] = off;
-        __syncthreads();
-        for (uint32_t q = threadIdx.x; q < tot; q += T) {
-          uint32_t lo = 0, hi = nq;
-          while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (qoff[mid] <= q)
-              lo = mid;
-            else
-              hi = mid;
-          }
-          const QEntry& e = queue[lo];
-          const int w = e.x1 - e.x0 + 1;
-          const int local = int(q - qoff[lo]);
-          const int px = e.x0 + local % w, py = e.y0 + local / w;
-          float z;
-          if (cover(e.X, e.Y, e.bias, e.zw0, e.d1, e.d2, e.inva, px, py, z))
-            depth_write(keys, (py - c.ry0) * c.rw + (px - c.rx0), z, e.ordinal);
-        }
-      }
       tiles_stale = true;
       __syncthreads();
     }
@@ -1000,7 +1027,8 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
         const uint32_t ord = uint32_t(key);
         dep = __uint_as_float(uint32_t(key >> 32));
         const uint32_t di = find_draw(prefix, vis, cached, nvis, ord);
-        shade(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, col, lin, sid);
+        shade(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, s_unorm, col, lin,
+              sid);
       }
       if (p.out.color) p.out.color[o] = col;
       if (p.out.depth) p.out.depth[o] = dep;
