@@ -17,9 +17,12 @@ import statistics
 
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "gbr_autotune.json")
 
-BATCHED_SPACE = [dict(threads=t, region_width=rw, region_height=rh, small_area=sa)
-                 for t in (1024, 512) for (rw, rh) in ((128, 128), (128, 64))
-                 for sa in (1, 4)]
+BATCHED_SPACE = ([dict(threads=1024, region_width=rw, region_height=rh, small_area=sa, ctas_per_sm=1)
+                  for (rw, rh) in ((128, 128), (128, 64)) for sa in (1, 4)] +
+                 [dict(threads=512, region_width=128, region_height=64, small_area=sa, ctas_per_sm=2)
+                  for sa in (1, 4)] +
+                 [dict(threads=256, region_width=64, region_height=64, small_area=sa, ctas_per_sm=4)
+                  for sa in (1, 4)])
 PLAIN_SPACE = [dict(plain_region_width=w, plain_region_height=h) for (w, h) in
                ((16, 32), (32, 32), (16, 16))]
 
@@ -103,7 +106,7 @@ def tune(renderer, poses, triangles, cache=DEFAULT_CACHE, draws=2, plain=True, f
         trials.append(dict(cand, raster_ms=_time_batched(renderer, poses, draws)))
     best = min((t for t in trials if "raster_ms" in t), key=lambda t: t["raster_ms"])
     renderer.setTuning(**{k: best[k] for k in ("threads", "region_width", "region_height",
-                                                 "small_area")})
+                                                 "small_area", "ctas_per_sm")})
     plain_trials = []
     if plain:
         for cand in PLAIN_SPACE:

@@ -38,9 +38,12 @@ namespace {
 constexpr uint64_t kEmptyKey = ~0ull;
 constexpr uint32_t kBackground = 0xFF1F1F1Fu;
 constexpr int kMaxHierarchyDepth = 64;
-// Capacity of the raster kernel's ring of chunks that passed culling (a
-// power of two >= 31 + the largest CTA).
-constexpr uint32_t kRing = 2048;
+// Capacity of the raster kernel's ring of chunks that passed culling: a
+// power of two >= 31 + the CTA size (a cull pass starts with fewer than 32
+// chunks waiting and adds at most one per thread).
+__host__ __device__ constexpr uint32_t ring_capacity(int threads) {
+  return threads > 512 ? 2048u : (threads > 256 ? 1024u : 512u);
+}
 
 __device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
@@ -338,7 +341,7 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int threads, int regi
   l.qoff = align16(l.queue + size_t(threads) * sizeof(QEntry));
   l.prefix = align16(l.qoff + size_t(threads + 1) * 4);
   l.chunks = align16(l.prefix + size_t(prefix_cap + 1) * 4);
-  l.tiles = align16(l.chunks + size_t(kRing) * sizeof(uint2));
+  l.tiles = align16(l.chunks + size_t(ring_capacity(threads)) * sizeof(uint2));
   l.coarse = align16(l.tiles + size_t(tile_capacity(region_px, kTile)) * 4);
   l.total = align16(l.coarse + size_t(tile_capacity(region_px, kTile * kCoarse)) * 4);
   return l;
@@ -795,7 +798,7 @@ __device__ __forceinline__ bool chunk_keep(const float* mvp, const ChunkBox& b, 
 }
 
 template <int T>
-__global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
+__global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SmemLayout L = smem_layout(T, p.region_px, p.prefix_cap);
   uint64_t* keys = reinterpret_cast<uint64_t*>(smem);
@@ -971,7 +974,7 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
           }
         }
         const uint32_t pos = block_exclusive_scan<T>(keep ? 1u : 0u, s_warp, &s_total);
-        if (keep) chunks[(wr + pos) & (kRing - 1)] = make_uint2(od.x, g - od.y);
+        if (keep) chunks[(wr + pos) & (ring_capacity(T) - 1)] = make_uint2(od.x, g - od.y);
         if (threadIdx.x == 0) {
           s_wr = wr + s_total;
           s_next = next + T;
@@ -984,7 +987,7 @@ __global__ void __launch_bounds__(T) raster_kernel(const RasterParams p) {
       // ---- round: one chunk per warp
       const uint32_t n = min(wr - rd, uint32_t(T / 32));
       if (uint32_t(warp) < n) {
-        const uint2 ch = chunks[(rd + warp) & (kRing - 1)];
+        const uint2 ch = chunks[(rd + warp) & (ring_capacity(T) - 1)];
         const VisibleRec* rec = vis + ch.x;
         const uint32_t t = ch.y * kChunkTris + lane;
         if (t < __ldg(&rec->tri_count)) {
@@ -1070,7 +1073,7 @@ size_t raster_smem_bytes(int threads, int region_px, int prefix_cap) {
     default: return cudaErrorInvalidValue; \
   }
 
-cudaError_t raster_configure(int threads, size_t* max_dynamic) {
+cudaError_t raster_configure(int threads, size_t* max_dynamic, size_t* static_bytes) {
   int optin = 0, dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -1086,6 +1089,7 @@ cudaError_t raster_configure(int threads, size_t* max_dynamic) {
                              int(dyn));                                                        \
     if (e != cudaSuccess) return e;                                                            \
     *max_dynamic = dyn;                                                                        \
+    *static_bytes = fa.sharedSizeBytes;                                                        \
   }
   GBR_RASTER_SWITCH(threads, GBR_CFG)
 #undef GBR_CFG
@@ -1335,8 +1339,8 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
   if (e != cudaSuccess)
     return no_alloc_fail(GBR_ERROR_CUDA, std::string("setup: ") + cudaGetErrorString(e));
   constexpr int kThreads = 1024;
-  size_t max_dyn = 0;
-  e = raster_configure(kThreads, &max_dyn);
+  size_t max_dyn = 0, static_bytes = 0;
+  e = raster_configure(kThreads, &max_dyn, &static_bytes);
   const size_t smem = raster_smem_bytes(kThreads, kNoAllocRegion * kNoAllocRegion, 1);
   int occ = 0, sms = 0;
   if (e == cudaSuccess) e = raster_max_ctas_per_sm(kThreads, smem, &occ);

@@ -74,8 +74,8 @@ struct RasterParams {
 cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStream_t stream);
 size_t raster_smem_bytes(int threads, int region_px, int prefix_cap);
 // Raises the kernel's dynamic shared-memory limit to the device maximum and
-// returns that maximum.
-cudaError_t raster_configure(int threads, size_t* max_dynamic);
+// returns that maximum and the kernel's static shared memory.
+cudaError_t raster_configure(int threads, size_t* max_dynamic, size_t* static_bytes);
 cudaError_t launch_raster(const RasterParams& p, int threads, uint32_t grid, size_t smem,
                           cudaStream_t stream);
 cudaError_t raster_max_ctas_per_sm(int threads, size_t smem, int* out);

@@ -901,11 +901,23 @@ gbr_status Renderer::ensure_raster_config() {
   if (raster_configured_) return GBR_OK;
   const int region_px = tuning_.region_width * tuning_.region_height;
   const int plain_px = tuning_.plain_region_width * tuning_.plain_region_height;
-  size_t max_dyn = 0;
-  GBR_CUDA(raster_configure(tuning_.threads, &max_dyn), "raster configure");
+  size_t max_dyn = 0, static_smem = 0;
+  GBR_CUDA(raster_configure(tuning_.threads, &max_dyn, &static_smem), "raster configure");
+  // Room for the requested CTAs per SM: the SM's shared memory less the
+  // per-CTA reservation and static part, shared by ctas_per_sm CTAs.
+  int per_sm = 0, reserved = 0;
+  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device_);
+  cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, device_);
+  const int want = std::max(1, tuning_.ctas_per_sm);
+  size_t budget = max_dyn;
+  if (want > 1 && per_sm > 0) {
+    const size_t share = size_t(per_sm) / size_t(want);
+    const size_t fixed = size_t(reserved) + static_smem;
+    budget = std::min(budget, share > fixed ? share - fixed : size_t(0));
+  }
   int cap = kPrefixCapMax;
   size_t smem = raster_smem_bytes(tuning_.threads, std::max(region_px, plain_px), cap);
-  while (smem > max_dyn && cap > 64) {
+  while (smem > budget && cap > 64) {
     cap /= 2;
     smem = raster_smem_bytes(tuning_.threads, std::max(region_px, plain_px), cap);
   }
