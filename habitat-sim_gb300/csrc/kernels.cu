@@ -400,9 +400,9 @@ __device__ __forceinline__ bool setup_sub(const float4* q, const Ctx& c, Setup& 
     const int dx = st.X[b] - st.X[a], dy = st.Y[b] - st.Y[a];
     if (dy < 0 || (dy == 0 && dx < 0)) bias |= 1u << i;
   }
-  st.bias = bias;
   const int minX = min(st.X[0], min(st.X[1], st.X[2])), maxX = max(st.X[0], max(st.X[1], st.X[2]));
   const int minY = min(st.Y[0], min(st.Y[1], st.Y[2])), maxY = max(st.Y[0], max(st.Y[1], st.Y[2]));
+  st.bias = bias;
   st.x0 = max((minX - 128 + 255) >> 8, c.rx0);
   st.x1 = min((maxX - 128) >> 8, c.rx0 + c.rw - 1);
   st.y0 = max((minY - 128 + 255) >> 8, c.ry0);
@@ -626,14 +626,28 @@ __device__ __forceinline__ uint32_t unorm8(float c) {
 __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec, uint32_t t,
                       int px, int py, const float* unorm, uint32_t& color, float& lin,
                       uint32_t& sid) {
+  // The record in 16-byte loads: mvp, zrow, (vertex_base, first_index,
+  // tri_count, material), (semantic_id, ordinal, flags, chunk).
+  const float4* r4 = reinterpret_cast<const float4*>(rec);
   float mvp[16], zr[4];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) mvp[i] = __ldg(&rec->mvp[i]);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) zr[i] = __ldg(&rec->zrow[i]);
-  const uint32_t flags = __ldg(&rec->flags);
-  const uint32_t vb = __ldg(&rec->vertex_base);
-  const uint32_t fi = __ldg(&rec->first_index) + 3u * t;
+  for (int i = 0; i < 4; ++i) {
+    const float4 v = __ldg(r4 + i);
+    mvp[4 * i] = v.x;
+    mvp[4 * i + 1] = v.y;
+    mvp[4 * i + 2] = v.z;
+    mvp[4 * i + 3] = v.w;
+  }
+  const float4 z4 = __ldg(r4 + 4);
+  zr[0] = z4.x;
+  zr[1] = z4.y;
+  zr[2] = z4.z;
+  zr[3] = z4.w;
+  const uint4 u5 = __ldg(reinterpret_cast<const uint4*>(rec) + 5);
+  const uint4 u6 = __ldg(reinterpret_cast<const uint4*>(rec) + 6);
+  const uint32_t flags = u6.z;
+  const uint32_t vb = u5.x;
+  const uint32_t fi = u5.y + 3u * t;
   uint32_t v[3];
   float4 c[3];
   float d[3];
@@ -675,7 +689,7 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
     vc[2] = GBR_INTERP(c0.z, c1.z, c2.z);
     vc[3] = GBR_INTERP(c0.w, c1.w, c2.w);
   }
-  const uint32_t mi = __ldg(&rec->material);
+  const uint32_t mi = u5.w;
   const MaterialRec& mat = p.materials[mi];
   float tc[4] = {1.0f, 1.0f, 1.0f, 1.0f};
   const int tex = mat.texture;
@@ -702,7 +716,7 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
     packed |= unorm8(val) << (8 * k);
   }
   color = packed;
-  sid = (flags & kMeshObjectId) ? __float_as_uint(__ldg(&p.pos[v[2]]).w) : __ldg(&rec->semantic_id);
+  sid = (flags & kMeshObjectId) ? __float_as_uint(__ldg(&p.pos[v[2]]).w) : u6.x;
 }
 
 // Largest k in [0, n) with order[k].y (first chunk in processing order) <= g.

@@ -8,13 +8,15 @@
 //   textures   texel[t]  uint32 RGBA8, layer-major, row 0 bottom
 //   tables     MeshRec, MaterialRec, TextureRec
 //   scenes     SceneRec[s]; per node parent (int32) + local 4x4 (64 B);
-//              DrawRec[] (64 B) in draw-batch order; CameraRec[s] (80 B)
-//   per step   VisibleRec[] (128 B, written by the prepare kernel),
+//              DrawRec[] (64 B) in draw-batch order; CameraRec[s] (96 B)
+//   per step   VisibleRec[] (128 B, written by the prepare kernel) and its
+//              processing order uint2[] (8 B per visible draw),
 //              vis_count[s], vis_tris[s], vis_chunks[s]; WorkItem[] + one counter
 //   views      ChunkBox[] (32 B per 32 triangles of every mesh view)
 //   output     colour u32, window depth f32, linear depth f32, id u32
 //              planes, one element per framebuffer pixel.
 #pragma once
+#include <cstddef>
 #include <cstdint>
 
 namespace gbr {
@@ -98,6 +100,10 @@ struct alignas(16) VisibleRec {
   uint32_t pad[2];
 };
 static_assert(sizeof(VisibleRec) == 128, "VisibleRec layout");
+// The raster kernel loads the record as 16-byte vectors by these offsets.
+static_assert(offsetof(VisibleRec, zrow) == 64 && offsetof(VisibleRec, vertex_base) == 80 &&
+                  offsetof(VisibleRec, semantic_id) == 96 && offsetof(VisibleRec, flags) == 104,
+              "VisibleRec vector layout");
 
 // Triangles per chunk: the unit of work a warp takes and of bounding-box culling.
 constexpr uint32_t kChunkTris = 32;
