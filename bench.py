@@ -285,9 +285,10 @@ def main():
     tune_report = {"cached": None, "trials": []}
     if not args.no_autotune:
         from habitat_sim_gb300 import autotune
-        autotune.tune(r, [procedural.camera_poses(wl, 1000 + i) for i in range(3)],
-                      int(wl.triangles_per_env().sum()),
-                      cache=os.path.join(ROOT, "habitat-sim_gb300", "_build", "autotune.json"))
+        _, tune_report = autotune.tune(
+            r, [procedural.camera_poses(wl, 1000 + i) for i in range(3)],
+            int(wl.triangles_per_env().sum()),
+            cache=os.path.join(ROOT, "habitat-sim_gb300", "_build", "autotune.json"))
 
     def batched_step(i, events=None):
         flush.zero_()
