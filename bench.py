@@ -58,7 +58,9 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--envs", type=int, default=1024)
+    p.add_argument("--envs", type=int, default=None)
+    p.add_argument("--workload", default="config1", choices=["config1", "config2", "config3"],
+                   help="config1 (the metric's workload) by default; config2/config3 for reference")
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--serving-scenes", type=int, default=256)
@@ -126,11 +128,22 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- workload
-def load_workload(envs):
+WORKLOADS = {
+    "config1": WORKLOAD,
+    "config2": ("config2 uneven batching: 4096 envs over 64 procedural scenes of 20k-2M triangles "
+                "(log-uniform), per-env resolution 64/128/256 px (p 0.3/0.5/0.2), hfov U(60,110)"),
+    "config3": ("config3 large scans: 256 envs over 8 scan-like rooms of 5.0M triangles each "
+                "(noisy 1.31 cm tessellation, value-noise colour, 64 Voronoi ids), 256x256, "
+                "random-walk cameras"),
+}
+
+
+def load_workload(name, envs=None):
     import __graft_entry__ as graft
     pkg = graft.build()
     from habitat_sim_gb300 import procedural
-    wl = procedural.config1(envs=envs)
+    kw = {} if envs is None else {"envs": envs}
+    wl = getattr(procedural, name)(**kw)
     return pkg, procedural, wl
 
 
@@ -226,7 +239,7 @@ def run_reference_impl(args):
     oracle_build.build()
     from habitat_sim_gb300 import procedural
     from oracle.model import OracleRenderer
-    wl = procedural.config1(envs=args.envs)
+    wl = getattr(procedural, args.workload)(**({} if args.envs is None else {"envs": args.envs}))
     threads = os.cpu_count() or 1
     # Size one step so that warmup + steps end within a few minutes.
     fps, n, dt = cpu_frames_per_s(procedural, wl, min(args.cpu_seconds, 8.0), threads)
@@ -248,7 +261,7 @@ def run_reference_impl(args):
         "ms_per_step": statistics.mean(ms), "p50_ms": float(np.percentile(ms, 50)),
         "p99_ms": float(np.percentile(ms, 99)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "envs_per_step": per_step_envs,
+        "config": {"workload": WORKLOADS[args.workload], "envs_per_step": per_step_envs,
                    "sample": f"first {per_step_envs} of {wl.envs} envs per step"},
         "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
                          "sample": f"{per_step_envs} envs per step, {args.steps} steps"},
@@ -272,7 +285,7 @@ def main():
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    pkg, procedural, wl = load_workload(args.envs)
+    pkg, procedural, wl = load_workload(args.workload, args.envs)
     planes = pkg.Plane.Color | pkg.Plane.LinearDepth | pkg.Plane.Semantic
     r = procedural.build_renderer(pkg, wl, mode=pkg.DrawMode.Batched, planes=planes)
     r.setKernelTiming(True)
@@ -378,10 +391,15 @@ def main():
         mism, max_err, px = 0, 0.0, 0
         for slot, e in enumerate(sample):
             off, pitch, w, h = r.sceneViewport(e)
-            y0, x0 = off // pitch, off % pitch
-            g_col = host_color[y0:y0 + h, x0:x0 + w]
-            g_lin = host_lin[y0:y0 + h, x0:x0 + w]
-            g_sem = host_sem[y0:y0 + h, x0:x0 + w]
+            if wl.uniform:
+                y0, x0 = off // pitch, off % pitch
+                g_col = host_color[y0:y0 + h, x0:x0 + w]
+                g_lin = host_lin[y0:y0 + h, x0:x0 + w]
+                g_sem = host_sem[y0:y0 + h, x0:x0 + w]
+            else:   # ragged: one row, scene after scene
+                g_col = host_color[0, off:off + w * h].reshape(h, w, 4)
+                g_lin = host_lin[0, off:off + w * h].reshape(h, w)
+                g_sem = host_sem[0, off:off + w * h].reshape(h, w)
             c_col = cpu.scene_image(cpu.color, slot).view(np.uint8).reshape(h, w, 4)
             c_lin = cpu.scene_image(cpu.linear_depth, slot)
             c_sem = cpu.scene_image(cpu.semantic, slot)
@@ -405,7 +423,7 @@ def main():
         peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "raster_kernel_config1.txt")
+    tpath = os.path.join(ROOT, "profiles", f"raster_kernel_{args.workload}.txt")
     if os.path.exists(tpath):
         for line in open(tpath):
             if line.startswith("dram_bytes_per_launch:"):
@@ -428,7 +446,8 @@ def main():
             "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "envs": wl.envs, "resolution": 128,
+            "config": {"workload": WORKLOADS[args.workload], "envs": wl.envs,
+                       "resolution": sorted({w for (w, _) in wl.viewports}),
                        "planes": "rgba8 + f32 linear depth + u32 semantic id",
                        "form": "batched: prepare + persistent raster per step, CUDA graph",
                        "l2": "flushed with a 256 MiB write before every step (outside timing)",

@@ -1180,7 +1180,6 @@ void* Renderer::plane_ptr(uint32_t plane, size_t* elem) const {
 }
 
 gbr_status Renderer::image_into(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes) {
-  if (ragged_) return fail(GBR_ERROR_STATE, "imageInto: the ragged layout has no tile grid; use sceneImageInto");
   size_t elem;
   const char* src = static_cast<const char*>(plane_ptr(plane, &elem));
   if (!src) return fail(GBR_ERROR_INVALID_ARGUMENT, "imageInto: plane not enabled");

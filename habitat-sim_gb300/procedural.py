@@ -23,6 +23,14 @@ Workloads (sizes as named by the benchmark configurations):
     in 20k-2M (shell subdivision and instance count raised together),
     resolution drawn from {64, 128, 256}^2 with p = {0.3, 0.5, 0.2}, hfov
     U(60, 110) deg.
+  * ``config3``  256 envs over 8 scan-like scenes: a 12 x 12 x 3 m room
+    (floor, walls, ceiling) tessellated into a quad grid, about 5M
+    triangles per scene (1.31 cm edges; 1 cm edges would give 8.6M),
+    vertex positions perturbed by Gaussian noise with sigma 1 cm, per-vertex
+    RGB from a smooth value-noise field (trilinear over a 0.5 m lattice),
+    per-vertex semantic ids from 64 Voronoi regions; triangles emitted in
+    16 x 16-quad tiles; 256 x 256 cameras at 1.25 m doing a random walk of
+    0.25 m and 10 deg per step.
 """
 import dataclasses
 import math
@@ -48,6 +56,8 @@ class Workload:
     instances: list = dataclasses.field(default_factory=list)  # per scene [(tmpl, bake, id)]
     seed: int = 0
     uniform: bool = True       # all envs share one resolution -> tile grid layout
+    room: tuple = ROOM         # extent (x, y, z) of the room the cameras move in
+    walk: bool = False         # cameras random-walk from step to step (else fresh poses)
 
     def triangles_per_env(self):
         tri = {name: sum(c // 3 for (_, _, c, _) in views) for name, views in self.templates}
@@ -272,6 +282,84 @@ def _add_textured_scene(wl, rng, s, lo, hi, shell_subdiv, instances, prototypes,
     wl.instances.append(inst)
 
 
+def _tiled_grid(origin, a, b, nu, nv, tile=16):
+    """nu x nv quads of the parallelogram origin + s*a + t*b, counter-clockwise
+    seen from the side a x b points to; triangles emitted tile x tile quads
+    at a time so that consecutive triangles lie close together."""
+    s = np.linspace(0.0, 1.0, nu + 1)
+    t = np.linspace(0.0, 1.0, nv + 1)
+    ss, tt = np.meshgrid(s, t, indexing="xy")
+    pos = (np.asarray(origin)[None, None, :] + ss[..., None] * np.asarray(a)[None, None, :] +
+           tt[..., None] * np.asarray(b)[None, None, :]).reshape(-1, 3)
+    idx = np.arange((nu + 1) * (nv + 1)).reshape(nv + 1, nu + 1)
+    qi, qj = np.meshgrid(np.arange(nu), np.arange(nv), indexing="xy")
+    tiles_u = (nu + tile - 1) // tile
+    key = (((qj // tile) * tiles_u + qi // tile) * tile + qj % tile) * tile + qi % tile
+    order = np.argsort(key.reshape(-1), kind="stable")
+    qi, qj = qi.reshape(-1)[order], qj.reshape(-1)[order]
+    v00, v10, v11, v01 = idx[qj, qi], idx[qj, qi + 1], idx[qj + 1, qi + 1], idx[qj + 1, qi]
+    tris = np.stack([np.stack([v00, v10, v11], 1), np.stack([v00, v11, v01], 1)], 1).reshape(-1, 3)
+    return pos, tris
+
+
+def _value_noise(rng, pts, lo, hi, spacing):
+    """Smooth RGB field: trilinear interpolation of uniform random values on a
+    lattice with the given spacing covering [lo, hi]."""
+    n = np.ceil((np.asarray(hi) - np.asarray(lo)) / spacing).astype(int) + 2
+    lattice = rng.uniform(0.0, 1.0, size=(n[0], n[1], n[2], 3))
+    f = (pts - np.asarray(lo)) / spacing
+    i = np.clip(np.floor(f).astype(int), 0, n - 2)
+    w = np.clip(f - i, 0.0, 1.0)
+    out = np.zeros((len(pts), 3))
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                wt = ((w[:, 0] if dx else 1 - w[:, 0]) * (w[:, 1] if dy else 1 - w[:, 1]) *
+                      (w[:, 2] if dz else 1 - w[:, 2]))
+                out += wt[:, None] * lattice[i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz]
+    return out
+
+
+def scan_scene(rng, lo, hi, edge, noise=0.01, regions=64):
+    """One scan-like room mesh (see config3)."""
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    d = hi - lo
+    X, Y, Z = np.array([d[0], 0, 0]), np.array([0, d[1], 0]), np.array([0, 0, d[2]])
+    faces = [(lo, Z, X), (lo + Y, X, Z), (lo, Y, Z), (lo + X, Z, Y), (lo, X, Y), (lo + Z, Y, X)]
+    pos_all, tri_all, base = [], [], 0
+    for (o, a, b) in faces:
+        nu = max(1, int(round(np.linalg.norm(a) / edge)))
+        nv = max(1, int(round(np.linalg.norm(b) / edge)))
+        p, t = _tiled_grid(o, a, b, nu, nv)
+        pos_all.append(p)
+        tri_all.append(t + base)
+        base += len(p)
+    pos = np.concatenate(pos_all)
+    pos += rng.normal(0.0, noise, size=pos.shape)
+    col = np.ones((len(pos), 4), np.float32)
+    rgb = _value_noise(rng, pos, lo - 0.5, hi + 0.5, 0.5)
+    col[:, :3] = np.round(np.clip(rgb, 0, 1) * 255.0).astype(np.float32) / np.float32(255.0)
+    seeds = rng.uniform(lo, hi, size=(regions, 3))
+    from scipy.spatial import cKDTree
+    ids = (1 + cKDTree(seeds).query(pos)[1]).astype(np.uint32)
+    return _mesh(pos, np.concatenate(tri_all), col, None, ids)
+
+
+def config3(seed=3, envs=256, scenes=8, resolution=256, edge=0.0131, room=(12.0, 3.0, 12.0)):
+    rng = np.random.default_rng(seed)
+    wl = Workload("config3", envs, [(resolution, resolution)] * envs, np.full(envs, 90.0),
+                  np.arange(envs) % scenes, seed=seed, room=tuple(room), walk=True)
+    lo = np.array([-room[0] / 2, 0.0, -room[2] / 2])
+    hi = np.array([room[0] / 2, room[1], room[2] / 2])
+    for s in range(scenes):
+        wl.meshes.append(scan_scene(rng, lo, hi, edge))
+        wl.templates.append((f"config3/s{s}", [(s, 0, len(wl.meshes[-1]["indices"]), 0)]))
+        wl.instances.append([(f"config3/s{s}", None, 0)])
+    wl.materials.append(((1, 1, 1, 1), -1, 0))
+    return wl
+
+
 def config2(seed=2, envs=4096, scenes=64, tri_range=(2e4, 2e6), prototypes=16, texture_size=512):
     rng = np.random.default_rng(seed)
     res = rng.choice([64, 128, 256], size=envs, p=[0.3, 0.5, 0.2])
@@ -306,14 +394,36 @@ def projection(hfov_deg, width, height, near=NEAR, far=FAR):
     return m
 
 
+def _walk(wl, step):
+    """Random walk of every env's camera: uniform start 0.5 m inside the
+    walls, then per step 0.25 m along a uniform direction (reflected at the
+    walls) and a yaw change of +-10 deg."""
+    rx, rz = wl.room[0] / 2 - 0.5, wl.room[2] / 2 - 0.5
+    rng = np.random.default_rng([wl.seed, 104723])
+    E = wl.envs
+    x, z = rng.uniform(-rx, rx, E), rng.uniform(-rz, rz, E)
+    yaw = rng.uniform(0, 2 * math.pi, E)
+    for k in range(step):
+        r = np.random.default_rng([wl.seed, 104729, k])
+        a = r.uniform(0, 2 * math.pi, E)
+        x, z = x + 0.25 * np.cos(a), z + 0.25 * np.sin(a)
+        x = np.where(x > rx, 2 * rx - x, np.where(x < -rx, -2 * rx - x, x))
+        z = np.where(z > rz, 2 * rz - z, np.where(z < -rz, -2 * rz - z, z))
+        yaw = yaw + np.radians(10.0) * r.choice([-1.0, 1.0], E)
+    return x, z, yaw
+
+
 def camera_poses(wl, step=0):
-    """(projections [E,4,4], views [E,4,4]) for one step: position uniform in
-    the room at 1.25 m, yaw uniform."""
+    """(projections [E,4,4], views [E,4,4]) for one step: at 1.25 m, position
+    uniform in the room and yaw uniform (fresh every step), or the random
+    walk of ``_walk`` for walking workloads."""
     rng = np.random.default_rng([wl.seed, 7919, step])
     E = wl.envs
-    x = rng.uniform(-ROOM[0] / 2 + 0.05, ROOM[0] / 2 - 0.05, E)
-    z = rng.uniform(-ROOM[2] / 2 + 0.05, ROOM[2] / 2 - 0.05, E)
+    x = rng.uniform(-wl.room[0] / 2 + 0.05, wl.room[0] / 2 - 0.05, E)
+    z = rng.uniform(-wl.room[2] / 2 + 0.05, wl.room[2] / 2 - 0.05, E)
     yaw = rng.uniform(0, 2 * math.pi, E)
+    if wl.walk:
+        x, z, yaw = _walk(wl, step)
     views = np.zeros((E, 4, 4), np.float64)
     c, s = np.cos(yaw), np.sin(yaw)
     # camera-to-world = T(x, 1.25, z) * Ry(yaw); view = its inverse

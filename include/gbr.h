@@ -217,8 +217,9 @@ gbr_status gbr_scene_stats(gbr_renderer* r, uint32_t scene, gbr_scene_stats_info
 /* RendererStandalone::colorImageInto / depthImageInto
  * (RendererStandalone.cpp:168-180, 189-202): copy rect {x0, y0, x1, y1} of a plane
  * of the tile-grid framebuffer into host memory with the given row pitch.
- * plane is one GBR_PLANE_* bit.  For the ragged layout use
- * gbr_scene_image_into. */
+ * plane is one GBR_PLANE_* bit.  The ragged layout is one row of all
+ * scenes' pixels ({total pixels, 1}, scene after scene); single scenes are
+ * easier read with gbr_scene_image_into. */
 gbr_status gbr_image_into(gbr_renderer* r, uint32_t plane, const int32_t rect[4], void* dst,
                           uint64_t dst_row_bytes);
 gbr_status gbr_color_image_into(gbr_renderer* r, const int32_t rect[4], void* dst,

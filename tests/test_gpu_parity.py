@@ -111,6 +111,50 @@ def test_ragged_mixed_resolution(pkg, procedural):
     _parity(pkg, procedural, wl)
 
 
+def test_config3_scan_subset(pkg, procedural):
+    """Scan-like rooms (noisy tessellated shell, value-noise colours,
+    Voronoi ids per vertex) at 5 cm edges, 256^2, three steps of the random
+    walk, both draw modes."""
+    wl = procedural.config3(envs=6, scenes=2, edge=0.05)
+    _parity(pkg, procedural, wl, steps=(0, 1, 7))
+
+
+def test_config3_full_density_scene(pkg, procedural):
+    """One 5M-triangle scan room at full density: 16 walking envs in one
+    batched step equal the per-scene path and the same step with occlusion
+    culling off; two envs equal the oracle."""
+    from oracle.model import OracleRenderer
+    wl = procedural.config3(envs=16, scenes=1)
+    gpu = procedural.build_renderer(pkg, wl, mode=1)
+    poses = procedural.camera_poses(wl, 3)
+    procedural.set_cameras(gpu, wl, poses)
+    gpu.draw(mode=1, graph=True)
+    planes = (pkg.Plane.Color, pkg.Plane.Depth, pkg.Plane.LinearDepth, pkg.Plane.Semantic)
+    ref = [gpu.sceneImage(p, s).copy() for s in range(16) for p in planes]
+    gpu.draw(mode=0)
+    assert all(np.array_equal(a.view(np.uint8), gpu.sceneImage(p, s).view(np.uint8))
+               for a, (s, p) in zip(ref, [(s, p) for s in range(16) for p in planes]))
+    gpu.setTuning(occlusion_culling=0)
+    gpu.draw(mode=1)
+    assert all(np.array_equal(a.view(np.uint8), gpu.sceneImage(p, s).view(np.uint8))
+               for a, (s, p) in zip(ref, [(s, p) for s in range(16) for p in planes]))
+    sample = [0, 9]
+    cpu = procedural.build_oracle(OracleRenderer, wl, envs=sample)
+    procedural.set_cameras(cpu, wl, poses, sample)
+    cpu.draw(threads=8)
+    assert_parity([compare_scene(_Subset(gpu, sample), cpu, pkg, k) for k in range(len(sample))])
+
+
+class _Subset:
+    """The GPU renderer seen through a list of its scenes (for compare_scene)."""
+
+    def __init__(self, r, scenes):
+        self.r, self.scenes = r, scenes
+
+    def sceneImage(self, plane, k):
+        return self.r.sceneImage(plane, self.scenes[k])
+
+
 def look_view(x, y, z, yaw, pitch):
     """View matrix ([col][row] float32) of a camera at (x, y, z) turned by yaw
     about +y, then pitch about its x axis."""
