@@ -44,6 +44,9 @@ constexpr int kMaxHierarchyDepth = 64;
 __host__ __device__ constexpr uint32_t ring_capacity(int threads) {
   return threads > 512 ? 2048u : (threads > 256 ? 1024u : 512u);
 }
+// Capacity of the ring of clusters that passed culling (a power of two); a
+// cluster pass tests at most as many clusters as there is room for.
+constexpr uint32_t kClusterRing = 256;
 
 __device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
@@ -135,14 +138,14 @@ constexpr uint32_t kSortCap = 2048;
 
 template <int T>
 __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
-  __shared__ uint32_t s_warp[T / 32], s_total, s_count, s_tris, s_chunks;
+  __shared__ uint32_t s_warp[T / 32], s_total, s_count, s_tris, s_clusters;
   __shared__ float s_key[kSortCap];
   __shared__ uint16_t s_idx[kSortCap];
   const uint32_t s = p.scene_base + blockIdx.x;
   const CameraRec& cam = p.cameras[s];
   const uint32_t vis_base = cam.vis_base;
   if (!cam.enabled) {
-    if (threadIdx.x == 0) p.vis_count[s] = p.vis_tris[s] = p.vis_chunks[s] = 0;
+    if (threadIdx.x == 0) p.vis_count[s] = p.vis_tris[s] = p.vis_clusters[s] = 0;
     return;
   }
   // The scene renders the nodes and draws of its source scene.
@@ -150,7 +153,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
   if (threadIdx.x == 0) {
     s_count = 0;
     s_tris = 0;
-    s_chunks = 0;
+    s_clusters = 0;
   }
   float pv[16], vrow[4];
 #pragma unroll
@@ -160,7 +163,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
   __syncthreads();
   for (uint32_t base = 0; base < sc.draw_count; base += T) {
     const uint32_t j = base + threadIdx.x;
-    uint32_t vis = 0, tris = 0, chunks = 0;
+    uint32_t vis = 0, tris = 0, clusters = 0;
     float far = 0.0f;  // distance of the bounding box's farthest corner along the view axis
     VisibleRec rec;
     if (j < sc.draw_count) {
@@ -221,7 +224,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
           const MeshRec m = p.meshes[d.mesh];
           vis = 1;
           tris = d.tri_count;
-          chunks = d.chunk_count;
+          clusters = cluster_count(d.chunk_count);
           rec.vertex_base = m.vertex_base;
           rec.first_index = d.first_index;
           rec.tri_count = d.tri_count;
@@ -240,11 +243,11 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
     const uint32_t to = block_exclusive_scan<T>(tris, s_warp, &s_total);
     const uint32_t ttot = s_total;
     __syncthreads();
-    const uint32_t co = block_exclusive_scan<T>(chunks, s_warp, &s_total);
+    const uint32_t co = block_exclusive_scan<T>(clusters, s_warp, &s_total);
     const uint32_t ctot = s_total;
     if (vis) {
       rec.ordinal = s_tris + to;
-      rec.chunk = s_chunks + co;
+      rec.cluster = s_clusters + co;
       p.visible[vis_base + s_count + vo] = rec;
       if (s_count + vo < kSortCap) s_key[s_count + vo] = far == far ? far : INFINITY;
     }
@@ -252,14 +255,14 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
     if (threadIdx.x == 0) {
       s_count += vtot;
       s_tris += ttot;
-      s_chunks += ctot;
+      s_clusters += ctot;
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     p.vis_count[s] = s_count;
     p.vis_tris[s] = s_tris;
-    p.vis_chunks[s] = s_chunks;
+    p.vis_clusters[s] = s_clusters;
   }
 
   // Processing order: visible draws by the distance of their farthest
@@ -271,7 +274,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
   uint2* order = p.order + vis_base;
   const VisibleRec* visible = p.visible + vis_base;  // written above by this CTA: plain loads
   if (n > kSortCap) {
-    for (uint32_t k = threadIdx.x; k < n; k += T) order[k] = make_uint2(k, visible[k].chunk);
+    for (uint32_t k = threadIdx.x; k < n; k += T) order[k] = make_uint2(k, visible[k].cluster);
     return;
   }
   uint32_t m = 1;
@@ -303,7 +306,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
   for (uint32_t base = 0; base < n; base += T) {
     const uint32_t k = base + threadIdx.x;
     const uint32_t d = k < n ? s_idx[k] : 0u;
-    const uint32_t cnt = k < n ? visible[d].chunk_count : 0u;
+    const uint32_t cnt = k < n ? cluster_count(visible[d].chunk_count) : 0u;
     const uint32_t off = block_exclusive_scan<T>(cnt, s_warp, &s_total);
     if (k < n) order[k] = make_uint2(d, running + off);
     running += s_total;
@@ -323,7 +326,7 @@ struct QEntry {
 // Dynamic shared-memory layout of raster_kernel; every section starts on a
 // 16-byte boundary.
 struct SmemLayout {
-  size_t queue, qoff, prefix, chunks, tiles, coarse, total;
+  size_t queue, qoff, prefix, chunks, clusters, tiles, coarse, total;
 };
 
 // Depth tiles of the occlusion test: kTile x kTile pixels of the region,
@@ -341,7 +344,8 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int threads, int regi
   l.qoff = align16(l.queue + size_t(threads) * sizeof(QEntry));
   l.prefix = align16(l.qoff + size_t(threads + 1) * 4);
   l.chunks = align16(l.prefix + size_t(prefix_cap + 1) * 4);
-  l.tiles = align16(l.chunks + size_t(ring_capacity(threads)) * sizeof(uint2));
+  l.clusters = align16(l.chunks + size_t(ring_capacity(threads)) * sizeof(uint2));
+  l.tiles = align16(l.clusters + size_t(kClusterRing) * sizeof(uint2));
   l.coarse = align16(l.tiles + size_t(tile_capacity(region_px, kTile)) * 4);
   l.total = align16(l.coarse + size_t(tile_capacity(region_px, kTile * kCoarse)) * 4);
   return l;
@@ -719,8 +723,8 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
   sid = (flags & kMeshObjectId) ? __float_as_uint(__ldg(&p.pos[v[2]]).w) : u6.x;
 }
 
-// Largest k in [0, n) with order[k].y (first chunk in processing order) <= g.
-__device__ __forceinline__ uint32_t find_chunk_draw(const uint2* order, uint32_t n, uint32_t g) {
+// Largest k in [0, n) with order[k].y (first cluster in processing order) <= g.
+__device__ __forceinline__ uint32_t find_cluster_draw(const uint2* order, uint32_t n, uint32_t g) {
   uint32_t lo = 0, hi = n;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
@@ -732,8 +736,8 @@ __device__ __forceinline__ uint32_t find_chunk_draw(const uint2* order, uint32_t
   return lo;
 }
 
-// Culling of one 32-triangle chunk by its object-space box, decided by the
-// thread that owns the chunk.  Rejected when
+// Culling of a 32-triangle chunk or a 1024-triangle cluster by its
+// object-space box, decided by the thread that owns it.  Rejected when
 //  * frustum: all eight corners lie beyond one clip plane (outcode margins);
 //  * region: the box projects (two pixels of margin) outside the region;
 //  * occlusion: every fragment it could produce loses the depth test against
@@ -820,9 +824,10 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
   uint32_t* qoff = reinterpret_cast<uint32_t*>(smem + L.qoff);
   uint32_t* prefix = reinterpret_cast<uint32_t*>(smem + L.prefix);
   uint2* chunks = reinterpret_cast<uint2*>(smem + L.chunks);
+  uint2* cring = reinterpret_cast<uint2*>(smem + L.clusters);
   uint32_t* tiles = reinterpret_cast<uint32_t*>(smem + L.tiles);
   uint32_t* coarse = reinterpret_cast<uint32_t*>(smem + L.coarse);
-  __shared__ uint32_t s_item, s_qcount, s_total, s_rd, s_wr, s_next;
+  __shared__ uint32_t s_item, s_qcount, s_total, s_rd, s_wr, s_crd, s_cwr, s_next;
   __shared__ float s_unorm[256];
   for (int i = threadIdx.x; i < 256; i += T) s_unorm[i] = __fdiv_rn(float(i), 255.0f);
   __shared__ uint32_t s_warp[T / 32];
@@ -860,16 +865,19 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
     if (threadIdx.x == 0) s_qcount = 0;
     __syncthreads();
 
-    // Chunks of the visible draws, in processing order (nearest draws
-    // first).  Cull passes: each thread tests one chunk (chunk_keep:
-    // frustum, region, occlusion against the depth tiles) and the survivors
-    // are appended to a ring.  Rounds: each warp takes one chunk of the ring
-    // and its lanes set up one triangle each; triangles covering more than
-    // small_area pixels are queued.  The queue is rasterised by the whole
-    // CTA (flush) once it is half full, before a cull pass and at the end.
-    // A cull pass runs whenever fewer chunks than warps wait in the ring,
-    // after the depth tiles are refreshed from the z-buffer.
-    const uint32_t nchunks = p.vis_chunks[wi.scene];
+    // Clusters (1024 triangles) and chunks (32 triangles) of the visible
+    // draws, in processing order (nearest draws first).  Cull passes test
+    // boxes with chunk_keep (frustum, region, occlusion against the depth
+    // tiles): a cluster pass tests one cluster per thread and appends the
+    // survivors to the cluster ring; a chunk pass gives each warp one
+    // surviving cluster, tests its 32 chunks (one per lane) and appends the
+    // survivors to the chunk ring.  Rounds: each warp takes one chunk of the
+    // ring and its lanes set up one triangle each; triangles covering more
+    // than small_area pixels are queued.  The queue is rasterised by the
+    // whole CTA (flush) once it is half full, before a cull pass and at the
+    // end.  A cull pass runs whenever fewer chunks than warps wait in the
+    // chunk ring, after the depth tiles are refreshed from the z-buffer.
+    const uint32_t nclusters = p.vis_clusters[wi.scene];
     const uint2* order = p.order + vis_base;
     const bool whole = c.rw == c.W && c.rh == c.H;
     const bool occlusion = p.occlusion && p.boxes;
@@ -877,15 +885,18 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
     const int tcols = (c.rw + kTile - 1) / kTile, trows = (c.rh + kTile - 1) / kTile;
     const int ccols = (tcols + kCoarse - 1) / kCoarse, crows = (trows + kCoarse - 1) / kCoarse;
     if (threadIdx.x == 0) {
-      s_rd = s_wr = s_next = 0;
+      s_rd = s_wr = s_crd = s_cwr = s_next = 0;
     }
     (void)total;
     bool tiles_stale = true;  // uniform: the z-buffer changed since the last refresh
     __syncthreads();
     for (;;) {
-      const uint32_t rd = s_rd, wr = s_wr, next = s_next, nq = min(s_qcount, uint32_t(T));
+      const uint32_t rd = s_rd, wr = s_wr, crd = s_crd, cwr = s_cwr, next = s_next,
+                     nq = min(s_qcount, uint32_t(T));
       __syncthreads();  // everyone has read the counters
-      const bool need_cull = wr - rd < uint32_t(T / 32) && next < nchunks;
+      const bool low = wr - rd < uint32_t(T / 32);
+      const bool clusters_left = next < nclusters, have_clusters = cwr != crd;
+      const bool need_cull = low && (clusters_left || have_clusters);
       if (nq > 0 && (nq >= uint32_t(T / 2) || need_cull || wr == rd)) {
         // ---- flush: every thread takes a contiguous run of the queued
         // triangles' bounding-box pixels.
@@ -938,7 +949,6 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
         continue;
       }
       if (need_cull) {
-        // ---- cull pass
         if (occlusion && tiles_stale) {
           // Deepest depth (as ordered bits; empty pixels are all ones) of
           // each tile; pixels outside the region count as 0.
@@ -963,35 +973,76 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
           __syncthreads();
           tiles_stale = false;
         }
-        const uint32_t g = next + threadIdx.x;
-        bool keep = false;
-        uint2 od = make_uint2(0u, 0u);
-        if (g < nchunks) {
-          const uint32_t k = find_chunk_draw(order, nvis, g);
-          od = __ldg(&order[k]);
-          const VisibleRec* rec = vis + od.x;
-          const bool inside = __ldg(&rec->flags) & kDrawInsideFrustum;
-          keep = true;
-          if (p.boxes && (occlusion || !(inside && whole))) {
-            float mvp[16];
-            const float4* m4 = reinterpret_cast<const float4*>(rec->mvp);
+        if (have_clusters && (cwr - crd >= uint32_t(T / 32) || !clusters_left)) {
+          // ---- chunk pass: warp w tests the chunks of surviving cluster w.
+          const uint32_t n = min(cwr - crd, uint32_t(T / 32));
+          bool keep = false;
+          uint2 out = make_uint2(0u, 0u);
+          if (uint32_t(warp) < n) {
+            const uint2 cl = cring[(crd + warp) & (kClusterRing - 1)];  // (draw, cluster in draw)
+            const VisibleRec* rec = vis + cl.x;
+            const uint32_t nch = __ldg(&rec->chunk_count);
+            const uint32_t chunk = cl.y * kClusterChunks + lane;
+            if (chunk < nch) {
+              keep = true;
+              const bool inside = __ldg(&rec->flags) & kDrawInsideFrustum;
+              if (p.boxes && (occlusion || !(inside && whole))) {
+                float mvp[16];
+                const float4* m4 = reinterpret_cast<const float4*>(rec->mvp);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              const float4 v = __ldg(m4 + i);
-              mvp[4 * i] = v.x;
-              mvp[4 * i + 1] = v.y;
-              mvp[4 * i + 2] = v.z;
-              mvp[4 * i + 3] = v.w;
+                for (int i = 0; i < 4; ++i) {
+                  const float4 v = __ldg(m4 + i);
+                  mvp[4 * i] = v.x;
+                  mvp[4 * i + 1] = v.y;
+                  mvp[4 * i + 2] = v.z;
+                  mvp[4 * i + 3] = v.w;
+                }
+                keep = chunk_keep(mvp, p.boxes[__ldg(&rec->box_base) + chunk], c, !inside, !whole,
+                                  occlusion ? tiles : nullptr, coarse, tcols, ccols);
+              }
+              out = make_uint2(cl.x, chunk);
             }
-            keep = chunk_keep(mvp, p.boxes[__ldg(&rec->box_base) + (g - od.y)], c, !inside, !whole,
-                              occlusion ? tiles : nullptr, coarse, tcols, ccols);
           }
-        }
-        const uint32_t pos = block_exclusive_scan<T>(keep ? 1u : 0u, s_warp, &s_total);
-        if (keep) chunks[(wr + pos) & (ring_capacity(T) - 1)] = make_uint2(od.x, g - od.y);
-        if (threadIdx.x == 0) {
-          s_wr = wr + s_total;
-          s_next = next + T;
+          const uint32_t pos = block_exclusive_scan<T>(keep ? 1u : 0u, s_warp, &s_total);
+          if (keep) chunks[(wr + pos) & (ring_capacity(T) - 1)] = out;
+          if (threadIdx.x == 0) {
+            s_wr = wr + s_total;
+            s_crd = crd + n;
+          }
+        } else {
+          // ---- cluster pass: one cluster per thread, as many as the ring holds.
+          const uint32_t m = min(min(uint32_t(T), kClusterRing - (cwr - crd)), nclusters - next);
+          const uint32_t g = next + threadIdx.x;
+          bool keep = false;
+          uint2 od = make_uint2(0u, 0u);
+          if (threadIdx.x < m) {
+            const uint32_t k = find_cluster_draw(order, nvis, g);
+            od = __ldg(&order[k]);
+            const VisibleRec* rec = vis + od.x;
+            const bool inside = __ldg(&rec->flags) & kDrawInsideFrustum;
+            keep = true;
+            if (p.boxes && (occlusion || !(inside && whole))) {
+              float mvp[16];
+              const float4* m4 = reinterpret_cast<const float4*>(rec->mvp);
+#pragma unroll
+              for (int i = 0; i < 4; ++i) {
+                const float4 v = __ldg(m4 + i);
+                mvp[4 * i] = v.x;
+                mvp[4 * i + 1] = v.y;
+                mvp[4 * i + 2] = v.z;
+                mvp[4 * i + 3] = v.w;
+              }
+              const uint32_t nch = __ldg(&rec->chunk_count);
+              keep = chunk_keep(mvp, p.boxes[__ldg(&rec->box_base) + nch + (g - od.y)], c, !inside,
+                                !whole, occlusion ? tiles : nullptr, coarse, tcols, ccols);
+            }
+          }
+          const uint32_t pos = block_exclusive_scan<T>(keep ? 1u : 0u, s_warp, &s_total);
+          if (keep) cring[(cwr + pos) & (kClusterRing - 1)] = make_uint2(od.x, g - od.y);
+          if (threadIdx.x == 0) {
+            s_cwr = cwr + s_total;
+            s_next = next + m;
+          }
         }
         __syncthreads();
         continue;
@@ -1180,7 +1231,7 @@ struct NoAllocScratch {
   SceneRec scene;
   VisibleRec visible;
   MaterialRec material;
-  uint32_t vis_count, vis_tris, vis_chunks, counter, bad_index;
+  uint32_t vis_count, vis_tris, vis_clusters, counter, bad_index;
   WorkItem items[kNoAllocMaxItems];
 };
 static_assert(sizeof(NoAllocScratch) <= kNoAllocScratchBytes, "no-alloc scratch too small");
@@ -1251,7 +1302,8 @@ __global__ void no_alloc_setup(const NoAllocSetup a, NoAllocScratch* s) {
     v.semantic_id = a.semantic_id;
     v.ordinal = 0;
     v.flags = a.flags;
-    v.chunk = 0;
+    v.cluster = 0;
+    v.chunk_count = (a.triangles + kChunkTris - 1) / kChunkTris;
     v.box_base = 0;
     s->visible = v;
     MaterialRec m{};
@@ -1262,7 +1314,7 @@ __global__ void no_alloc_setup(const NoAllocSetup a, NoAllocScratch* s) {
     s->material = m;
     s->vis_count = ok && a.triangles ? 1u : 0u;
     s->vis_tris = ok ? a.triangles : 0u;
-    s->vis_chunks = ok ? (a.triangles + kChunkTris - 1) / kChunkTris : 0u;
+    s->vis_clusters = ok ? cluster_count((a.triangles + kChunkTris - 1) / kChunkTris) : 0u;
     s->counter = 0u;
   }
   const int cols = (a.width + kNoAllocRegion - 1) / kNoAllocRegion;
@@ -1368,7 +1420,7 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
   p.visible = &s->visible;
   p.vis_count = &s->vis_count;
   p.vis_tris = &s->vis_tris;
-  p.vis_chunks = &s->vis_chunks;
+  p.vis_clusters = &s->vis_clusters;
   p.boxes = nullptr;
   p.pos = static_cast<const float4*>(positions);
   p.color = static_cast<const float4*>(colors);

@@ -29,10 +29,10 @@ struct PrepareParams {
   const float* local;
   const MeshRec* meshes;
   VisibleRec* visible;
-  uint2* order;        // per visible draw: (draw, first chunk) in processing order
+  uint2* order;        // per visible draw: (draw, first cluster) in processing order
   uint32_t* vis_count;
   uint32_t* vis_tris;
-  uint32_t* vis_chunks;
+  uint32_t* vis_clusters;
   uint32_t* status;
   uint32_t scene_base;
 };
@@ -48,8 +48,8 @@ struct RasterParams {
   const uint2* order;         // processing order of the visible draws (see PrepareParams)
   const uint32_t* vis_count;
   const uint32_t* vis_tris;
-  const uint32_t* vis_chunks;
-  const ChunkBox* boxes;      // box per 32-triangle chunk (null: no chunk culling)
+  const uint32_t* vis_clusters;
+  const ChunkBox* boxes;      // chunk and cluster boxes (null: no box culling)
   const float4* pos;
   const float4* color;
   const float2* uv;

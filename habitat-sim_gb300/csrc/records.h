@@ -12,7 +12,8 @@
 //   per step   VisibleRec[] (128 B, written by the prepare kernel) and its
 //              processing order uint2[] (8 B per visible draw),
 //              vis_count[s], vis_tris[s], vis_chunks[s]; WorkItem[] + one counter
-//   views      ChunkBox[] (32 B per 32 triangles of every mesh view)
+//   views      ChunkBox[] (32 B per 32 triangles of every mesh view, then
+//              32 B per 1024 triangles: the cluster boxes)
 //   output     colour u32, window depth f32, linear depth f32, id u32
 //              planes, one element per framebuffer pixel.
 #pragma once
@@ -94,8 +95,8 @@ struct alignas(16) VisibleRec {
   uint32_t semantic_id;
   uint32_t ordinal;    // index of this draw's first triangle in the scene
   uint32_t flags;      // mesh flags
-  uint32_t chunk;      // index of this draw's first chunk in the scene
-  uint32_t box_base;   // first chunk box of the draw's view
+  uint32_t cluster;    // index of this draw's first cluster in the scene (draw order)
+  uint32_t box_base;   // first chunk box of the draw's view; its cluster boxes follow
   uint32_t chunk_count;
   uint32_t pad[2];
 };
@@ -107,6 +108,12 @@ static_assert(offsetof(VisibleRec, zrow) == 64 && offsetof(VisibleRec, vertex_ba
 
 // Triangles per chunk: the unit of work a warp takes and of bounding-box culling.
 constexpr uint32_t kChunkTris = 32;
+// Chunks per cluster: the coarser culling level.  A mesh view's boxes are
+// its chunk_count chunk boxes followed by ceil(chunk_count / 32) cluster boxes.
+constexpr uint32_t kClusterChunks = 32;
+__host__ __device__ inline uint32_t cluster_count(uint32_t chunks) {
+  return (chunks + kClusterChunks - 1) / kClusterChunks;
+}
 
 // Object-space bounding box of one chunk of a mesh view.
 struct ChunkBox {

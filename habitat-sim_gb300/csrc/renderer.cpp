@@ -423,7 +423,7 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
       mv.bbox[3 + c] = hi[c];
     }
     mv.chunk_count = (v.index_count / 3 + kChunkTris - 1) / kChunkTris;
-    mv.box_base = uint32_t(box_pool_.alloc(mv.chunk_count));
+    mv.box_base = uint32_t(box_pool_.alloc(mv.chunk_count + cluster_count(mv.chunk_count)));
     if (boxes_.size() < box_pool_.end) boxes_.resize(box_pool_.end);
     build_chunk_boxes(m, v.index_offset, v.index_count, mv.box_base);
     mv.live = true;
@@ -455,6 +455,17 @@ void Renderer::build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32
       }
     }
     boxes_[box_base + t0 / kChunkTris] = b;
+  }
+  // Cluster boxes: the union of every kClusterChunks consecutive chunk boxes.
+  const uint32_t chunks = (tris + kChunkTris - 1) / kChunkTris;
+  for (uint32_t c0 = 0; c0 < chunks; c0 += kClusterChunks) {
+    ChunkBox b = boxes_[box_base + c0];
+    for (uint32_t c = c0 + 1; c < std::min(chunks, c0 + kClusterChunks); ++c)
+      for (int k = 0; k < 3; ++k) {
+        b.lo[k] = std::min(b.lo[k], boxes_[box_base + c].lo[k]);
+        b.hi[k] = std::max(b.hi[k], boxes_[box_base + c].hi[k]);
+      }
+    boxes_[box_base + chunks + c0 / kClusterChunks] = b;
   }
 }
 
@@ -724,7 +735,7 @@ gbr_status Renderer::remove_template(const char* name) {
   if (gbr_status s = quiesce()) return s;
   for (uint32_t i = found->second.first; i < found->second.second; ++i) {
     MeshView& v = views_[i];
-    box_pool_.release(v.box_base, v.chunk_count);
+    box_pool_.release(v.box_base, v.chunk_count + cluster_count(v.chunk_count));
     v.live = false;
   }
   names_.erase(found);
@@ -734,7 +745,7 @@ gbr_status Renderer::remove_template(const char* name) {
 
 gbr_status Renderer::memory_usage(uint64_t* live, uint64_t* reserved) const {
   // Bytes per element: vertices 16 position + 16 colour + 8 texcoord,
-  // indices and texels 4, chunk boxes 32.
+  // indices and texels 4, chunk and cluster boxes 32.
   constexpr uint64_t kV = 40, kI = 4, kT = 4, kB = sizeof(ChunkBox);
   if (live)
     *live = vertex_pool_.live() * kV + index_pool_.live() * kI + texel_pool_.live() * kT +
@@ -871,7 +882,7 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
       !d_visible_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(VisibleRec), false) ||
       !d_order_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(uint2), false) ||
       !d_vis_count_.reserve(S1 * 4, false) || !d_vis_tris_.reserve(S1 * 4, false) ||
-      !d_vis_chunks_.reserve(S1 * 4, false) ||
+      !d_vis_clusters_.reserve(S1 * 4, false) ||
       !d_status_.reserve(4, false) || !d_counter_.reserve(4, false) ||
       !d_items_.reserve(std::max<size_t>(items.size(), 1) * sizeof(WorkItem), false) ||
       !d_items_lpt_.reserve(std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem), false) ||
@@ -1046,7 +1057,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   pp.order = d_order_.as<uint2>();
   pp.vis_count = d_vis_count_.as<uint32_t>();
   pp.vis_tris = d_vis_tris_.as<uint32_t>();
-  pp.vis_chunks = d_vis_chunks_.as<uint32_t>();
+  pp.vis_clusters = d_vis_clusters_.as<uint32_t>();
   pp.status = d_status_.as<uint32_t>();
   RasterParams rp{};
   rp.scenes = pp.scenes;
@@ -1055,7 +1066,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   rp.order = pp.order;
   rp.vis_count = pp.vis_count;
   rp.vis_tris = pp.vis_tris;
-  rp.vis_chunks = pp.vis_chunks;
+  rp.vis_clusters = pp.vis_clusters;
   rp.boxes = d_boxes_.as<ChunkBox>();
   rp.pos = d_pos_.as<float4>();
   rp.color = d_color_.as<float4>();

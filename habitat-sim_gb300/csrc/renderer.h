@@ -49,7 +49,7 @@ struct MeshView {
   uint32_t mesh, index_offset, index_count, material;
   float transform[16];
   float bbox[6];
-  uint32_t box_base;     // first chunk box of this view
+  uint32_t box_base;     // first chunk box of this view (its cluster boxes follow)
   uint32_t chunk_count;  // 32-triangle chunks of this view
   bool live;             // false once its template was removed
 };
@@ -185,7 +185,7 @@ class Renderer {
   DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_;
   DeviceBuffer d_meshes_, d_materials_, d_textures_, d_boxes_;
   DeviceBuffer d_scenes_, d_parents_, d_local_, d_draws_, d_cameras_;
-  DeviceBuffer d_visible_, d_order_, d_vis_count_, d_vis_tris_, d_vis_chunks_, d_status_, d_items_,
+  DeviceBuffer d_visible_, d_order_, d_vis_count_, d_vis_tris_, d_vis_clusters_, d_status_, d_items_,
       d_items_lpt_, d_counter_;
   DeviceBuffer d_planes_[4];
   PinnedBuffer h_stage_;

@@ -52,9 +52,10 @@ class SceneAsset:
     def device_bytes(self):
         """Bytes the renderer keeps on the device for this scene: 40 per
         vertex (position, colour, texcoord), 4 per index, 4 per texel, 32 per
-        32-triangle chunk box."""
+        box (one per 32-triangle chunk and one per 32 chunks)."""
         chunks = (self.triangles + 31) // 32
-        return len(self.positions) * 40 + len(self.indices) * 4 + self.texture.size + chunks * 32
+        boxes = chunks + (chunks + 31) // 32
+        return len(self.positions) * 40 + len(self.indices) * 4 + self.texture.size + boxes * 32
 
 
 def serving_scene(seed, triangles, texture_size=64):

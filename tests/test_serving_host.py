@@ -91,5 +91,6 @@ def test_catalog_scene_sizes(server):
         assert a.indices.max() < len(a.positions)
         assert set(np.unique(a.object_ids)) == set(range(1, 22))
         chunks = (a.triangles + 31) // 32
-        assert a.device_bytes() == len(a.positions) * 40 + a.triangles * 12 + 64 * 64 * 4 + chunks * 32
+        boxes = chunks + (chunks + 31) // 32
+        assert a.device_bytes() == len(a.positions) * 40 + a.triangles * 12 + 64 * 64 * 4 + boxes * 32
     assert cat.asset(2) is cat.asset(2)
