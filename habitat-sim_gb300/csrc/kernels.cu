@@ -618,11 +618,13 @@ __device__ void sample(const TextureRec& t, const uint32_t* texels, int layer, f
   }
 }
 
+// Float -> unorm8: round to nearest, values within 1e-4 above a tie rounded
+// down (the rounding of the reference's images).
 __device__ __forceinline__ uint32_t unorm8(float c) {
   if (!(c > 0.0f)) c = 0.0f;
   if (c > 1.0f) c = 1.0f;
   float t = __fmul_rn(c, 255.0f);
-  t = __fadd_rn(t, 0.5f);
+  t = __fadd_rn(t, 0.4999f);
   return __float2uint_rz(t);
 }
 

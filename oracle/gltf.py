@@ -369,6 +369,9 @@ def load_gltf(path, whole=False, name=None, no_textures=False):
             if "TEXCOORD_0" in attrs:
                 tc = accessor(attrs["TEXCOORD_0"]).astype(np.float32).copy()
                 tc[:, 1] = np.float32(1.0) - tc[:, 1]
+            normals = None
+            if "NORMAL" in attrs:
+                normals = accessor(attrs["NORMAL"]).astype(np.float32).reshape(-1, 3)
             oid = None
             if "_OBJECT_ID" in attrs:
                 oid = accessor(attrs["_OBJECT_ID"]).reshape(-1).astype(np.uint32)
@@ -392,7 +395,7 @@ def load_gltf(path, whole=False, name=None, no_textures=False):
                 raise ImportError_(f"unsupported primitive mode {mode}")
             ids.append(len(out.meshes))
             out.meshes.append(dict(positions=pos, colors=colors, texcoords=tc,
-                                   object_ids=oid, indices=idx))
+                                   object_ids=oid, indices=idx, normals=normals))
             prim_ids.append(prim.get("material", -1))
         m["_ids"] = ids
 

@@ -44,12 +44,22 @@ class _Mesh(ctypes.Structure):
     _fields_ = [("positions", ctypes.c_void_p), ("colors", ctypes.c_void_p),
                 ("texcoords", ctypes.c_void_p), ("object_ids", ctypes.c_void_p),
                 ("indices", ctypes.c_void_p), ("vertex_count", ctypes.c_uint32),
-                ("index_count", ctypes.c_uint32)]
+                ("index_count", ctypes.c_uint32), ("normals", ctypes.c_void_p)]
 
 
 class _Mat(ctypes.Structure):
     _fields_ = [("color", ctypes.c_float * 4), ("texture", ctypes.c_int32),
-                ("layer", ctypes.c_int32), ("matrix", ctypes.c_float * 9)]
+                ("layer", ctypes.c_int32), ("matrix", ctypes.c_float * 9),
+                ("phong", ctypes.c_int32)]
+
+
+class _Light(ctypes.Structure):
+    _fields_ = [("node", ctypes.c_int32), ("type", ctypes.c_int32),
+                ("color", ctypes.c_float * 3), ("range", ctypes.c_float)]
+
+
+LIGHT_DIRECTIONAL = 0
+LIGHT_POINT = 1
 
 
 class _Draw(ctypes.Structure):
@@ -64,7 +74,8 @@ class _Scene(ctypes.Structure):
                 ("pv", ctypes.c_float * 16), ("view", ctypes.c_float * 16),
                 ("node_count", ctypes.c_int32), ("parents", ctypes.c_void_p),
                 ("transforms", ctypes.c_void_p), ("draw_count", ctypes.c_int32),
-                ("draws", ctypes.c_void_p)]
+                ("draws", ctypes.c_void_p), ("light_count", ctypes.c_int32),
+                ("lights", ctypes.c_void_p)]
 
 
 class _Out(ctypes.Structure):
@@ -94,8 +105,11 @@ class OracleRenderer:
     switches the framebuffer to a ragged layout: scene ``s`` occupies
     ``width*height`` consecutive pixels, rows bottom-up."""
 
-    def __init__(self, tile_size=(128, 128), tile_count=(1, 1), flags=0, viewports=None):
+    def __init__(self, tile_size=(128, 128), tile_count=(1, 1), flags=0, viewports=None,
+                 max_light_count=0, ambient_factor=0.1):
         self.flags = flags
+        self.max_light_count = int(max_light_count)
+        self.ambient_factor = float(ambient_factor)
         self.tile_size = tuple(tile_size)
         self.tile_count = tuple(tile_count)
         if viewports is None:
@@ -119,7 +133,7 @@ class OracleRenderer:
         self.textures = [dict(pixels=white, filter=0, wrap_s=0, wrap_t=0)]
         self.meshes = []
         self.materials = [dict(color=np.ones(4, np.float32), texture=0, layer=0,
-                               matrix=np.eye(3, dtype=np.float32))]
+                               matrix=np.eye(3, dtype=np.float32), phong=False)]
         self.mesh_views = []
         self.names = {}
         self.scenes = [self._empty_scene() for _ in range(n)]
@@ -131,7 +145,9 @@ class OracleRenderer:
 
     @staticmethod
     def _empty_scene():
-        return dict(parents=[], transforms=[], draws=[], batches=[])
+        return dict(parents=[], transforms=[], draws=[], batches=[], light_nodes=[],
+                    light_types=[], light_colors=np.zeros((0, 3), np.float32),
+                    light_ranges=np.zeros(0, np.float32))
 
     def sceneCount(self):
         return len(self.scenes)
@@ -149,13 +165,13 @@ class OracleRenderer:
                                       wrap_s=t["wrap_s"], wrap_t=t["wrap_t"]))
         for m in f.meshes:
             self.add_mesh(m["positions"], m["colors"], m["texcoords"], m["object_ids"],
-                          m["indices"])
+                          m["indices"], m.get("normals"))
         for m in f.materials:
             tex = 0 if m["texture"] is None else m["texture"] + texture_offset
             layer = 0 if m["texture"] is None else m["layer"]
             matrix = np.eye(3, dtype=np.float32) if m["texture"] is None else m["matrix"]
             self.materials.append(dict(color=m["color"].astype(np.float32), texture=tex,
-                                       layer=layer, matrix=matrix))
+                                       layer=layer, matrix=matrix, phong=not m["flat"]))
         for v in f.mesh_views:
             mat = 0 if v["material"] == -1 else v["material"] + material_offset
             self.mesh_views.append(dict(mesh=v["mesh"] + mesh_offset,
@@ -169,8 +185,10 @@ class OracleRenderer:
         return True
 
     # ----------------------------------------------------------- procedural
-    def add_mesh(self, positions, colors=None, texcoords=None, object_ids=None, indices=None):
+    def add_mesh(self, positions, colors=None, texcoords=None, object_ids=None, indices=None,
+                 normals=None):
         self.meshes.append(dict(
+            normals=None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 3),
             positions=np.ascontiguousarray(positions, np.float32).reshape(-1, 3),
             colors=None if colors is None else np.ascontiguousarray(colors, np.float32).reshape(-1, 4),
             texcoords=None if texcoords is None else np.ascontiguousarray(texcoords, np.float32).reshape(-1, 2),
@@ -185,11 +203,12 @@ class OracleRenderer:
         self.textures.append(dict(pixels=p, filter=filter, wrap_s=wrap_s, wrap_t=wrap_t))
         return len(self.textures) - 1
 
-    def add_material(self, color=(1, 1, 1, 1), texture=0, layer=0, matrix=None):
+    def add_material(self, color=(1, 1, 1, 1), texture=0, layer=0, matrix=None, shaded=False):
         self.materials.append(dict(color=np.asarray(color, np.float32), texture=int(texture),
                                    layer=int(layer),
                                    matrix=np.eye(3, dtype=np.float32) if matrix is None
-                                   else np.asarray(matrix, np.float32).reshape(3, 3)))
+                                   else np.asarray(matrix, np.float32).reshape(3, 3),
+                                   phong=bool(shaded)))
         return len(self.materials) - 1
 
     def add_node_hierarchy_template(self, name, views):
@@ -235,6 +254,32 @@ class OracleRenderer:
         sc["parents"].append(-1)
         sc["transforms"].append(np.eye(4, dtype=np.float32))
         return len(sc["transforms"]) - 1
+
+    # --------------------------------------------------------------- lights
+    def addLight(self, scene, node, light_type):
+        """Renderer::addLight (Renderer.cpp:990-1015): white, infinite range."""
+        if not self.max_light_count:
+            raise ValueError("max light count is zero")
+        sc = self.scenes[scene]
+        if not 0 <= node < len(sc["parents"]):
+            raise IndexError("node out of range")
+        sc["light_nodes"].append(int(node))
+        sc["light_types"].append(int(light_type))
+        sc["light_colors"] = np.concatenate([sc["light_colors"], np.ones((1, 3), np.float32)])
+        sc["light_ranges"] = np.concatenate([sc["light_ranges"], np.full(1, np.inf, np.float32)])
+        return len(sc["light_nodes"]) - 1
+
+    def clearLights(self, scene):
+        sc = self.scenes[scene]
+        fresh = self._empty_scene()
+        for k in ("light_nodes", "light_types", "light_colors", "light_ranges"):
+            sc[k] = fresh[k]
+
+    def lightColors(self, scene):
+        return self.scenes[scene]["light_colors"]
+
+    def lightRanges(self, scene):
+        return self.scenes[scene]["light_ranges"]
 
     def set_semantic_id(self, scene, node, semantic_id):
         for d in self.scenes[scene]["draws"]:
@@ -283,11 +328,12 @@ class OracleRenderer:
         for i, m in enumerate(self.meshes):
             meshes[i] = _Mesh(_ptr(m["positions"]), _ptr(m["colors"]), _ptr(m["texcoords"]),
                               _ptr(m["object_ids"]), _ptr(m["indices"]), len(m["positions"]),
-                              len(m["indices"]))
+                              len(m["indices"]), _ptr(m.get("normals")))
         mats = (_Mat * len(self.materials))()
         for i, m in enumerate(self.materials):
             mats[i] = _Mat((ctypes.c_float * 4)(*m["color"]), m["texture"], m["layer"],
-                           (ctypes.c_float * 9)(*np.asarray(m["matrix"], np.float32).reshape(-1)))
+                           (ctypes.c_float * 9)(*np.asarray(m["matrix"], np.float32).reshape(-1)),
+                           1 if m.get("phong") else 0)
         scenes = (_Scene * len(self.scenes))()
         for s, sc in enumerate(self.scenes):
             w, h, off, pitch = self.layout[s]
@@ -299,12 +345,18 @@ class OracleRenderer:
             for i, d in enumerate(dl):
                 draws[i] = _Draw(d["node"], d["mesh"], d["index_offset"], d["index_count"],
                                  d["material"], d["semantic"])
-            keep += [parents, transforms, draws]
+            nl = len(sc["light_nodes"])
+            lights = (_Light * max(1, nl))()
+            for j in range(nl):
+                lights[j] = _Light(sc["light_nodes"][j], sc["light_types"][j],
+                                   (ctypes.c_float * 3)(*sc["light_colors"][j].tolist()),
+                                   float(sc["light_ranges"][j]))
+            keep += [parents, transforms, draws, lights]
             scenes[s] = _Scene(w, h, off, pitch,
                                (ctypes.c_float * 16)(*self.pv[s].reshape(-1)),
                                (ctypes.c_float * 16)(*self.view[s].reshape(-1)),
                                len(parents), _ptr(parents), _ptr(transforms), len(dl),
-                               ctypes.addressof(draws))
+                               ctypes.addressof(draws), nl, ctypes.addressof(lights))
         self.color = np.zeros(self.fb_shape, np.uint32)
         self.depth = np.ones(self.fb_shape, np.float32) if window_depth else None
         self.linear_depth = np.zeros(self.fb_shape, np.float32) if linear_depth else None
@@ -312,7 +364,8 @@ class OracleRenderer:
         out = _Out(_ptr(self.color), _ptr(self.depth), _ptr(self.linear_depth),
                    _ptr(self.semantic))
         lib.oracle_render(tex, len(self.textures), meshes, mats, scenes, len(self.scenes),
-                          self.flags, out, threads)
+                          self.flags, out, threads, self.max_light_count,
+                          ctypes.c_float(self.ambient_factor))
 
     # --------------------------------------------------------------- images
     def colorImage(self):

@@ -20,11 +20,20 @@
 //     pixel centres at (x+0.5, y+0.5), window origin bottom-left;
 //   * flat shading when no lights are enabled: colour = base colour *
 //     texture(layer, M * uv) * vertex colour (Renderer.cpp:579-620), written
-//     as RGBA8 with round-to-nearest; background (31,31,31,255)
+//     as RGBA8 with round-to-nearest (see unorm8); background (31,31,31,255)
 //     (GfxBatchRendererTest.cpp:1514-1521);
 //   * linear depth = perspective-correct interpolation of -z_eye, the method
 //     of src/shaders/gfx_batch/depth.vert:15-17, 0 where nothing was drawn
 //     (DepthUnprojection.cpp:116-128); window depth as D32F;
+//   * lit shading when lights are enabled (max_lights > 0) and the material
+//     is not unlit: ambient = colour * ambient factor, diffuse = colour
+//     (Renderer.cpp:579-620), both times texture and vertex colour; every
+//     light of the scene (at most max_lights, world space from its node:
+//     translation for point lights, negative backward axis for directional
+//     ones, Renderer.cpp:1263-1289) adds diffuse * light colour * max(0, N.L)
+//     * attenuation, attenuation = clamp(1 - (d/range)^4, 0, 1)^2 / (1 + d^2);
+//     no specular term (the reference compiles its shaders with NoSpecular);
+//     N = normalize(cofactor(abs) * normal) interpolated per fragment;
 //   * semantic ID: the provoking (last) vertex's object ID when the mesh has
 //     per-vertex IDs, else the draw's ID; 0 where nothing was drawn
 //     (src/esp/gfx/RenderTarget.cpp:189-190).
@@ -70,6 +79,7 @@ struct OracleMesh {
   const uint32_t* object_ids;  // 1 per vertex or null
   const uint32_t* indices;
   uint32_t vertex_count, index_count;
+  const float* normals;     // 3 per vertex or null
 };
 
 struct OracleMaterial {
@@ -77,6 +87,14 @@ struct OracleMaterial {
   int32_t texture;   // renderer texture id, 0 = white
   int32_t layer;
   float matrix[9];   // 3x3, [col][row]
+  int32_t phong;     // 1: lit (ambient = color * ambient factor, diffuse = color)
+};
+
+struct OracleLight {
+  int32_t node;
+  int32_t type;      // 0 directional (along -backward of the node), 1 point
+  float color[3];
+  float range;
 };
 
 struct OracleDraw {
@@ -99,6 +117,8 @@ struct OracleScene {
   const float* transforms;  // 16 per node
   int32_t draw_count;
   const OracleDraw* draws;
+  int32_t light_count;
+  const OracleLight* lights;
 };
 
 struct OracleOutput {
@@ -145,6 +165,16 @@ struct Frame {
   const OracleMaterial* mats;
   int flags;
   OracleOutput out;
+  int max_lights;        // 0: every material flat
+  float ambient_factor;
+};
+
+// A light in world space: position (w = 1) or direction towards the light
+// (w = 0), colour, range.
+struct WorldLight {
+  float pos[4];
+  float color[3];
+  float range;
 };
 
 inline int wrap(int i, int n, int mode) {
@@ -189,11 +219,15 @@ void sample(const OracleTexture& t, int layer, float s, float u, float out[4]) {
   }
 }
 
+// Float -> unorm8: round to nearest, with values within 1e-4 above a tie
+// rounded down.  The reference's images round that way (its shaders land a
+// hair below this restatement's values: e.g. an ambient 0.1 is stored as 25,
+// not 26); every golden image of the flat path matches either way.
 inline uint32_t unorm8(float c) {
   if (!(c > 0.0f)) c = 0.0f;
   if (c > 1.0f) c = 1.0f;
   float t = c * 255.0f;
-  t = t + 0.5f;
+  t = t + 0.4999f;
   return uint32_t(t);
 }
 
@@ -201,11 +235,43 @@ struct Tri {
   V4 c[3];        // clip coordinates
   float d[3];     // -z_eye
   uint32_t vi[3]; // vertex indices
+  float wp[3][3]; // world positions (lit draws)
+  float wn[3][3]; // normals times the normal matrix (lit draws)
 };
+
+// Lit shading (Phong without a specular term, the reference's shader
+// configuration): every light adds diffuse * light colour * max(0, N.L) *
+// attenuation, attenuation = clamp(1 - (d / range)^4, 0, 1)^2 / (1 + d^2)
+// with d the distance to a point light (0 for directional lights).
+void light_rgb(const float n_in[3], const float P[3], const WorldLight* lights, int nl,
+               const float dif[4], float rgb[3]) {
+  float len2 = fma_(n_in[2], n_in[2], fma_(n_in[1], n_in[1], n_in[0] * n_in[0]));
+  float inv = 1.0f / std::sqrt(len2);
+  float n[3] = {n_in[0] * inv, n_in[1] * inv, n_in[2] * inv};
+  for (int j = 0; j < nl; ++j) {
+    const WorldLight& L = lights[j];
+    float l[3];
+    for (int k = 0; k < 3; ++k) l[k] = L.pos[k] - P[k] * L.pos[3];
+    float d2 = fma_(l[2], l[2], fma_(l[1], l[1], l[0] * l[0]));
+    float len = std::sqrt(d2);
+    if (!(len > 0.0f)) continue;
+    float dist = len * L.pos[3];
+    float q = dist / std::max(L.range, 0.0001f);
+    float q2 = q * q;
+    float a = 1.0f - q2 * q2;
+    a = a < 0.0f ? 0.0f : (a > 1.0f ? 1.0f : a);
+    float att = (a * a) / (1.0f + dist * dist);
+    float il = 1.0f / len;
+    float ndl = fma_(n[2], l[2] * il, fma_(n[1], l[1] * il, n[0] * (l[0] * il)));
+    float intensity = (ndl > 0.0f ? ndl : 0.0f) * att;
+    for (int c = 0; c < 3; ++c) rgb[c] = fma_(dif[c] * L.color[c], intensity, rgb[c]);
+  }
+}
 
 // Shade the fragment of `tri` at pixel (px, py): returns colour, linear depth, id.
 void shade(const Frame& f, const OracleScene& sc, const OracleDraw& dr, const Tri& tri,
-           int px, int py, uint32_t* color, float* lin, uint32_t* sid) {
+           const WorldLight* lights, int nl, int px, int py, uint32_t* color, float* lin,
+           uint32_t* sid) {
   const OracleMesh& m = f.meshes[dr.mesh];
   const float sx = float(2 * px + 1 - sc.width) / float(sc.width);
   const float sy = float(2 * py + 1 - sc.height) / float(sc.height);
@@ -247,9 +313,28 @@ void shade(const Frame& f, const OracleScene& sc, const OracleDraw& dr, const Tr
     sample(f.tex[mat.texture], mat.layer, ts, tt, tc);
   }
   uint32_t packed = 0;
-  for (int c = 0; c < 4; ++c) {
-    float v = (mat.color[c] * tc[c]) * vc[c];
-    packed |= unorm8(v) << (8 * c);
+  if (mat.phong && f.max_lights > 0) {
+    float amb[4], dif[4], rgb[3];
+    for (int c = 0; c < 4; ++c) {
+      amb[c] = ((mat.color[c] * f.ambient_factor) * tc[c]) * vc[c];
+      dif[c] = (mat.color[c] * tc[c]) * vc[c];
+    }
+    for (int c = 0; c < 3; ++c) rgb[c] = amb[c];
+    if (nl > 0 && m.normals) {
+      float P[3], N[3];
+      for (int c = 0; c < 3; ++c) {
+        P[c] = interp(tri.wp[0][c], tri.wp[1][c], tri.wp[2][c]);
+        N[c] = interp(tri.wn[0][c], tri.wn[1][c], tri.wn[2][c]);
+      }
+      light_rgb(N, P, lights, nl, dif, rgb);
+    }
+    for (int c = 0; c < 3; ++c) packed |= unorm8(rgb[c]) << (8 * c);
+    packed |= unorm8(dif[3]) << 24;
+  } else {
+    for (int c = 0; c < 4; ++c) {
+      float v = (mat.color[c] * tc[c]) * vc[c];
+      packed |= unorm8(v) << (8 * c);
+    }
   }
   *color = packed;
   *sid = m.object_ids ? m.object_ids[tri.vi[2]] : dr.semantic_id;
@@ -276,6 +361,7 @@ struct SceneRaster {
   const Frame& f;
   const OracleScene& sc;
   std::vector<float> zbuf;
+  std::vector<WorldLight> lights;
 
   SceneRaster(const Frame& f_, const OracleScene& sc_) : f(f_), sc(sc_) {
     zbuf.assign(size_t(sc.width) * sc.height, 1.0f);
@@ -332,7 +418,7 @@ struct SceneRaster {
         const int64_t o = sc.fb_offset + int64_t(py) * sc.pitch + px;
         uint32_t col, sid;
         float lin;
-        shade(f, sc, dr, tri, px, py, &col, &lin, &sid);
+        shade(f, sc, dr, tri, lights.data(), int(lights.size()), px, py, &col, &lin, &sid);
         f.out.color[o] = col;
         if (f.out.depth) f.out.depth[o] = z;
         if (f.out.linear_depth) f.out.linear_depth[o] = lin;
@@ -402,10 +488,49 @@ struct SceneRaster {
       else
         matmul(&abs[size_t(sc.parents[i]) * 16], local, &abs[size_t(i) * 16]);
     }
+    // Lights in world space: the node's translation (point) or its negative
+    // backward axis (directional); at most max_lights of them.
+    const int nl = std::min(sc.light_count, f.max_lights);
+    for (int j = 0; j < nl; ++j) {
+      const OracleLight& L = sc.lights[j];
+      const float* A = &abs[size_t(L.node) * 16];
+      WorldLight w{};
+      if (L.type == 0) {
+        w.pos[0] = -A[8];
+        w.pos[1] = -A[9];
+        w.pos[2] = -A[10];
+        w.pos[3] = 0.0f;
+      } else {
+        w.pos[0] = A[12];
+        w.pos[1] = A[13];
+        w.pos[2] = A[14];
+        w.pos[3] = 1.0f;
+      }
+      for (int c = 0; c < 3; ++c) w.color[c] = L.color[c];
+      w.range = L.range;
+      lights.push_back(w);
+    }
     for (int di = 0; di < sc.draw_count; ++di) {
       const OracleDraw& dr = sc.draws[di];
       const OracleMesh& m = f.meshes[dr.mesh];
       const float* A = &abs[size_t(dr.node) * 16];
+      // Normal matrix: cofactor of the upper-left 3x3 (columns c1 x c2,
+      // c2 x c0, c0 x c1), [col][row].
+      const bool lit = f.max_lights > 0 && f.mats[dr.material].phong && m.normals;
+      float NM[9];
+      if (lit) {
+        const float* c0 = A;
+        const float* c1 = A + 4;
+        const float* c2 = A + 8;
+        const float* cols[3][2] = {{c1, c2}, {c2, c0}, {c0, c1}};
+        for (int k = 0; k < 3; ++k) {
+          const float* u = cols[k][0];
+          const float* v = cols[k][1];
+          NM[k * 3 + 0] = u[1] * v[2] - u[2] * v[1];
+          NM[k * 3 + 1] = u[2] * v[0] - u[0] * v[2];
+          NM[k * 3 + 2] = u[0] * v[1] - u[1] * v[0];
+        }
+      }
       float mvp[16], zrow[4];
       matmul(sc.pv, A, mvp);
       for (int col = 0; col < 4; ++col) {
@@ -429,6 +554,12 @@ struct SceneRaster {
           ze = fma_(zrow[1], p[1], ze);
           ze = fma_(zrow[2], p[2], ze);
           tri.d[k] = -ze;
+          if (lit) {
+            for (int r = 0; r < 3; ++r) tri.wp[k][r] = mrow(A, r, p[0], p[1], p[2]);
+            const float* nv = m.normals + size_t(vi) * 3;
+            for (int r = 0; r < 3; ++r)
+              tri.wn[k][r] = fma_(NM[6 + r], nv[2], fma_(NM[3 + r], nv[1], NM[r] * nv[0]));
+          }
         }
         triangle(dr, tri);
       }
@@ -441,8 +572,9 @@ struct SceneRaster {
 extern "C" int oracle_render(const OracleTexture* textures, int32_t texture_count,
                              const OracleMesh* meshes, const OracleMaterial* materials,
                              const OracleScene* scenes, int32_t scene_count, int32_t flags,
-                             OracleOutput out, int32_t threads) {
-  Frame f{textures, texture_count, meshes, materials, flags, out};
+                             OracleOutput out, int32_t threads, int32_t max_lights,
+                             float ambient_factor) {
+  Frame f{textures, texture_count, meshes, materials, flags, out, max_lights, ambient_factor};
   if (threads < 1) threads = 1;
   std::atomic<int> next{0};
   auto worker = [&]() {

@@ -97,6 +97,33 @@ def camera_at_z(z):
     return translation(0.0, 0.0, -z)  # translation(zAxis(z)).inverted()
 
 
+def look_at(eye, target, up):
+    """Magnum ``Matrix4::lookAt(eye, target, up)``: -Z towards the target."""
+    eye, target, up = (np.asarray(v, f32) for v in (eye, target, up))
+    b = eye - target
+    b = b / f32(np.sqrt((b * b).sum()))
+    r = np.cross(up, b).astype(f32)
+    r = r / f32(np.sqrt((r * r).sum()))
+    u = np.cross(b, r).astype(f32)
+    m = identity()
+    m[0, :3], m[1, :3], m[2, :3], m[3, :3] = r, u, b, eye
+    return m
+
+
+def rotation_y(deg):
+    """Magnum ``Matrix4::rotationY(angle)`` (float sine and cosine)."""
+    a = f32(math.radians(deg))
+    c, s = f32(math.cos(a)), f32(math.sin(a))
+    m = identity()
+    m[0, 0], m[0, 2], m[2, 0], m[2, 2] = c, -s, s, c
+    return m
+
+
+def rgb_hex(v, scale=1.0):
+    """``0xRRGGBB_rgbf * scale``."""
+    return np.array([(v >> 16) & 255, (v >> 8) & 255, v & 255], f32) / f32(255.0) * f32(scale)
+
+
 # ---------------------------------------------------------------- data
 # (name, [(file, flags, name)], singleSceneBatchCount, multipleScenesBatchCount,
 #  maxThreshold, meanThreshold) -- GfxBatchRendererTest.cpp:100-165
@@ -388,6 +415,106 @@ UNPROJECT_DATA = [
 ]
 
 
+LIGHT_DATA = [
+    # name, max lights, scene lights, rotation, three objects, golden
+    ("no lights enabled", 0, 0, 0.0, "flat checkerboard sphere", "shaded yellow sphere",
+     "shaded checkerboard sphere", "GfxBatchRendererTestLightsDisabled.png"),
+    ("no lights added", 2, 0, 0.0, "flat checkerboard sphere", "shaded yellow sphere",
+     "shaded checkerboard sphere", "GfxBatchRendererTestLightsNone.png"),
+    ("two lights", 2, 2, 0.0, "flat checkerboard sphere", "shaded yellow sphere",
+     "shaded checkerboard sphere", "GfxBatchRendererTestLights.png"),
+    ("two lights, rotated", 2, 2, 180.0, "flat checkerboard sphere", "shaded yellow sphere",
+     "shaded checkerboard sphere", "GfxBatchRendererTestLights.png"),
+    ("four lights used but two max", 2, 4, 0.0, "flat checkerboard sphere",
+     "shaded yellow sphere", "shaded checkerboard sphere", "GfxBatchRendererTestLights.png"),
+    ("two lights used but four max", 4, 2, 0.0, "flat checkerboard sphere",
+     "shaded yellow sphere", "shaded checkerboard sphere", "GfxBatchRendererTestLights.png"),
+    ("two lights but everything flat-shaded", 2, 2, 0.0, "flat checkerboard sphere",
+     "flat yellow sphere", "flat checkerboard sphere", "GfxBatchRendererTestLightsDisabled.png"),
+]
+
+DIRECTIONAL, POINT = 0, 1
+
+
+def _light_scene(r, objects, up):
+    checks = []
+    for want, obj in zip((0, 2, 4), objects):
+        checks.append(Check("eq", what=f"node {obj}", got=r.addNodeHierarchy(0, obj), want=want))
+    t = r.transformations(0)
+    t[0] = translation(-1.5, -1.0, 0.0)
+    t[2] = translation(0.0, 1.0, 0.0)
+    t[4] = translation(1.5, -1.0, 0.0)
+    return checks
+
+
+def _add_lights(r, count, up):
+    checks = [Check("eq", what="empty node 6", got=r.addEmptyNode(0), want=6),
+              Check("eq", what="empty node 7", got=r.addEmptyNode(0), want=7)]
+    t = r.transformations(0)
+    t[6] = translation(-1.0, 1.5, 1.0)
+    t[7] = look_at([0, 0, 0], [3, 1, 3], up)
+    for i in range(count):
+        checks.append(Check("eq", what=f"light {i}",
+                            got=r.addLight(0, 6 + i % 2, DIRECTIONAL if i % 2 else POINT), want=i))
+        r.lightColors(0)[i] = rgb_hex(0xccffff, 1.0) if i % 2 else rgb_hex(0x3333ff, 3.0)
+        r.lightRanges(0)[i] = np.inf if i % 2 else 1.0
+    return checks
+
+
+def lights(make_lit, data):
+    """GfxBatchRendererTest::lights (:1908-1993)."""
+    name, max_lights, count, rot, a, b, c, golden = data
+    r = make_lit((128, 96), (1, 1), 0, max_lights)
+    add_files(r, [("batch.gltf", 0, None)])
+    r.updateCamera(0, perspective(60.0, f32(4.0) / f32(3.0), 0.1, 10.0), camera_at_z(5.0))
+    checks = _light_scene(r, (a, b, c), None)
+    if count:
+        checks += _add_lights(r, count, [1, 0, 0])
+    st = r.sceneStats(0)
+    checks.append(Check("eq", what="stats", got=(st.nodeCount, st.drawCount, st.drawBatchCount),
+                        want=(8 if count else 6, 3, 2)))
+    r.draw()
+    checks.append(Check("image", image=r.colorImage().copy(), golden=golden, max=0.75, mean=0.005))
+    t = r.transformations(0)
+    for n in (0, 2, 4):
+        t[n] = mul(t[n], rotation_y(rot))
+    r.draw()
+    checks.append(Check("image", image=r.colorImage().copy(), golden=golden, max=95.0, mean=0.07))
+    return checks
+
+
+def clear_lights(make_lit, data=None):
+    """GfxBatchRendererTest::clearLights (:1995-2117)."""
+    objects = ("flat checkerboard sphere", "shaded yellow sphere", "shaded checkerboard sphere")
+    r = make_lit((128, 96), (1, 1), 0, 2)
+    add_files(r, [("batch.gltf", 0, None)])
+    r.updateCamera(0, perspective(60.0, f32(4.0) / f32(3.0), 0.1, 10.0), camera_at_z(5.0))
+    checks = _light_scene(r, objects, None) + _add_lights(r, 2, [0, 1, 0])
+    r.draw()
+    checks.append(Check("image", image=r.colorImage().copy(),
+                        golden="GfxBatchRendererTestLights.png", max=0.75, mean=0.005))
+    checks.append(Check("eq", what="nodes", got=len(r.transformations(0)), want=8))
+    checks.append(Check("eq", what="lights", got=len(r.lightColors(0)), want=2))
+    r.clearLights(0)
+    checks.append(Check("eq", what="nodes after clearLights", got=len(r.transformations(0)),
+                        want=8))
+    checks.append(Check("eq", what="lights after clearLights", got=len(r.lightColors(0)), want=0))
+    r.draw()
+    checks.append(Check("image", image=r.colorImage().copy(),
+                        golden="GfxBatchRendererTestLightsNone.png", max=0.75, mean=0.005))
+    r.addLight(0, 6, POINT)
+    r.addLight(0, 7, DIRECTIONAL)
+    checks.append(Check("eq", what="lights re-added", got=len(r.lightColors(0)), want=2))
+    r.clear(0)
+    checks.append(Check("eq", what="nodes after clear", got=len(r.transformations(0)), want=0))
+    checks.append(Check("eq", what="lights after clear", got=len(r.lightColors(0)), want=0))
+    checks += _light_scene(r, objects, None) + _add_lights(r, 2, [1, 0, 0])
+    r.draw()
+    checks.append(Check("image", image=r.colorImage().copy(),
+                        golden="GfxBatchRendererTestLights.png", max=0.75, mean=0.005))
+    return checks
+
+
 def image_delta(image, golden):
     """Magnum's image-comparison delta: per pixel the mean of the absolute
     channel differences; returns (max over pixels, mean over pixels)."""
@@ -428,3 +555,10 @@ ALL = ([("defaults", defaults, d) for d in FILE_DATA] +
 
 def ids():
     return [f"{n}[{d[0] or 'default'}]" for (n, _, d) in ALL]
+
+
+LIT = ([("lights", lights, d) for d in LIGHT_DATA] + [("clearLights", clear_lights, None)])
+
+
+def lit_ids():
+    return [n if d is None else f"{n}[{d[0]}]" for (n, _, d) in LIT]

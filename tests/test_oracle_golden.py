@@ -1,10 +1,11 @@
 """Pin the CPU oracle against habitat-sim's own batch-renderer goldens.
 
-Every scenario of ``src/tests/GfxBatchRendererTest.cpp`` that runs without
-lights is replayed on the oracle and compared with the reference's golden
-screenshot using the reference's thresholds (0/0 for uncompressed textures,
-1.5/0.5 for BC1), plus the known-answer pixels, depths, node ids and scene
-stats the reference test asserts."""
+Every scenario of ``src/tests/GfxBatchRendererTest.cpp`` is replayed on the
+oracle and compared with the reference's golden screenshot using the
+reference's thresholds (0/0 for uncompressed textures, 1.5/0.5 for BC1,
+0.75/0.005 for the lit scenes and 95/0.07 after their rotation), plus the
+known-answer pixels, depths, node ids, light ids and scene stats the
+reference test asserts."""
 import numpy as np
 import pytest
 
@@ -20,6 +21,17 @@ def make(tile_size, tile_count, flags):
 def test_golden(case, oracle_lib):
     _, fn, data = S.ALL[case]
     fails = S.evaluate(fn(make, data))
+    assert not fails, fails
+
+
+def make_lit(tile_size, tile_count, flags, max_lights):
+    return OracleRenderer(tile_size, tile_count, flags, max_light_count=max_lights)
+
+
+@pytest.mark.parametrize("case", range(len(S.LIT)), ids=S.lit_ids())
+def test_golden_lights(case, oracle_lib):
+    _, fn, data = S.LIT[case]
+    fails = S.evaluate(fn(make_lit, data))
     assert not fails, fails
 
 
