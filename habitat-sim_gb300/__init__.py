@@ -2,11 +2,11 @@
 ``esp::gfx_batch`` draw path (C ABI in ``include/gbr.h``, CUDA kernels for
 sm_103a in ``csrc/``)."""
 from .gfx_batch import (DrawMode, GbrError, Plane, RendererConfiguration, RendererFileFlags,
-                        RendererFlags, RendererStandalone, RendererStandaloneConfiguration,
-                        RendererStandaloneFlags, SceneStats, calculateDepthUnprojection,
-                        unprojectDepth, unprojectDepthDevice)
+                        RendererFlags, RendererLightType, RendererStandalone,
+                        RendererStandaloneConfiguration, RendererStandaloneFlags, SceneStats,
+                        calculateDepthUnprojection, unprojectDepth, unprojectDepthDevice)
 
 __all__ = ["DrawMode", "GbrError", "Plane", "RendererConfiguration", "RendererFileFlags",
-           "RendererFlags", "RendererStandalone", "RendererStandaloneConfiguration",
-           "RendererStandaloneFlags", "SceneStats", "calculateDepthUnprojection",
-           "unprojectDepth", "unprojectDepthDevice"]
+           "RendererFlags", "RendererLightType", "RendererStandalone",
+           "RendererStandaloneConfiguration", "RendererStandaloneFlags", "SceneStats",
+           "calculateDepthUnprojection", "unprojectDepth", "unprojectDepthDevice"]

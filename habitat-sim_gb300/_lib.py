@@ -20,7 +20,7 @@ class MeshData(ctypes.Structure):
     _fields_ = [("vertex_count", ctypes.c_uint32), ("positions", ctypes.c_void_p),
                 ("colors", ctypes.c_void_p), ("texcoords", ctypes.c_void_p),
                 ("object_ids", ctypes.c_void_p), ("index_count", ctypes.c_uint32),
-                ("indices", ctypes.c_void_p)]
+                ("indices", ctypes.c_void_p), ("normals", ctypes.c_void_p)]
 
 
 class TextureData(ctypes.Structure):
@@ -31,7 +31,8 @@ class TextureData(ctypes.Structure):
 
 class MaterialData(ctypes.Structure):
     _fields_ = [("color", ctypes.c_float * 4), ("texture", ctypes.c_uint32),
-                ("layer", ctypes.c_uint32), ("matrix", ctypes.c_float * 9)]
+                ("layer", ctypes.c_uint32), ("matrix", ctypes.c_float * 9),
+                ("shaded", ctypes.c_int32)]
 
 
 class MeshView(ctypes.Structure):
@@ -79,6 +80,10 @@ PROTOTYPES = {
     "gbr_add_texture": (_ST, [_P, ctypes.POINTER(TextureData), ctypes.POINTER(_U32)]),
     "gbr_add_material": (_ST, [_P, ctypes.POINTER(MaterialData), ctypes.POINTER(_U32)]),
     "gbr_add_node_hierarchy_template": (_ST, [_P, ctypes.c_char_p, _U32, ctypes.POINTER(MeshView)]),
+    "gbr_add_light": (_ST, [_P, _U32, _U64, _U32, ctypes.POINTER(_U64)]),
+    "gbr_clear_lights": (_ST, [_P, _U32]),
+    "gbr_light_colors": (_ST, [_P, _U32, ctypes.POINTER(c_float_p), ctypes.POINTER(_U64)]),
+    "gbr_light_ranges": (_ST, [_P, _U32, ctypes.POINTER(c_float_p), ctypes.POINTER(_U64)]),
     "gbr_set_scene_sources": (_ST, [_P, _U32, _U32, ctypes.POINTER(_U32)]),
     "gbr_set_scene_enabled": (_ST, [_P, _U32, _I32]),
     "gbr_remove_mesh": (_ST, [_P, _U32]),

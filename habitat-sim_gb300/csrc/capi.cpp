@@ -165,6 +165,32 @@ gbr_status gbr_add_node_hierarchy_template(gbr_renderer* r, const char* name, ui
   return guarded([&] { return R(r)->add_template(name, count, views); });
 }
 
+gbr_status gbr_add_light(gbr_renderer* r, uint32_t scene, uint64_t node, uint32_t type,
+                         uint64_t* out) {
+  GBR_HANDLE(r);
+  GBR_ARG(out);
+  return guarded([&] { return R(r)->add_light(scene, node, type, out); });
+}
+
+gbr_status gbr_clear_lights(gbr_renderer* r, uint32_t scene) {
+  GBR_HANDLE(r);
+  return guarded([&] { return R(r)->clear_lights(scene); });
+}
+
+gbr_status gbr_light_colors(gbr_renderer* r, uint32_t scene, float** out, uint64_t* count) {
+  GBR_HANDLE(r);
+  GBR_ARG(out);
+  GBR_ARG(count);
+  return guarded([&] { return R(r)->light_colors(scene, out, count); });
+}
+
+gbr_status gbr_light_ranges(gbr_renderer* r, uint32_t scene, float** out, uint64_t* count) {
+  GBR_HANDLE(r);
+  GBR_ARG(out);
+  GBR_ARG(count);
+  return guarded([&] { return R(r)->light_ranges(scene, out, count); });
+}
+
 gbr_status gbr_set_scene_sources(gbr_renderer* r, uint32_t first, uint32_t count,
                                  const uint32_t* sources) {
   GBR_HANDLE(r);

@@ -784,6 +784,10 @@ bool import_gltf(const std::string& path, bool whole, const std::string& name, b
             m.texcoords[k * 2 + 1] = 1.0f - float(v[k * 2 + 1]);
           }
         }
+        if (const Json* nj = attrs->get("NORMAL")) {
+          if (!doc.accessor(int(nj->num), nc, v) || nc != 3) { error = "bad NORMAL"; return false; }
+          m.normals.assign(v.begin(), v.end());
+        }
         if (const Json* oj = attrs->get("_OBJECT_ID")) {
           if (!doc.accessor(int(oj->num), nc, v) || nc != 1) { error = "bad _OBJECT_ID"; return false; }
           m.object_ids.resize(m.vertex_count);
@@ -833,6 +837,7 @@ bool import_gltf(const std::string& path, bool whole, const std::string& name, b
   if (const Json* mats = doc.j.get("materials"))
     for (size_t i = 0; i < mats->size(); ++i) {
       ImportedMaterial m;
+      if (const Json* ex = (*mats)[i].get("extensions")) m.flat = ex->get("KHR_materials_unlit") != nullptr;
       const Json* pbr = (*mats)[i].get("pbrMetallicRoughness");
       if (pbr) {
         if (const Json* bc = pbr->get("baseColorFactor"))

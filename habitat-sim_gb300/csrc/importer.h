@@ -18,6 +18,7 @@ struct ImportedMesh {
   std::vector<float> colors;      // 4 per vertex, empty if absent
   std::vector<float> texcoords;   // 2 per vertex (Y-up), empty if absent
   std::vector<uint32_t> object_ids;
+  std::vector<float> normals;     // 3 per vertex, empty if absent
   std::vector<uint32_t> indices;  // triangle list
   uint32_t vertex_count = 0;
 };
@@ -27,6 +28,7 @@ struct ImportedMaterial {
   int texture = -1;  // file-local texture id, -1 = none
   int layer = 0;
   float matrix[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  bool flat = false;  // KHR_materials_unlit
 };
 
 struct ImportedView {

@@ -132,6 +132,52 @@ __device__ __forceinline__ bool inside_frustum(const float* mvp, float x, float 
 }
 
 // ================================================================ prepare
+// Absolute transform of a scene-local node: L_root * ... * L_node (parents
+// precede children), the order of the reference's transform pass
+// (Renderer.cpp:1214-1220).  False (and a status bit) for a bad node or a
+// chain deeper than kMaxHierarchyDepth.
+__device__ bool node_transform(const PrepareParams& p, const SceneRec& sc, int32_t node, float a[16]) {
+  uint32_t chain[kMaxHierarchyDepth];
+  int depth = 0;
+  int32_t n = node;
+  bool ok = n >= 0 && uint32_t(n) < sc.node_count;
+  while (ok && n >= 0 && depth < kMaxHierarchyDepth) {
+    chain[depth++] = uint32_t(n);
+    n = p.parents[sc.node_base + n];
+    if (n >= 0 && uint32_t(n) >= sc.node_count) ok = false;
+  }
+  if (!ok) {
+    atomicOr(p.status, kStatusBadNode);
+    return false;
+  }
+  if (n >= 0) {
+    atomicOr(p.status, kStatusHierarchyTooDeep);
+    return false;
+  }
+  const float* l = p.local + size_t(sc.node_base + chain[depth - 1]) * 16;
+  for (int i = 0; i < 16; ++i) a[i] = l[i];
+  for (int k = depth - 2; k >= 0; --k) {
+    const float* lk = p.local + size_t(sc.node_base + chain[k]) * 16;
+    float b[16], t[16];
+    for (int i = 0; i < 16; ++i) b[i] = lk[i];
+    matmul(a, b, t);
+    for (int i = 0; i < 16; ++i) a[i] = t[i];
+  }
+  return true;
+}
+
+// Normal matrix: the cofactor of the upper-left 3x3 (columns c1 x c2,
+// c2 x c0, c0 x c1), column-major, each entry a difference of two products.
+__device__ __forceinline__ void normal_matrix(const float a[16], float nm[9]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float* u = a + 4 * ((k + 1) % 3);
+    const float* v = a + 4 * ((k + 2) % 3);
+    nm[k * 3 + 0] = __fsub_rn(__fmul_rn(u[1], v[2]), __fmul_rn(u[2], v[1]));
+    nm[k * 3 + 1] = __fsub_rn(__fmul_rn(u[2], v[0]), __fmul_rn(u[0], v[2]));
+    nm[k * 3 + 2] = __fsub_rn(__fmul_rn(u[0], v[1]), __fmul_rn(u[1], v[0]));
+  }
+}
 // Scenes with at most this many visible draws get a nearest-first
 // processing order; larger ones keep the draw order.
 constexpr uint32_t kSortCap = 2048;
@@ -166,6 +212,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
     uint32_t vis = 0, tris = 0, clusters = 0;
     float far = 0.0f;  // distance of the bounding box's farthest corner along the view axis
     VisibleRec rec;
+    ModelRec model;
     if (j < sc.draw_count) {
       const DrawRec d = p.draws[sc.draw_base + j];
       // Absolute transform: abs = L_root * ... * L_node (parents precede children).
@@ -198,6 +245,14 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
           for (int i = 0; i < 16; ++i) a[i] = t[i];
         }
         matmul(pv, a, rec.mvp);
+        if (p.model) {
+#pragma unroll
+          for (int col = 0; col < 4; ++col)
+#pragma unroll
+            for (int row = 0; row < 3; ++row) model.a[col * 3 + row] = a[col * 4 + row];
+          normal_matrix(a, model.nm);
+          model.pad[0] = model.pad[1] = model.pad[2] = 0.0f;
+        }
 #pragma unroll
         for (int col = 0; col < 4; ++col) {
           float z = __fmul_rn(vrow[0], a[col * 4 + 0]);
@@ -249,6 +304,7 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
       rec.ordinal = s_tris + to;
       rec.cluster = s_clusters + co;
       p.visible[vis_base + s_count + vo] = rec;
+      if (p.model) p.model[vis_base + s_count + vo] = model;
       if (s_count + vo < kSortCap) s_key[s_count + vo] = far == far ? far : INFINITY;
     }
     __syncthreads();
@@ -263,6 +319,35 @@ __global__ void __launch_bounds__(T) prepare_kernel(const PrepareParams p) {
     p.vis_count[s] = s_count;
     p.vis_tris[s] = s_tris;
     p.vis_clusters[s] = s_clusters;
+  }
+  // Lights of the source scene in world space (Renderer.cpp:1263-1289): a
+  // point light at its node's translation, a directional light towards the
+  // node's negative backward axis.
+  if (p.lights) {
+    const uint32_t nl = min(p.cameras[cam.source].light_count, p.max_lights);
+    for (uint32_t j = threadIdx.x; j < nl; j += T) {
+      const LightSrc src = p.light_src[size_t(cam.source) * p.max_lights + j];
+      float a[16];
+      WorldLight w{};
+      if (node_transform(p, sc, src.node, a)) {
+        if (src.type == 0) {
+          w.pos[0] = -a[8];
+          w.pos[1] = -a[9];
+          w.pos[2] = -a[10];
+          w.pos[3] = 0.0f;
+        } else {
+          w.pos[0] = a[12];
+          w.pos[1] = a[13];
+          w.pos[2] = a[14];
+          w.pos[3] = 1.0f;
+        }
+      }
+      w.color[0] = src.color[0];
+      w.color[1] = src.color[1];
+      w.color[2] = src.color[2];
+      w.range = src.range;
+      p.lights[size_t(s) * p.max_lights + j] = w;
+    }
   }
 
   // Processing order: visible draws by the distance of their farthest
@@ -628,10 +713,87 @@ __device__ __forceinline__ uint32_t unorm8(float c) {
   return __float2uint_rz(t);
 }
 
+// Lit colour (Phong without a specular term, the reference's shader
+// configuration): ambient + sum over lights of diffuse * light colour *
+// max(0, N.L) * attenuation, attenuation = clamp(1 - (d / range)^4, 0, 1)^2
+// / (1 + d^2), d = distance to a point light (0 for directional lights);
+// N = the normalised interpolation of the vertices' normal-matrix normals,
+// the fragment's world position the interpolation of theirs.  Alpha is the
+// diffuse alpha.
+__device__ __noinline__ uint32_t lit_color(const RasterParams& p, const MaterialRec& mat,
+                                           const float tc[4], const float vc[4],
+                                           const WorldLight* lights, uint32_t nl,
+                                           const ModelRec* model, const uint32_t v[3],
+                                           const float4 q[3], float b0, float b1, float b2,
+                                           bool normals) {
+#define GBR_INTERP(a0, a1, a2) fma_(b2, (a2), fma_(b1, (a1), __fmul_rn(b0, (a0))))
+  float amb[4], dif[4], rgb[3];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    amb[c] = __fmul_rn(__fmul_rn(__fmul_rn(mat.color[c], p.ambient_factor), tc[c]), vc[c]);
+    dif[c] = __fmul_rn(__fmul_rn(mat.color[c], tc[c]), vc[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) rgb[c] = amb[c];
+  if (nl > 0 && normals) {
+    float A[12], NM[9];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) A[i] = __ldg(&model->a[i]);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) NM[i] = __ldg(&model->nm[i]);
+    float wp[3][3], wn[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float4 n = __ldg(&p.normals[v[k]]);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        float t = A[9 + r];
+        t = fma_(A[r], q[k].x, t);
+        t = fma_(A[3 + r], q[k].y, t);
+        t = fma_(A[6 + r], q[k].z, t);
+        wp[k][r] = t;
+        wn[k][r] = fma_(NM[6 + r], n.z, fma_(NM[3 + r], n.y, __fmul_rn(NM[r], n.x)));
+      }
+    }
+    float P[3], N[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      P[r] = GBR_INTERP(wp[0][r], wp[1][r], wp[2][r]);
+      N[r] = GBR_INTERP(wn[0][r], wn[1][r], wn[2][r]);
+    }
+    const float len2 = fma_(N[2], N[2], fma_(N[1], N[1], __fmul_rn(N[0], N[0])));
+    const float inv = __frcp_rn(__fsqrt_rn(len2));
+    const float n0 = __fmul_rn(N[0], inv), n1 = __fmul_rn(N[1], inv), n2 = __fmul_rn(N[2], inv);
+    for (uint32_t j = 0; j < nl; ++j) {
+      const WorldLight L = lights[j];
+      const float l0 = __fsub_rn(L.pos[0], __fmul_rn(P[0], L.pos[3]));
+      const float l1 = __fsub_rn(L.pos[1], __fmul_rn(P[1], L.pos[3]));
+      const float l2 = __fsub_rn(L.pos[2], __fmul_rn(P[2], L.pos[3]));
+      const float d2 = fma_(l2, l2, fma_(l1, l1, __fmul_rn(l0, l0)));
+      const float len = __fsqrt_rn(d2);
+      if (!(len > 0.0f)) continue;
+      const float dist = __fmul_rn(len, L.pos[3]);
+      const float qd = __fdiv_rn(dist, fmaxf(L.range, 0.0001f));
+      const float q2 = __fmul_rn(qd, qd);
+      float a = __fsub_rn(1.0f, __fmul_rn(q2, q2));
+      a = a < 0.0f ? 0.0f : (a > 1.0f ? 1.0f : a);
+      const float att = __fdiv_rn(__fmul_rn(a, a), __fadd_rn(1.0f, __fmul_rn(dist, dist)));
+      const float il = __frcp_rn(len);
+      const float ndl = fma_(n2, __fmul_rn(l2, il),
+                             fma_(n1, __fmul_rn(l1, il), __fmul_rn(n0, __fmul_rn(l0, il))));
+      const float intensity = __fmul_rn(ndl > 0.0f ? ndl : 0.0f, att);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) rgb[c] = fma_(__fmul_rn(dif[c], L.color[c]), intensity, rgb[c]);
+    }
+  }
+#undef GBR_INTERP
+  return unorm8(rgb[0]) | (unorm8(rgb[1]) << 8) | (unorm8(rgb[2]) << 16) | (unorm8(dif[3]) << 24);
+}
+
 // Shade the winning triangle `t` of visible draw `rec` at pixel (px, py).
 __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec, uint32_t t,
-                      int px, int py, const float* unorm, uint32_t& color, float& lin,
-                      uint32_t& sid) {
+                      int px, int py, const float* unorm, const WorldLight* lights, uint32_t nl,
+                      const ModelRec* model, uint32_t& color, float& lin, uint32_t& sid) {
   // The record in 16-byte loads: mvp, zrow, (vertex_base, first_index,
   // tri_count, material), (semantic_id, ordinal, flags, chunk).
   const float4* r4 = reinterpret_cast<const float4*>(rec);
@@ -655,18 +817,18 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
   const uint32_t vb = u5.x;
   const uint32_t fi = u5.y + 3u * t;
   uint32_t v[3];
-  float4 c[3];
+  float4 c[3], q[3];
   float d[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     v[k] = vb + __ldg(&p.indices[fi + k]);
-    const float4 q = __ldg(&p.pos[v[k]]);
-    c[k] = make_float4(mrow(mvp, 0, q.x, q.y, q.z), mrow(mvp, 1, q.x, q.y, q.z),
-                       mrow(mvp, 2, q.x, q.y, q.z), mrow(mvp, 3, q.x, q.y, q.z));
+    q[k] = __ldg(&p.pos[v[k]]);
+    c[k] = make_float4(mrow(mvp, 0, q[k].x, q[k].y, q[k].z), mrow(mvp, 1, q[k].x, q[k].y, q[k].z),
+                       mrow(mvp, 2, q[k].x, q[k].y, q[k].z), mrow(mvp, 3, q[k].x, q[k].y, q[k].z));
     float ze = zr[3];
-    ze = fma_(zr[0], q.x, ze);
-    ze = fma_(zr[1], q.y, ze);
-    ze = fma_(zr[2], q.z, ze);
+    ze = fma_(zr[0], q[k].x, ze);
+    ze = fma_(zr[1], q[k].y, ze);
+    ze = fma_(zr[2], q[k].z, ze);
     d[k] = -ze;
   }
   const float sx = __fdiv_rn(float(2 * px + 1 - W), float(W));
@@ -715,13 +877,18 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
     sample(p.textures[tex], p.texels, mat.layer, ts, tt, unorm, tc);
   }
 #undef GBR_INTERP
-  uint32_t packed = 0;
+  if (p.max_lights > 0 && mat.phong) {
+    color = lit_color(p, mat, tc, vc, lights, nl, model, v, q, b0, b1, b2,
+                      (flags & kMeshNormals) != 0u);
+  } else {
+    uint32_t packed = 0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const float val = __fmul_rn(__fmul_rn(mat.color[k], tc[k]), vc[k]);
-    packed |= unorm8(val) << (8 * k);
+    for (int k = 0; k < 4; ++k) {
+      const float val = __fmul_rn(__fmul_rn(mat.color[k], tc[k]), vc[k]);
+      packed |= unorm8(val) << (8 * k);
+    }
+    color = packed;
   }
-  color = packed;
   sid = (flags & kMeshObjectId) ? __float_as_uint(__ldg(&p.pos[v[2]]).w) : u6.x;
 }
 
@@ -1087,6 +1254,9 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
     __syncthreads();
 
     // Resolve + shade + write the planes.
+    const uint32_t nlights =
+        p.lights ? min(p.cameras[p.cameras[wi.scene].source].light_count, p.max_lights) : 0u;
+    const WorldLight* lights = p.lights ? p.lights + size_t(wi.scene) * p.max_lights : nullptr;
     for (int i = threadIdx.x; i < npx; i += T) {
       const int px = c.rx0 + i % c.rw, py = c.ry0 + i / c.rw;
       const uint64_t key = keys[i];
@@ -1097,8 +1267,8 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
         const uint32_t ord = uint32_t(key);
         dep = __uint_as_float(uint32_t(key >> 32));
         const uint32_t di = find_draw(prefix, vis, cached, nvis, ord);
-        shade(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, s_unorm, col, lin,
-              sid);
+        shade(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, s_unorm, lights,
+              nlights, p.model ? p.model + vis_base + di : nullptr, col, lin, sid);
       }
       if (p.out.color) p.out.color[o] = col;
       if (p.out.depth) p.out.depth[o] = dep;

@@ -35,6 +35,10 @@ struct PrepareParams {
   uint32_t* vis_clusters;
   uint32_t* status;
   uint32_t scene_base;
+  const LightSrc* light_src;  // [scene][max_lights] (lit renderers)
+  WorldLight* lights;         // [scene][max_lights] (lit renderers)
+  ModelRec* model;            // per visible draw (lit renderers, else null)
+  uint32_t max_lights;
 };
 
 // Raster: per work item (scene, region), warps take 32-triangle chunks,
@@ -69,6 +73,12 @@ struct RasterParams {
   int32_t prefix_cap;  // visible draws whose ordinals are cached in shared memory
   int32_t small_area;  // boxes up to this many pixels are rasterised by one lane
   int32_t occlusion;   // skip chunks hidden behind the depths written so far
+  // Lighting (max_lights > 0): lights per scene, per-draw model data, normals.
+  const WorldLight* lights;
+  const ModelRec* model;
+  const float4* normals;
+  uint32_t max_lights;
+  float ambient_factor;
 };
 
 cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStream_t stream);

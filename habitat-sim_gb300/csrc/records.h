@@ -2,15 +2,18 @@
 //
 // HBM layout (all arrays renderer-owned, 256-byte aligned allocations):
 //   geometry   pos[v]    float4 (x, y, z, object-id bits)   16 B / vertex
+//              normal[v] float4 (lit renderers only)        16 B / vertex
 //              color[v]  float4 RGBA                        16 B / vertex
 //              uv[v]     float2                              8 B / vertex
 //              index[i]  uint32                              4 B / index
 //   textures   texel[t]  uint32 RGBA8, layer-major, row 0 bottom
 //   tables     MeshRec, MaterialRec, TextureRec
 //   scenes     SceneRec[s]; per node parent (int32) + local 4x4 (64 B);
-//              DrawRec[] (64 B) in draw-batch order; CameraRec[s] (96 B)
+//              DrawRec[] (64 B) in draw-batch order; CameraRec[s] (96 B) followed
+//              by LightSrc[s][max lights] (24 B); WorldLight[s][max lights] (32 B)
 //   per step   VisibleRec[] (128 B, written by the prepare kernel) and its
-//              processing order uint2[] (8 B per visible draw),
+//              processing order uint2[] (8 B per visible draw); ModelRec[]
+//              (96 B per visible draw, lit renderers only),
 //              vis_count[s], vis_tris[s], vis_chunks[s]; WorkItem[] + one counter
 //   views      ChunkBox[] (32 B per 32 triangles of every mesh view, then
 //              32 B per 1024 triangles: the cluster boxes)
@@ -22,7 +25,12 @@
 
 namespace gbr {
 
-enum : uint32_t { kMeshVertexColor = 1u, kMeshObjectId = 2u, kMeshTexcoords = 4u };
+enum : uint32_t {
+  kMeshVertexColor = 1u,
+  kMeshObjectId = 2u,
+  kMeshTexcoords = 4u,
+  kMeshNormals = 8u,  // normals stored (lighting enabled)
+};
 // VisibleRec::flags bit: the draw's bounding box lies inside the frustum.
 constexpr uint32_t kDrawInsideFrustum = 0x100u;
 
@@ -40,7 +48,7 @@ struct MaterialRec {
   int32_t texture;  // 0 = white
   int32_t layer;
   float m[9];       // 3x3 column-major texture matrix
-  int32_t pad;
+  int32_t phong;    // lit: ambient = color * ambient factor, diffuse = color
 };
 
 struct TextureRec {
@@ -80,9 +88,37 @@ struct CameraRec {
   uint32_t source;    // scene whose nodes and draws are rendered
   uint32_t vis_base;  // first visible record of this scene
   uint32_t enabled;   // 0: not drawn, framebuffer rectangle untouched
-  uint32_t pad;
+  uint32_t light_count;  // this scene's lights in use (at most the maximum)
 };
 static_assert(sizeof(CameraRec) == 96, "CameraRec layout");
+
+// A light as the host keeps it (uploaded with the camera block): node of
+// the scene it follows, type (0 directional, 1 point), colour, range.
+struct LightSrc {
+  int32_t node;
+  int32_t type;
+  float color[3];
+  float range;
+};
+static_assert(sizeof(LightSrc) == 24, "LightSrc layout");
+
+// A light in world space, written by the prepare kernel: position (w = 1)
+// or direction towards the light (w = 0), colour, range.
+struct WorldLight {
+  float pos[4];
+  float color[3];
+  float range;
+};
+
+// Per visible draw of a lit renderer: the draw's absolute transform (rows
+// 0-2 of columns 0-3) and its normal matrix (cofactor of the upper-left
+// 3x3, column-major).
+struct ModelRec {
+  float a[12];   // a[col * 3 + row]
+  float nm[9];   // nm[col * 3 + row]
+  float pad[3];
+};
+static_assert(sizeof(ModelRec) == 96, "ModelRec layout");
 
 // 16-byte aligned: the raster kernel reads the matrix with float4 loads.
 struct alignas(16) VisibleRec {

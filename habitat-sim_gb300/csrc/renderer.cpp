@@ -157,8 +157,8 @@ gbr_status Renderer::check_scene(uint32_t scene, const char* fn) const {
 
 // -------------------------------------------------------------- create
 Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
-  if (cfg.max_light_count != 0) {
-    err = "max_light_count > 0 (Phong lighting) is not supported; flat shading only";
+  if (cfg.max_light_count > 64) {
+    err = "max_light_count above 64 is not supported";
     return nullptr;
   }
   if (cfg.scene_count == 0 &&
@@ -173,6 +173,7 @@ Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
   }
   std::unique_ptr<Renderer> r(new Renderer());
   r->cfg_ = cfg;
+  r->max_lights_ = cfg.max_light_count;
   if (r->cfg_.planes == 0) r->cfg_.planes = GBR_PLANE_ALL;
   r->device_ = cfg.cuda_device;
   cudaError_t e = cudaSetDevice(r->device_);
@@ -317,6 +318,18 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
            "addMesh upload");
   GBR_CUDA(cudaMemcpy(d_uv_.as<char>() + vb * 8, uv.data(), nv * 8, cudaMemcpyHostToDevice),
            "addMesh upload");
+  const bool normals = max_lights_ > 0 && m.normals;
+  if (normals) {
+    if (!d_normal_.reserve(ve * 16, true)) {
+      undo();
+      return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of device memory");
+    }
+    std::vector<float> nrm(nv * 4, 0.0f);
+    for (size_t v = 0; v < nv; ++v)
+      for (int c = 0; c < 3; ++c) nrm[v * 4 + c] = m.normals[v * 3 + c];
+    GBR_CUDA(cudaMemcpy(d_normal_.as<char>() + vb * 16, nrm.data(), nv * 16, cudaMemcpyHostToDevice),
+             "addMesh upload");
+  }
   if (m.index_count)
     GBR_CUDA(cudaMemcpy(d_indices_.as<char>() + size_t(ib) * 4, m.indices,
                         size_t(m.index_count) * 4, cudaMemcpyHostToDevice),
@@ -327,7 +340,7 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
   rec.index_base = uint32_t(ib);
   rec.index_count = m.index_count;
   rec.flags = (m.colors ? kMeshVertexColor : 0u) | (m.object_ids ? kMeshObjectId : 0u) |
-              (m.texcoords ? kMeshTexcoords : 0u);
+              (m.texcoords ? kMeshTexcoords : 0u) | (normals ? kMeshNormals : 0u);
   meshes_.push_back(rec);
   mesh_live_.push_back(true);
   if (host_pos_.size() < ve * 3) host_pos_.resize(ve * 3);
@@ -376,6 +389,9 @@ gbr_status Renderer::add_material(const gbr_material_data& m, uint32_t* id) {
   rec.texture = int32_t(m.texture);
   rec.layer = int32_t(m.layer);
   std::memcpy(rec.m, m.matrix, 36);
+  // Lit only when lights are enabled (Renderer.cpp:579-620: every material is
+  // flat otherwise).
+  rec.phong = (m.shaded && max_lights_ > 0) ? 1 : 0;
   materials_.push_back(rec);
   tables_dirty_ = true;
   graph_valid_ = false;
@@ -498,7 +514,8 @@ gbr_status Renderer::add_file(const char* filename, uint32_t flags, const char* 
                      m.texcoords.empty() ? nullptr : m.texcoords.data(),
                      m.object_ids.empty() ? nullptr : m.object_ids.data(),
                      uint32_t(m.indices.size()),
-                     m.indices.data()};
+                     m.indices.data(),
+                     m.normals.empty() ? nullptr : m.normals.data()};
     uint32_t id;
     gbr_status s = add_mesh(md, &id);
     if (s != GBR_OK) return s;
@@ -506,6 +523,7 @@ gbr_status Renderer::add_file(const char* filename, uint32_t flags, const char* 
   for (auto& m : f.materials) {
     gbr_material_data md{};
     std::memcpy(md.color, m.color, 16);
+    md.shaded = m.flat ? 0 : 1;
     if (m.texture < 0) {
       md.texture = 0;
       md.layer = 0;
@@ -600,8 +618,59 @@ gbr_status Renderer::clear(uint32_t scene) {
   sc.transforms.clear();
   sc.draws.clear();
   sc.batches.clear();
+  sc.light_nodes.clear();
+  sc.light_types.clear();
+  sc.light_colors.clear();
+  sc.light_ranges.clear();
   structure_dirty_ = true;
   return GBR_OK;
+}
+
+gbr_status Renderer::add_light(uint32_t scene, uint64_t node, uint32_t type, uint64_t* id) {
+  if (max_lights_ == 0) return fail(GBR_ERROR_STATE, "Renderer::addLight(): max light count is zero");
+  if (gbr_status s = check_scene(scene, "Renderer::addLight()")) return s;
+  SceneState& sc = scenes_[scene];
+  if (node >= sc.parents.size())
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "Renderer::addLight(): index " + std::to_string(node) +
+                                                " out of range for " +
+                                                std::to_string(sc.parents.size()) + " nodes");
+  if (type > 1) return fail(GBR_ERROR_INVALID_ARGUMENT, "Renderer::addLight(): bad light type");
+  *id = sc.light_nodes.size();
+  sc.light_nodes.push_back(int32_t(node));
+  sc.light_types.push_back(int32_t(type));
+  sc.light_colors.insert(sc.light_colors.end(), {1.0f, 1.0f, 1.0f});
+  sc.light_ranges.push_back(INFINITY);
+  return GBR_OK;
+}
+
+gbr_status Renderer::clear_lights(uint32_t scene) {
+  if (gbr_status s = check_scene(scene, "Renderer::clearLights()")) return s;
+  SceneState& sc = scenes_[scene];
+  sc.light_nodes.clear();
+  sc.light_types.clear();
+  sc.light_colors.clear();
+  sc.light_ranges.clear();
+  return GBR_OK;
+}
+
+gbr_status Renderer::light_colors(uint32_t scene, float** out, uint64_t* count) {
+  if (gbr_status s = check_scene(scene, "Renderer::lightColors()")) return s;
+  SceneState& sc = scenes_[scene];
+  *out = sc.light_colors.empty() ? nullptr : sc.light_colors.data();
+  *count = sc.light_nodes.size();
+  return GBR_OK;
+}
+
+gbr_status Renderer::light_ranges(uint32_t scene, float** out, uint64_t* count) {
+  if (gbr_status s = check_scene(scene, "Renderer::lightRanges()")) return s;
+  SceneState& sc = scenes_[scene];
+  *out = sc.light_ranges.empty() ? nullptr : sc.light_ranges.data();
+  *count = sc.light_nodes.size();
+  return GBR_OK;
+}
+
+size_t Renderer::camera_block_bytes() const {
+  return scenes_.size() * (kCameraBytes + size_t(max_lights_) * sizeof(LightSrc));
 }
 
 gbr_status Renderer::set_semantic_id(uint32_t scene, uint64_t node, uint32_t id) {
@@ -878,7 +947,8 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
       !d_parents_.reserve(std::max<size_t>(nodes, 1) * 4, false) ||
       !d_local_.reserve(std::max<size_t>(nodes, 1) * 64, false) ||
       !d_draws_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(DrawRec), false) ||
-      !d_cameras_.reserve(S1 * kCameraBytes, false) ||
+      !d_cameras_.reserve(std::max<size_t>(camera_block_bytes(), 1), false) ||
+      !d_lights_.reserve(std::max<size_t>(size_t(S) * max_lights_ * sizeof(WorldLight), 16), false) ||
       !d_visible_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(VisibleRec), false) ||
       !d_order_.reserve(std::max<size_t>(draws.size(), 1) * sizeof(uint2), false) ||
       !d_vis_count_.reserve(S1 * 4, false) || !d_vis_tris_.reserve(S1 * 4, false) ||
@@ -886,7 +956,7 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
       !d_status_.reserve(4, false) || !d_counter_.reserve(4, false) ||
       !d_items_.reserve(std::max<size_t>(items.size(), 1) * sizeof(WorkItem), false) ||
       !d_items_lpt_.reserve(std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem), false) ||
-      !h_stage_.reserve(S1 * kCameraBytes + std::max<size_t>(nodes, 1) * 64 +
+      !h_stage_.reserve(std::max<size_t>(camera_block_bytes(), 1) + std::max<size_t>(nodes, 1) * 64 +
                         std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem)))
     return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of memory for scene data");
   GBR_CUDA(cudaMemcpy(d_scenes_.ptr, recs.data(), S * sizeof(SceneRec), cudaMemcpyHostToDevice),
@@ -966,10 +1036,14 @@ gbr_status Renderer::upload_step(cudaStream_t stream) {
     vis_needed_ = base;
     void* before = d_visible_.ptr;
     void* before_order = d_order_.ptr;
+    void* before_model = d_model_.ptr;
     if (!d_visible_.reserve(std::max<uint64_t>(base, 1) * sizeof(VisibleRec), false) ||
-        !d_order_.reserve(std::max<uint64_t>(base, 1) * sizeof(uint2), false))
+        !d_order_.reserve(std::max<uint64_t>(base, 1) * sizeof(uint2), false) ||
+        (max_lights_ > 0 &&
+         !d_model_.reserve(std::max<uint64_t>(base, 1) * sizeof(ModelRec), false)))
       return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of device memory for visible draws");
-    if (d_visible_.ptr != before || d_order_.ptr != before_order) graph_valid_ = false;
+    if (d_visible_.ptr != before || d_order_.ptr != before_order || d_model_.ptr != before_model)
+      graph_valid_ = false;
     order_items();
     bindings_dirty_ = false;
   }
@@ -981,16 +1055,35 @@ gbr_status Renderer::upload_step(cudaStream_t stream) {
     cams[s].source = sc.source;
     cams[s].vis_base = sc.vis_base;
     cams[s].enabled = sc.enabled ? 1u : 0u;
-    cams[s].pad = 0;
+    cams[s].light_count = uint32_t(std::min<size_t>(sc.light_nodes.size(), max_lights_));
+  }
+  if (max_lights_ > 0) {
+    // Light sources (colours and ranges are host-writable views): re-staged
+    // every step after the cameras, uploaded with them.
+    LightSrc* ls = reinterpret_cast<LightSrc*>(stage + S * kCameraBytes);
+    for (uint32_t s = 0; s < S; ++s) {
+      const SceneState& sc = scenes_[s];
+      for (uint32_t j = 0; j < max_lights_; ++j) {
+        LightSrc& d = ls[size_t(s) * max_lights_ + j];
+        if (j < sc.light_nodes.size()) {
+          d.node = sc.light_nodes[j];
+          d.type = sc.light_types[j];
+          for (int c = 0; c < 3; ++c) d.color[c] = sc.light_colors[j * 3 + c];
+          d.range = sc.light_ranges[j];
+        } else {
+          d = LightSrc{};
+        }
+      }
+    }
   }
   if (items_staged_) {
-    WorkItem* istage = reinterpret_cast<WorkItem*>(stage + size_t(S) * kCameraBytes +
+    WorkItem* istage = reinterpret_cast<WorkItem*>(stage + camera_block_bytes() +
                                                    size_t(total_nodes_) * 64);
     GBR_CUDA(cudaMemcpyAsync(d_items_lpt_.ptr, istage, size_t(lpt_count_) * sizeof(WorkItem),
                              cudaMemcpyHostToDevice, stream), "work item upload");
     items_staged_ = false;
   }
-  float* tstage = reinterpret_cast<float*>(stage + size_t(S) * kCameraBytes);
+  float* tstage = reinterpret_cast<float*>(stage + camera_block_bytes());
   // Coalesce runs of dirty scenes into single copies.
   uint32_t s = 0;
   while (s < S) {
@@ -1038,7 +1131,7 @@ void Renderer::order_items() {
     return cost[a] > cost[b];
   });
   WorkItem* istage = reinterpret_cast<WorkItem*>(static_cast<char*>(h_stage_.ptr) +
-                                                 scenes_.size() * kCameraBytes +
+                                                 camera_block_bytes() +
                                                  size_t(total_nodes_) * 64);
   for (size_t i = 0; i < n; ++i) istage[i] = batched_items_[perm[i]];
   items_staged_ = n != 0;
@@ -1055,6 +1148,12 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   pp.meshes = d_meshes_.as<MeshRec>();
   pp.visible = d_visible_.as<VisibleRec>();
   pp.order = d_order_.as<uint2>();
+  pp.max_lights = max_lights_;
+  if (max_lights_ > 0) {
+    pp.light_src = reinterpret_cast<const LightSrc*>(d_cameras_.as<char>() + S * kCameraBytes);
+    pp.lights = d_lights_.as<WorldLight>();
+    pp.model = d_model_.as<ModelRec>();
+  }
   pp.vis_count = d_vis_count_.as<uint32_t>();
   pp.vis_tris = d_vis_tris_.as<uint32_t>();
   pp.vis_clusters = d_vis_clusters_.as<uint32_t>();
@@ -1085,6 +1184,13 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   rp.prefix_cap = prefix_cap_;
   rp.small_area = tuning_.small_area;
   rp.occlusion = tuning_.occlusion_culling;
+  rp.max_lights = max_lights_;
+  rp.ambient_factor = cfg_.ambient_factor;
+  if (max_lights_ > 0) {
+    rp.lights = pp.lights;
+    rp.model = pp.model;
+    rp.normals = d_normal_.as<float4>();
+  }
   uint64_t launches = 0;
   if (mode == GBR_DRAW_BATCHED) {
     pp.scene_base = 0;
@@ -1131,7 +1237,7 @@ gbr_status Renderer::draw(cudaStream_t stream, uint32_t mode, bool use_graph) {
     if (gbr_status s = upload_tables()) return s;
   if (gbr_status s = upload_step(stream)) return s;
   const uint32_t S = uint32_t(scenes_.size());
-  const size_t cam_bytes = size_t(S) * kCameraBytes;
+  const size_t cam_bytes = camera_block_bytes();
   if (mode == GBR_DRAW_BATCHED && use_graph) {
     if (!graph_valid_ || graph_stream_ != stream) {
       if (graph_exec_) {

@@ -82,6 +82,9 @@ struct SceneState {
   uint32_t source = 0;     // scene whose nodes and draws this scene renders
   uint32_t vis_base = 0;   // first visible record (from the current bindings)
   bool enabled = true;
+  // lights (Renderer.cpp:990-1121): node, type, colour (3 floats), range
+  std::vector<int32_t> light_nodes, light_types;
+  std::vector<float> light_colors, light_ranges;
 };
 
 class Renderer {
@@ -119,6 +122,10 @@ class Renderer {
   gbr_status transformations(uint32_t scene, float** out, uint64_t* count);
   gbr_status stats(uint32_t scene, gbr_scene_stats_info* out) const;
   gbr_status set_sources(uint32_t first, uint32_t count, const uint32_t* sources);
+  gbr_status add_light(uint32_t scene, uint64_t node, uint32_t type, uint64_t* id);
+  gbr_status clear_lights(uint32_t scene);
+  gbr_status light_colors(uint32_t scene, float** out, uint64_t* count);
+  gbr_status light_ranges(uint32_t scene, float** out, uint64_t* count);
   gbr_status set_enabled(uint32_t scene, bool enabled);
 
   // -- drawing
@@ -154,6 +161,7 @@ class Renderer {
   void* plane_ptr(uint32_t plane, size_t* elem) const;
   gbr_status sync_and_check();
   gbr_status quiesce();
+  size_t camera_block_bytes() const;  // cameras then light sources, per step
   bool texture_removed(uint32_t t) const { return t < texture_live_.size() && !texture_live_[t]; }
   void order_items();
 
@@ -182,7 +190,9 @@ class Renderer {
   bool structure_dirty_ = true;
 
   // device
-  DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_;
+  DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_, d_normal_;
+  DeviceBuffer d_lights_, d_model_;  // lit renderers: world lights, per-draw model data
+  uint32_t max_lights_ = 0;
   DeviceBuffer d_meshes_, d_materials_, d_textures_, d_boxes_;
   DeviceBuffer d_scenes_, d_parents_, d_local_, d_draws_, d_cameras_;
   DeviceBuffer d_visible_, d_order_, d_vis_count_, d_vis_tris_, d_vis_clusters_, d_status_, d_items_,

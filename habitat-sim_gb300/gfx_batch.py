@@ -48,6 +48,12 @@ class Plane(enum.IntFlag):
     All = 15
 
 
+class RendererLightType(enum.IntEnum):
+    """``RendererLightType`` (Renderer.h:170-173)."""
+    Directional = 0
+    Point = 1
+
+
 class DrawMode(enum.IntEnum):
     PerScene = 0
     Batched = 1
@@ -244,16 +250,19 @@ class RendererStandalone:
         return True
 
     # -------------------------------------------------------- procedural
-    def addMesh(self, positions, colors=None, texcoords=None, objectIds=None, indices=None):
+    def addMesh(self, positions, colors=None, texcoords=None, objectIds=None, indices=None,
+                normals=None):
         pos = _f32(positions, (-1, 3))
         n = len(pos)
         col = None if colors is None else _f32(colors, (n, 4))
         uv = None if texcoords is None else _f32(texcoords, (n, 2))
         ids = None if objectIds is None else np.ascontiguousarray(objectIds, np.uint32).reshape(n)
+        nrm = None if normals is None else _f32(normals, (n, 3))
         idx = np.ascontiguousarray(indices, np.uint32).reshape(-1)
         md = _lib.MeshData(n, pos.ctypes.data, None if col is None else col.ctypes.data,
                            None if uv is None else uv.ctypes.data,
-                           None if ids is None else ids.ctypes.data, len(idx), idx.ctypes.data)
+                           None if ids is None else ids.ctypes.data, len(idx), idx.ctypes.data,
+                           None if nrm is None else nrm.ctypes.data)
         out = ctypes.c_uint32()
         check(self._lib.gbr_add_mesh(self._h, ctypes.byref(md), ctypes.byref(out)))
         return out.value
@@ -269,10 +278,12 @@ class RendererStandalone:
         check(self._lib.gbr_add_texture(self._h, ctypes.byref(td), ctypes.byref(out)))
         return out.value
 
-    def addMaterial(self, color=(1, 1, 1, 1), texture=0, layer=0, matrix=None):
+    def addMaterial(self, color=(1, 1, 1, 1), texture=0, layer=0, matrix=None, shaded=False):
+        """A flat material, or with ``shaded`` a lit one (when the renderer has lights)."""
         m = np.eye(3, dtype=np.float32) if matrix is None else _f32(matrix, (3, 3))
         md = _lib.MaterialData((ctypes.c_float * 4)(*[float(c) for c in color]), int(texture),
-                               int(layer), (ctypes.c_float * 9)(*m.reshape(-1).tolist()))
+                               int(layer), (ctypes.c_float * 9)(*m.reshape(-1).tolist()),
+                               1 if shaded else 0)
         out = ctypes.c_uint32()
         check(self._lib.gbr_add_material(self._h, ctypes.byref(md), ctypes.byref(out)))
         return out.value
@@ -349,6 +360,34 @@ class RendererStandalone:
         s = _lib.SceneStatsInfo()
         check(self._lib.gbr_scene_stats(self._h, sceneId, ctypes.byref(s)))
         return SceneStats(s.node_count, s.draw_count, s.draw_batch_count)
+
+    # ------------------------------------------------------------- lights
+    def addLight(self, sceneId, nodeId, type):
+        """Renderer::addLight: the light follows the node (translation for a
+        point light, negative backward axis for a directional one)."""
+        out = ctypes.c_uint64()
+        check(self._lib.gbr_add_light(self._h, sceneId, int(nodeId), int(type), ctypes.byref(out)))
+        return out.value
+
+    def clearLights(self, sceneId):
+        check(self._lib.gbr_clear_lights(self._h, sceneId))
+
+    def lightColors(self, sceneId):
+        """Writable [lights, 3] view of the scene's light colours; valid until
+        the next add/clear on this scene."""
+        ptr, n = _lib.c_float_p(), ctypes.c_uint64()
+        check(self._lib.gbr_light_colors(self._h, sceneId, ctypes.byref(ptr), ctypes.byref(n)))
+        if n.value == 0:
+            return np.zeros((0, 3), np.float32)
+        return np.ctypeslib.as_array(ptr, shape=(n.value, 3))
+
+    def lightRanges(self, sceneId):
+        """Writable [lights] view of the scene's light ranges."""
+        ptr, n = _lib.c_float_p(), ctypes.c_uint64()
+        check(self._lib.gbr_light_ranges(self._h, sceneId, ctypes.byref(ptr), ctypes.byref(n)))
+        if n.value == 0:
+            return np.zeros(0, np.float32)
+        return np.ctypeslib.as_array(ptr, shape=(n.value,))
 
     # ------------------------------------------- serving extensions (new)
     def setSceneSources(self, sources, first=0):

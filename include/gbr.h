@@ -65,7 +65,8 @@ typedef struct gbr_config {
   uint32_t flags;            /* GBR_FLAG_*                                  */
   int32_t tile_size[2];      /* default {128,128}                           */
   int32_t tile_count[2];     /* default {1,1}                               */
-  uint32_t max_light_count;  /* must be 0 (flat shading); lights not built  */
+  uint32_t max_light_count;  /* lights used per scene; 0 = every material
+                                flat (Renderer.cpp:579-620)                 */
   float ambient_factor;      /* default 0.1, used by lit materials only     */
   int32_t cuda_device;       /* default 0                                   */
   uint32_t standalone_flags; /* GBR_STANDALONE_*                            */
@@ -114,6 +115,8 @@ typedef struct gbr_mesh_data {
   const uint32_t* object_ids; /* 1 per vertex or NULL                       */
   uint32_t index_count;
   const uint32_t* indices;    /* triangle list                              */
+  const float* normals;       /* 3 per vertex or NULL (kept only when
+                                 max_light_count > 0)                       */
 } gbr_mesh_data;
 gbr_status gbr_add_mesh(gbr_renderer* r, const gbr_mesh_data* mesh, uint32_t* out_mesh_id);
 
@@ -131,6 +134,9 @@ typedef struct gbr_material_data {
   uint32_t texture;           /* texture id, 0 = the reserved white texel   */
   uint32_t layer;             /* array layer                                */
   float matrix[9];            /* 3x3 texture matrix, column-major           */
+  int32_t shaded;             /* 1: lit when max_light_count > 0 (ambient =
+                                 colour * ambient_factor, diffuse = colour);
+                                 0: flat (unlit)                            */
 } gbr_material_data;
 gbr_status gbr_add_material(gbr_renderer* r, const gbr_material_data* material,
                             uint32_t* out_material_id);
@@ -185,6 +191,21 @@ gbr_status gbr_draw(gbr_renderer* r, void* stream);
  * step into a CUDA graph and replays it while the scene structure and the
  * stream stay the same. */
 gbr_status gbr_draw_mode(gbr_renderer* r, void* stream, uint32_t mode, int32_t use_graph);
+
+/* Lights: Renderer::addLight / clearLights / lightColors / lightRanges
+ * (Renderer.h:600-720, Renderer.cpp:990-1121).  A light takes the node's
+ * translation (point) or negative backward axis (directional) every draw;
+ * colour defaults to white, range to infinity.  Needs max_light_count > 0;
+ * a scene uses its first max_light_count lights.  The colour (3 floats per
+ * light) and range views are writable and valid until the next
+ * add/clear on that scene. */
+typedef enum gbr_light_type { GBR_LIGHT_DIRECTIONAL = 0, GBR_LIGHT_POINT = 1 } gbr_light_type;
+gbr_status gbr_add_light(gbr_renderer* r, uint32_t scene, uint64_t node, uint32_t type,
+                         uint64_t* out_light_id);
+gbr_status gbr_clear_lights(gbr_renderer* r, uint32_t scene);
+gbr_status gbr_light_colors(gbr_renderer* r, uint32_t scene, float** out_rgb, uint64_t* out_count);
+gbr_status gbr_light_ranges(gbr_renderer* r, uint32_t scene, float** out_ranges,
+                            uint64_t* out_count);
 
 /* Serving and batching extensions (no counterpart in the reference).
  * gbr_set_scene_sources: scene first+i renders the nodes and draws of scene

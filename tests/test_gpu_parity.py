@@ -64,6 +64,47 @@ def test_golden(pkg, case, mode):
             assert np.array_equal(g.image, c.image), g.golden
 
 
+def lit_factory(pkg, mode):
+    def make(tile_size, tile_count, flags, max_lights):
+        cfg = (pkg.RendererConfiguration().setTileSizeCount(tile_size, tile_count)
+               .setFlags(flags).setDrawMode(mode).setMaxLightCount(max_lights))
+        return pkg.RendererStandalone(cfg, pkg.RendererStandaloneConfiguration().setFlags(
+            pkg.RendererStandaloneFlags.QuietLog))
+    return make
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["per_scene", "batched"])
+@pytest.mark.parametrize("case", range(len(S.LIT)), ids=S.lit_ids())
+def test_golden_lights(pkg, case, mode):
+    """GfxBatchRendererTest::lights / clearLights against the reference's
+    golden images at its thresholds, and bit for bit against the oracle."""
+    from oracle.model import OracleRenderer
+    _, fn, data = S.LIT[case]
+    gpu_checks = fn(lit_factory(pkg, mode), data)
+    fails = S.evaluate(gpu_checks)
+    assert not fails, fails
+    oracle_checks = fn(lambda ts, tc, fl, ml: OracleRenderer(ts, tc, fl, max_light_count=ml), data)
+    for g, c in zip(gpu_checks, oracle_checks):
+        if g.kind == "image":
+            assert np.array_equal(g.image, c.image), g.golden
+
+
+def test_lights_errors(pkg):
+    r = lit_factory(pkg, 1)((32, 32), (1, 1), 0, 0)
+    r.addEmptyNode(0)
+    with pytest.raises(pkg.GbrError) as e:
+        r.addLight(0, 0, pkg.RendererLightType.Point)
+    assert e.value.status == 7
+    r = lit_factory(pkg, 1)((32, 32), (1, 1), 0, 2)
+    with pytest.raises(pkg.GbrError) as e:
+        r.addLight(0, 0, pkg.RendererLightType.Point)   # no node 0 yet
+    assert e.value.status == 1
+    r.addEmptyNode(0)
+    assert r.addLight(0, 0, pkg.RendererLightType.Directional) == 0
+    assert r.lightColors(0).shape == (1, 3) and (r.lightColors(0) == 1).all()
+    assert np.isinf(r.lightRanges(0)).all()
+
+
 def test_depth_unprojection_scene(pkg):
     fails = S.evaluate(S.depth_unprojection(gpu_factory(pkg, 1), pkg.unprojectDepth))
     assert not fails, fails
