@@ -322,6 +322,19 @@ gbr_status gbr_image_into(gbr_renderer* r, uint32_t plane, const int32_t rect[4]
   return guarded([&] { return R(r)->image_into(plane, rect, dst, row_bytes); });
 }
 
+gbr_status gbr_image_into_async(gbr_renderer* r, uint32_t plane, const int32_t rect[4], void* dst,
+                                uint64_t row_bytes) {
+  GBR_HANDLE(r);
+  GBR_ARG(rect);
+  GBR_ARG(dst);
+  return guarded([&] { return R(r)->image_into_async(plane, rect, dst, row_bytes); });
+}
+
+gbr_status gbr_readback_wait(gbr_renderer* r) {
+  GBR_HANDLE(r);
+  return guarded([&] { return R(r)->readback_wait(); });
+}
+
 gbr_status gbr_color_image_into(gbr_renderer* r, const int32_t rect[4], void* dst,
                                 uint64_t row_bytes) {
   return gbr_image_into(r, GBR_PLANE_COLOR, rect, dst, row_bytes);

@@ -233,12 +233,14 @@ Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
     std::memcpy(sc.view, kIdentity, 64);
     sc.source = s;
   }
-  for (int i = 0; i < 4; ++i)
-    if (r->cfg_.planes & (1u << i))
-      if (!r->d_planes_[i].reserve(size_t(r->fb_px_) * 4, false)) {
-        err = "out of device memory for the framebuffer";
-        return nullptr;
-      }
+  r->double_buffer_ = (cfg.standalone_flags & GBR_STANDALONE_DOUBLE_BUFFER) != 0;
+  for (int set = 0; set < (r->double_buffer_ ? 2 : 1); ++set)
+    for (int i = 0; i < 4; ++i)
+      if (r->cfg_.planes & (1u << i))
+        if (!r->d_planes_[set][i].reserve(size_t(r->fb_px_) * 4, false)) {
+          err = "out of device memory for the framebuffer";
+          return nullptr;
+        }
   if (cudaEventCreateWithFlags(&r->upload_done_, cudaEventDisableTiming) != cudaSuccess) {
     err = "cudaEventCreate failed";
     return nullptr;
@@ -266,7 +268,12 @@ Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
 Renderer::~Renderer() {
   cudaSetDevice(device_);
   if (last_stream_ || upload_pending_) cudaDeviceSynchronize();
-  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  if (copy_stream_) cudaStreamSynchronize(copy_stream_);
+  for (auto& g : graph_exec_)
+    if (g) cudaGraphExecDestroy(g);
+  for (auto& e : copy_done_)
+    if (e) cudaEventDestroy(e);
+  if (copy_stream_) cudaStreamDestroy(copy_stream_);
   if (upload_done_) cudaEventDestroy(upload_done_);
   if (own_stream_) cudaStreamDestroy(own_stream_);
   for (auto& e : ev_)
@@ -1177,10 +1184,11 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   rp.texture_count = int32_t(textures_.size());
   rp.flags = (cfg_.flags & GBR_FLAG_NO_TEXTURES) ? 1u : 0u;
   rp.counter = d_counter_.as<uint32_t>();
-  rp.out.color = (cfg_.planes & GBR_PLANE_COLOR) ? d_planes_[0].as<uint32_t>() : nullptr;
-  rp.out.depth = (cfg_.planes & GBR_PLANE_DEPTH) ? d_planes_[1].as<float>() : nullptr;
-  rp.out.linear = (cfg_.planes & GBR_PLANE_LINEAR_DEPTH) ? d_planes_[2].as<float>() : nullptr;
-  rp.out.semantic = (cfg_.planes & GBR_PLANE_SEMANTIC) ? d_planes_[3].as<uint32_t>() : nullptr;
+  DeviceBuffer* planes = d_planes_[draw_set_];
+  rp.out.color = (cfg_.planes & GBR_PLANE_COLOR) ? planes[0].as<uint32_t>() : nullptr;
+  rp.out.depth = (cfg_.planes & GBR_PLANE_DEPTH) ? planes[1].as<float>() : nullptr;
+  rp.out.linear = (cfg_.planes & GBR_PLANE_LINEAR_DEPTH) ? planes[2].as<float>() : nullptr;
+  rp.out.semantic = (cfg_.planes & GBR_PLANE_SEMANTIC) ? planes[3].as<uint32_t>() : nullptr;
   rp.prefix_cap = prefix_cap_;
   rp.small_area = tuning_.small_area;
   rp.occlusion = tuning_.occlusion_culling;
@@ -1238,11 +1246,23 @@ gbr_status Renderer::draw(cudaStream_t stream, uint32_t mode, bool use_graph) {
   if (gbr_status s = upload_step(stream)) return s;
   const uint32_t S = uint32_t(scenes_.size());
   const size_t cam_bytes = camera_block_bytes();
+  // The plane set this draw writes; with double buffering, the one the last
+  // draw did not write, once the readbacks of its previous contents are done.
+  const int set = double_buffer_ ? (front_ ^ 1) : 0;
+  draw_set_ = set;
+  if (copy_pending_[set]) {
+    GBR_CUDA(cudaStreamWaitEvent(stream, copy_done_[set], 0), "wait for readback");
+    copy_pending_[set] = false;
+  }
+  if (!graph_valid_) {
+    graph_built_[0] = graph_built_[1] = false;
+    graph_valid_ = true;
+  }
   if (mode == GBR_DRAW_BATCHED && use_graph) {
-    if (!graph_valid_ || graph_stream_ != stream) {
-      if (graph_exec_) {
-        cudaGraphExecDestroy(graph_exec_);
-        graph_exec_ = nullptr;
+    if (!graph_built_[set] || graph_stream_[set] != stream) {
+      if (graph_exec_[set]) {
+        cudaGraphExecDestroy(graph_exec_[set]);
+        graph_exec_[set] = nullptr;
       }
       cudaGraph_t g;
       GBR_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "graph capture");
@@ -1252,13 +1272,13 @@ gbr_status Renderer::draw(cudaStream_t stream, uint32_t mode, bool use_graph) {
       cudaError_t e2 = cudaStreamEndCapture(stream, &g);
       if (st != GBR_OK) return st;
       GBR_CUDA(e2, "graph capture");
-      e = cudaGraphInstantiate(&graph_exec_, g, 0);
+      e = cudaGraphInstantiate(&graph_exec_[set], g, 0);
       cudaGraphDestroy(g);
       GBR_CUDA(e, "graph instantiate");
-      graph_valid_ = true;
-      graph_stream_ = stream;
+      graph_built_[set] = true;
+      graph_stream_[set] = stream;
     }
-    GBR_CUDA(cudaGraphLaunch(graph_exec_, stream), "graph launch");
+    GBR_CUDA(cudaGraphLaunch(graph_exec_[set], stream), "graph launch");
   } else {
     GBR_CUDA(cudaMemcpyAsync(d_cameras_.ptr, h_stage_.ptr, cam_bytes, cudaMemcpyHostToDevice, stream),
              "camera upload");
@@ -1267,6 +1287,7 @@ gbr_status Renderer::draw(cudaStream_t stream, uint32_t mode, bool use_graph) {
   GBR_CUDA(cudaEventRecord(upload_done_, stream), "event record");
   upload_pending_ = true;
   last_stream_ = stream;
+  front_ = set;
   last_stats_.scenes = S;
   last_stats_.draws = total_draws_;
   last_stats_.kernel_launches = launches_;
@@ -1293,7 +1314,42 @@ void* Renderer::plane_ptr(uint32_t plane, size_t* elem) const {
   const int slot = plane_slot(plane);
   if (slot < 0 || !(cfg_.planes & plane)) return nullptr;
   *elem = plane_elem(plane);
-  return d_planes_[slot].ptr;
+  return d_planes_[front_][slot].ptr;
+}
+
+gbr_status Renderer::image_into_async(uint32_t plane, const int32_t* rect, void* dst,
+                                      uint64_t row_bytes) {
+  size_t elem;
+  const char* src = static_cast<const char*>(plane_ptr(plane, &elem));
+  if (!src) return fail(GBR_ERROR_INVALID_ARGUMENT, "imageIntoAsync: plane not enabled");
+  if (!(rect[0] >= 0 && rect[1] >= 0 && rect[2] <= fb_w_ && rect[3] <= fb_h_ && rect[0] <= rect[2] &&
+        rect[1] <= rect[3]))
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "imageIntoAsync: rectangle doesn't fit in the framebuffer");
+  const size_t w = size_t(rect[2] - rect[0]), h = size_t(rect[3] - rect[1]);
+  if (row_bytes < w * elem)
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "imageIntoAsync: row pitch too small");
+  cudaSetDevice(device_);
+  if (!copy_stream_) {
+    GBR_CUDA(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking), "copy stream");
+    for (auto& e : copy_done_)
+      GBR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy event");
+  }
+  if (upload_pending_) GBR_CUDA(cudaStreamWaitEvent(copy_stream_, upload_done_, 0), "wait for draw");
+  if (w && h)
+    GBR_CUDA(cudaMemcpy2DAsync(dst, row_bytes, src + (size_t(rect[1]) * fb_w_ + rect[0]) * elem,
+                               size_t(fb_w_) * elem, w * elem, h, cudaMemcpyDeviceToHost,
+                               copy_stream_),
+             "imageIntoAsync copy");
+  GBR_CUDA(cudaEventRecord(copy_done_[front_], copy_stream_), "copy event");
+  copy_pending_[front_] = true;
+  return GBR_OK;
+}
+
+gbr_status Renderer::readback_wait() {
+  if (!copy_stream_) return GBR_OK;
+  cudaSetDevice(device_);
+  GBR_CUDA(cudaStreamSynchronize(copy_stream_), "readback wait");
+  return GBR_OK;
 }
 
 gbr_status Renderer::image_into(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes) {

@@ -131,6 +131,8 @@ class Renderer {
   // -- drawing
   gbr_status draw(cudaStream_t stream, uint32_t mode, bool use_graph);
   gbr_status image_into(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes);
+  gbr_status image_into_async(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes);
+  gbr_status readback_wait();
   gbr_status scene_image_into(uint32_t plane, uint32_t scene, void* dst, uint64_t row_bytes);
   gbr_status plane_pointer(uint32_t plane, void** out, uint64_t* bytes);
   gbr_status plane_dlpack(uint32_t plane, void** out);
@@ -197,7 +199,13 @@ class Renderer {
   DeviceBuffer d_scenes_, d_parents_, d_local_, d_draws_, d_cameras_;
   DeviceBuffer d_visible_, d_order_, d_vis_count_, d_vis_tris_, d_vis_clusters_, d_status_, d_items_,
       d_items_lpt_, d_counter_;
-  DeviceBuffer d_planes_[4];
+  DeviceBuffer d_planes_[2][4];  // output planes; two sets when double-buffered
+  bool double_buffer_ = false;
+  int front_ = 0;                // set written by the last draw
+  int draw_set_ = 0;             // set the draw being enqueued writes
+  cudaStream_t copy_stream_ = nullptr;
+  cudaEvent_t copy_done_[2] = {nullptr, nullptr};
+  bool copy_pending_[2] = {false, false};
   PinnedBuffer h_stage_;
   cudaEvent_t upload_done_ = nullptr;
   bool upload_pending_ = false;
@@ -219,10 +227,11 @@ class Renderer {
   bool raster_configured_ = false;
   int ctas_per_sm_ = 1;
 
-  // CUDA graph of the batched step
-  cudaGraphExec_t graph_exec_ = nullptr;
-  cudaStream_t graph_stream_ = nullptr;
-  bool graph_valid_ = false;
+  // CUDA graphs of the batched step, one per plane set
+  cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
+  cudaStream_t graph_stream_[2] = {nullptr, nullptr};
+  bool graph_built_[2] = {false, false};
+  bool graph_valid_ = false;  // false: every graph must be re-captured
 
   gbr_draw_stats last_stats_{};
   bool timing_ = false;

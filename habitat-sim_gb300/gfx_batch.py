@@ -36,8 +36,11 @@ class RendererFileFlags(enum.IntFlag):
 
 
 class RendererStandaloneFlags(enum.IntFlag):
-    """``RendererStandaloneFlag`` (RendererStandalone.h:21-36)."""
+    """``RendererStandaloneFlag`` (RendererStandalone.h:21-36), plus
+    ``DoubleBuffer``: two sets of output planes, alternated by the draws, so
+    that an asynchronous readback of one draw overlaps the next draw."""
     QuietLog = 1
+    DoubleBuffer = 2
 
 
 class Plane(enum.IntFlag):
@@ -476,7 +479,7 @@ class RendererStandalone:
     def semanticImage(self):
         return self._image(Plane.Semantic, np.uint32)
 
-    def _image_into(self, plane, rectangle, image):
+    def _image_into(self, plane, rectangle, image, asynchronous=False):
         (x0, y0), (x1, y1) = rectangle
         if image.shape[0] != y1 - y0 or image.shape[1] != x1 - x0:
             raise GbrError(1, f"expected image size of {(x1 - x0, y1 - y0)} pixels but got "
@@ -484,8 +487,17 @@ class RendererStandalone:
         if not image.flags.c_contiguous:
             raise GbrError(1, "image must be C-contiguous")
         rect = (ctypes.c_int32 * 4)(x0, y0, x1, y1)
-        check(self._lib.gbr_image_into(self._h, int(plane), rect, image.ctypes.data,
-                                       image.strides[0]))
+        fn = self._lib.gbr_image_into_async if asynchronous else self._lib.gbr_image_into
+        check(fn(self._h, int(plane), rect, image.ctypes.data, image.strides[0]))
+
+    def imageIntoAsync(self, plane, rectangle, image):
+        """Start copying a rectangle of a plane of the last draw into
+        ``image`` (host memory; pinned for full speed) and return at once;
+        ``readbackWait()`` waits for the copies."""
+        self._image_into(Plane(plane), rectangle, image, asynchronous=True)
+
+    def readbackWait(self):
+        check(self._lib.gbr_readback_wait(self._h))
 
     def colorImageInto(self, rectangle, image):
         """``colorImageInto`` (RendererStandalone.cpp:168-180); rectangle is

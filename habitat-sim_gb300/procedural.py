@@ -466,7 +466,7 @@ def grid_for(n):
     return x, int(math.ceil(n / x))
 
 
-def build_renderer(pkg, wl, mode=None, envs=None, planes=None):
+def build_renderer(pkg, wl, mode=None, envs=None, planes=None, double_buffer=False):
     env_list = list(range(wl.envs)) if envs is None else list(envs)
     cfg = pkg.RendererConfiguration()
     if wl.uniform:
@@ -478,8 +478,10 @@ def build_renderer(pkg, wl, mode=None, envs=None, planes=None):
         cfg.setDrawMode(mode)
     if planes is not None:
         cfg.setPlanes(planes)
-    r = pkg.RendererStandalone(cfg, pkg.RendererStandaloneConfiguration().setFlags(
-        pkg.RendererStandaloneFlags.QuietLog))
+    flags = pkg.RendererStandaloneFlags.QuietLog
+    if double_buffer:
+        flags |= pkg.RendererStandaloneFlags.DoubleBuffer
+    r = pkg.RendererStandalone(cfg, pkg.RendererStandaloneConfiguration().setFlags(flags))
     populate(r, wl, env_list)
     return r
 

@@ -47,6 +47,11 @@ typedef struct gbr_renderer gbr_renderer;
 #define GBR_FILE_GENERATE_MIPMAP 2u
 /* RendererStandaloneFlag::QuietLog (RendererStandalone.h:21-36). */
 #define GBR_STANDALONE_QUIET_LOG 1u
+/* Two sets of output planes: each draw renders into the set the previous
+ * draw did not, so an asynchronous readback of one draw
+ * (gbr_image_into_async) overlaps the next draw.  Plane pointers and DLPack
+ * views refer to the set of the last draw at the time of the call. */
+#define GBR_STANDALONE_DOUBLE_BUFFER 2u
 
 /* Output planes of the framebuffer. */
 #define GBR_PLANE_COLOR 1u        /* RGBA8, background (31,31,31,255)       */
@@ -228,6 +233,16 @@ gbr_status gbr_remove_node_hierarchy_template(gbr_renderer* r, const char* name)
 /* Device bytes of live geometry, textures and chunk boxes, and the bytes
  * currently reserved for them (live + free ranges). */
 gbr_status gbr_memory_usage(gbr_renderer* r, uint64_t* live_bytes, uint64_t* reserved_bytes);
+
+/* Asynchronous readback (no counterpart in the reference): enqueue the copy
+ * of rect {x0, y0, x1, y1} of a plane of the last draw into host memory on
+ * the renderer's copy stream, after that draw, and return at once.  dst must
+ * stay valid until gbr_readback_wait (pinned memory copies at full speed).
+ * The ragged layout is one row ({total pixels, 1}). */
+gbr_status gbr_image_into_async(gbr_renderer* r, uint32_t plane, const int32_t rect[4], void* dst,
+                                uint64_t dst_row_bytes);
+/* Wait for every readback enqueued so far (not for later draws). */
+gbr_status gbr_readback_wait(gbr_renderer* r);
 
 /* Renderer::sceneStats (Renderer.cpp:1356-1375). */
 typedef struct gbr_scene_stats_info {

@@ -334,6 +334,49 @@ def test_image_into_rectangles(pkg, procedural):
         gpu.colorImageInto(((0, 0), (97, 10)), np.empty((10, 97, 4), np.uint8))
 
 
+@pytest.mark.parametrize("graph", [False, True], ids=["plain", "graph"])
+def test_double_buffer_async_readback(pkg, procedural, graph):
+    """Double-buffered planes with asynchronous readback: each step's images
+    (read while the next step draws) equal a single-buffered renderer's
+    synchronous images of the same poses; a ragged layout reads one row."""
+    import torch
+    wl = procedural.config0(seed=8, envs=6, resolution=64, room_subdiv=16, boxes=6)
+    ref = procedural.build_renderer(pkg, wl, mode=1)
+    dbl = procedural.build_renderer(pkg, wl, mode=1, double_buffer=True)
+    fbw, fbh = dbl.framebufferSize()
+    rect = ((0, 0), (fbw, fbh))
+    bufs = [(torch.empty((fbh, fbw, 4), dtype=torch.uint8, pin_memory=True).numpy(),
+             torch.empty((fbh, fbw), dtype=torch.float32, pin_memory=True).numpy(),
+             torch.empty((fbh, fbw), dtype=torch.int32, pin_memory=True).numpy())
+            for _ in range(4)]
+    planes = (pkg.Plane.Color, pkg.Plane.LinearDepth, pkg.Plane.Semantic)
+    for k in range(4):
+        procedural.set_cameras(dbl, wl, procedural.camera_poses(wl, k))
+        dbl.draw(graph=graph)
+        for p, b in zip(planes, bufs[k]):
+            dbl.imageIntoAsync(p, rect, b)
+    dbl.readbackWait()
+    for k in range(4):
+        procedural.set_cameras(ref, wl, procedural.camera_poses(wl, k))
+        ref.draw(graph=graph)
+        assert np.array_equal(bufs[k][0], ref.colorImage())
+        assert np.array_equal(bufs[k][1].view(np.uint32), ref.linearDepthImage().view(np.uint32))
+        assert np.array_equal(bufs[k][2].view(np.uint32), ref.semanticImage())
+    # the synchronous calls read the last draw's set
+    assert np.array_equal(dbl.colorImage(), ref.colorImage())
+    wl2 = procedural.config2(envs=5, scenes=2, tri_range=(2e4, 4e4))
+    rag = procedural.build_renderer(pkg, wl2, mode=1, double_buffer=True)
+    procedural.set_cameras(rag, wl2, procedural.camera_poses(wl2, 0))
+    rag.draw(graph=graph)
+    n = rag.framebufferSize()[0]
+    row = np.empty((1, n, 4), np.uint8)
+    rag.imageIntoAsync(pkg.Plane.Color, ((0, 0), (n, 1)), row)
+    rag.readbackWait()
+    off, _, w, h = rag.sceneViewport(3)
+    assert np.array_equal(row[0, off:off + w * h].reshape(h, w, 4),
+                          rag.sceneImage(pkg.Plane.Color, 3))
+
+
 def test_unproject_device_matches_host(pkg):
     import torch
     p = S.perspective(60.0, 1.0, 0.01, 10.0)
