@@ -446,6 +446,7 @@ struct Setup {
 struct Ctx {
   uint64_t* keys;
   QEntry* queue;
+  QEntry* spill;  // this CTA's global spill area (qcap more entries), or null
   uint32_t* qcount;
   int qcap;
   int rx0, ry0, rw, rh;  // region
@@ -539,6 +540,24 @@ __device__ __forceinline__ void raster_setup(const Setup& st, uint32_t ordinal, 
     }
 }
 
+__device__ __forceinline__ void store_entry(QEntry& e, const Setup& st, uint32_t ordinal) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    e.X[i] = st.X[i];
+    e.Y[i] = st.Y[i];
+  }
+  e.zw0 = st.zw0;
+  e.d1 = st.d1;
+  e.d2 = st.d2;
+  e.inva = st.inva;
+  e.ordinal = ordinal;
+  e.bias = st.bias;
+  e.x0 = int16_t(st.x0);
+  e.y0 = int16_t(st.y0);
+  e.x1 = int16_t(st.x1);
+  e.y1 = int16_t(st.y1);
+}
+
 __device__ __forceinline__ void emit(const float4* q, uint32_t ordinal, const Ctx& c) {
   Setup st;
   if (!setup_sub(q, c, st)) return;
@@ -546,22 +565,11 @@ __device__ __forceinline__ void emit(const float4* q, uint32_t ordinal, const Ct
   if (area > c.small_area) {
     const uint32_t slot = atomicAdd(c.qcount, 1u);
     if (slot < uint32_t(c.qcap)) {
-      QEntry& e = c.queue[slot];
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        e.X[i] = st.X[i];
-        e.Y[i] = st.Y[i];
-      }
-      e.zw0 = st.zw0;
-      e.d1 = st.d1;
-      e.d2 = st.d2;
-      e.inva = st.inva;
-      e.ordinal = ordinal;
-      e.bias = st.bias;
-      e.x0 = int16_t(st.x0);
-      e.y0 = int16_t(st.y0);
-      e.x1 = int16_t(st.x1);
-      e.y1 = int16_t(st.y1);
+      store_entry(c.queue[slot], st, ordinal);
+      return;
+    }
+    if (c.spill && slot < 2u * uint32_t(c.qcap)) {
+      store_entry(c.spill[slot - c.qcap], st, ordinal);
       return;
     }
   }
@@ -1015,6 +1023,7 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
     Ctx c;
     c.keys = keys;
     c.queue = queue;
+    c.spill = p.spill ? static_cast<QEntry*>(p.spill) + size_t(blockIdx.x) * T : nullptr;
     c.qcount = &s_qcount;
     c.qcap = T;
     c.rx0 = wi.x0;
@@ -1061,7 +1070,8 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
     __syncthreads();
     for (;;) {
       const uint32_t rd = s_rd, wr = s_wr, crd = s_crd, cwr = s_cwr, next = s_next,
-                     nq = min(s_qcount, uint32_t(T));
+                     queued = min(s_qcount, uint32_t(c.spill ? 2 * T : T)),
+                     nq = min(queued, uint32_t(T));
       __syncthreads();  // everyone has read the counters
       const bool low = wr - rd < uint32_t(T / 32);
       const bool clusters_left = next < nclusters, have_clusters = cwr != crd;
@@ -1115,6 +1125,13 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
         if (threadIdx.x == 0) s_qcount = 0;
         tiles_stale = true;
         __syncthreads();
+        if (queued > nq) {
+          // A round queued more than the shared queue holds: the rest went to
+          // this CTA's spill area; move it into the emptied queue.
+          for (uint32_t i = threadIdx.x; i < queued - nq; i += T) queue[i] = c.spill[i];
+          if (threadIdx.x == 0) s_qcount = queued - nq;
+          __syncthreads();
+        }
         continue;
       }
       if (need_cull) {
@@ -1300,6 +1317,10 @@ cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStr
 
 size_t raster_smem_bytes(int threads, int region_px, int prefix_cap) {
   return smem_layout(threads, region_px, prefix_cap).total;
+}
+
+size_t raster_spill_bytes(int threads, uint32_t grid) {
+  return size_t(grid) * size_t(threads) * sizeof(QEntry);
 }
 
 #define GBR_RASTER_SWITCH(threads, F) \

@@ -53,6 +53,7 @@ struct RasterParams {
   const uint32_t* vis_count;
   const uint32_t* vis_tris;
   const uint32_t* vis_clusters;
+  void* spill;                // per CTA (blockIdx) `threads` queue entries of spill space, or null
   const ChunkBox* boxes;      // chunk and cluster boxes (null: no box culling)
   const float4* pos;
   const float4* color;
@@ -83,6 +84,8 @@ struct RasterParams {
 
 cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStream_t stream);
 size_t raster_smem_bytes(int threads, int region_px, int prefix_cap);
+// Bytes of the queue spill area for `grid` CTAs of `threads` threads.
+size_t raster_spill_bytes(int threads, uint32_t grid);
 // Raises the kernel's dynamic shared-memory limit to the device maximum and
 // returns that maximum and the kernel's static shared memory.
 cudaError_t raster_configure(int threads, size_t* max_dynamic, size_t* static_bytes);

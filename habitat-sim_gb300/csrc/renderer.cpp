@@ -241,10 +241,11 @@ Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
           err = "out of device memory for the framebuffer";
           return nullptr;
         }
-  if (cudaEventCreateWithFlags(&r->upload_done_, cudaEventDisableTiming) != cudaSuccess) {
-    err = "cudaEventCreate failed";
-    return nullptr;
-  }
+  for (auto& e : r->upload_done_)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      err = "cudaEventCreate failed";
+      return nullptr;
+    }
   // A blocking stream (ordered with the legacy default stream) for graph
   // capture when the caller passes the default stream, which cannot be captured.
   if (cudaStreamCreate(&r->own_stream_) != cudaSuccess) {
@@ -267,14 +268,15 @@ Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
 
 Renderer::~Renderer() {
   cudaSetDevice(device_);
-  if (last_stream_ || upload_pending_) cudaDeviceSynchronize();
+  if (last_stream_ || upload_pending_[0] || upload_pending_[1]) cudaDeviceSynchronize();
   if (copy_stream_) cudaStreamSynchronize(copy_stream_);
   for (auto& g : graph_exec_)
     if (g) cudaGraphExecDestroy(g);
   for (auto& e : copy_done_)
     if (e) cudaEventDestroy(e);
   if (copy_stream_) cudaStreamDestroy(copy_stream_);
-  if (upload_done_) cudaEventDestroy(upload_done_);
+  for (auto& e : upload_done_)
+    if (e) cudaEventDestroy(e);
   if (own_stream_) cudaStreamDestroy(own_stream_);
   for (auto& e : ev_)
     if (e) cudaEventDestroy(e);
@@ -770,11 +772,16 @@ gbr_status Renderer::set_enabled(uint32_t scene, bool enabled) {
 // Device ranges of a removed resource are reused by later adds, so nothing
 // the GPU may still be reading (the last draw) can be released early.
 gbr_status Renderer::quiesce() {
-  if (upload_pending_) {  // upload_done_ follows the whole last step on its stream
-    cudaSetDevice(device_);
-    GBR_CUDA(cudaEventSynchronize(upload_done_), "synchronise before removal");
-    upload_pending_ = false;
-  }
+  cudaSetDevice(device_);
+  return wait_uploads();  // upload_done_ follows the whole step that used each slot
+}
+
+gbr_status Renderer::wait_uploads() {
+  for (int s = 0; s < 2; ++s)
+    if (upload_pending_[s]) {
+      GBR_CUDA(cudaEventSynchronize(upload_done_[s]), "wait for previous steps");
+      upload_pending_[s] = false;
+    }
   return GBR_OK;
 }
 
@@ -856,10 +863,7 @@ gbr_status Renderer::upload_tables() {
 
 gbr_status Renderer::rebuild(cudaStream_t stream) {
   GBR_CUDA(cudaStreamSynchronize(stream), "draw: synchronise before rebuild");
-  if (upload_pending_) {
-    cudaEventSynchronize(upload_done_);
-    upload_pending_ = false;
-  }
+  if (gbr_status st = wait_uploads()) return st;
   const uint32_t S = uint32_t(scenes_.size());
   std::vector<SceneRec> recs(S);
   std::vector<int32_t> parents;
@@ -963,8 +967,10 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
       !d_status_.reserve(4, false) || !d_counter_.reserve(4, false) ||
       !d_items_.reserve(std::max<size_t>(items.size(), 1) * sizeof(WorkItem), false) ||
       !d_items_lpt_.reserve(std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem), false) ||
-      !h_stage_.reserve(std::max<size_t>(camera_block_bytes(), 1) + std::max<size_t>(nodes, 1) * 64 +
-                        std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem)))
+      !h_stage_[0].reserve(std::max<size_t>(camera_block_bytes(), 1) +
+                           std::max<size_t>(nodes, 1) * 64 +
+                           std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem)) ||
+      !h_stage_[1].reserve(h_stage_[0].bytes))
     return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of memory for scene data");
   GBR_CUDA(cudaMemcpy(d_scenes_.ptr, recs.data(), S * sizeof(SceneRec), cudaMemcpyHostToDevice),
            "scene upload");
@@ -1026,11 +1032,11 @@ gbr_status Renderer::ensure_raster_config() {
 gbr_status Renderer::upload_step(cudaStream_t stream) {
   // Cameras always, local transforms of scenes whose view was taken.
   const uint32_t S = uint32_t(scenes_.size());
-  if (upload_pending_) {
-    GBR_CUDA(cudaEventSynchronize(upload_done_), "draw: wait for previous upload");
-    upload_pending_ = false;
+  if (upload_pending_[slot_]) {  // the step that last used this staging slot
+    GBR_CUDA(cudaEventSynchronize(upload_done_[slot_]), "draw: wait for previous upload");
+    upload_pending_[slot_] = false;
   }
-  char* stage = static_cast<char*>(h_stage_.ptr);
+  char* stage = static_cast<char*>(h_stage_[slot_].ptr);
   if (bindings_dirty_) {
     // Visible records: each enabled scene gets room for its source's draws.
     uint64_t base = 0;
@@ -1137,7 +1143,7 @@ void Renderer::order_items() {
     if (on[a] != on[b]) return on[a] > on[b];
     return cost[a] > cost[b];
   });
-  WorkItem* istage = reinterpret_cast<WorkItem*>(static_cast<char*>(h_stage_.ptr) +
+  WorkItem* istage = reinterpret_cast<WorkItem*>(static_cast<char*>(h_stage_[slot_].ptr) +
                                                  camera_block_bytes() +
                                                  size_t(total_nodes_) * 64);
   for (size_t i = 0; i < n; ++i) istage[i] = batched_items_[perm[i]];
@@ -1190,6 +1196,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   rp.out.linear = (cfg_.planes & GBR_PLANE_LINEAR_DEPTH) ? planes[2].as<float>() : nullptr;
   rp.out.semantic = (cfg_.planes & GBR_PLANE_SEMANTIC) ? planes[3].as<uint32_t>() : nullptr;
   rp.prefix_cap = prefix_cap_;
+  rp.spill = d_spill_.ptr;
   rp.small_area = tuning_.small_area;
   rp.occlusion = tuning_.occlusion_culling;
   rp.max_lights = max_lights_;
@@ -1243,12 +1250,28 @@ gbr_status Renderer::draw(cudaStream_t stream, uint32_t mode, bool use_graph) {
   if (gbr_status s = ensure_raster_config()) return s;
   if (tables_dirty_)
     if (gbr_status s = upload_tables()) return s;
-  if (gbr_status s = upload_step(stream)) return s;
+  {
+    // Queue spill space for every CTA of the largest launch (allocated
+    // before any graph capture).
+    uint32_t grid = uint32_t(sm_count_) * uint32_t(ctas_per_sm_);
+    if (mode != GBR_DRAW_BATCHED)
+      for (uint32_t c : scene_item_count_) grid = std::max(grid, c);
+    void* before = d_spill_.ptr;
+    if (!d_spill_.reserve(raster_spill_bytes(tuning_.threads, grid), false))
+      return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of device memory for the raster queue");
+    if (d_spill_.ptr != before) graph_valid_ = false;
+  }
+  const int prev_slot = slot_;
+  slot_ ^= 1;  // this draw's staging slot (and plane set when double-buffered)
+  if (gbr_status s = upload_step(stream)) {
+    slot_ = prev_slot;
+    return s;
+  }
   const uint32_t S = uint32_t(scenes_.size());
   const size_t cam_bytes = camera_block_bytes();
   // The plane set this draw writes; with double buffering, the one the last
   // draw did not write, once the readbacks of its previous contents are done.
-  const int set = double_buffer_ ? (front_ ^ 1) : 0;
+  const int set = double_buffer_ ? slot_ : 0;
   draw_set_ = set;
   if (copy_pending_[set]) {
     GBR_CUDA(cudaStreamWaitEvent(stream, copy_done_[set], 0), "wait for readback");
@@ -1258,34 +1281,36 @@ gbr_status Renderer::draw(cudaStream_t stream, uint32_t mode, bool use_graph) {
     graph_built_[0] = graph_built_[1] = false;
     graph_valid_ = true;
   }
+  const int gi = slot_;  // graphs by staging slot (and with it the plane set)
   if (mode == GBR_DRAW_BATCHED && use_graph) {
-    if (!graph_built_[set] || graph_stream_[set] != stream) {
-      if (graph_exec_[set]) {
-        cudaGraphExecDestroy(graph_exec_[set]);
-        graph_exec_[set] = nullptr;
+    if (!graph_built_[gi] || graph_stream_[gi] != stream) {
+      if (graph_exec_[gi]) {
+        cudaGraphExecDestroy(graph_exec_[gi]);
+        graph_exec_[gi] = nullptr;
       }
       cudaGraph_t g;
       GBR_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "graph capture");
-      cudaError_t e = cudaMemcpyAsync(d_cameras_.ptr, h_stage_.ptr, cam_bytes,
+      cudaError_t e = cudaMemcpyAsync(d_cameras_.ptr, h_stage_[gi].ptr, cam_bytes,
                                       cudaMemcpyHostToDevice, stream);
       gbr_status st = e == cudaSuccess ? enqueue_step(stream, mode) : cuda_fail(e, "graph camera copy");
       cudaError_t e2 = cudaStreamEndCapture(stream, &g);
       if (st != GBR_OK) return st;
       GBR_CUDA(e2, "graph capture");
-      e = cudaGraphInstantiate(&graph_exec_[set], g, 0);
+      e = cudaGraphInstantiate(&graph_exec_[gi], g, 0);
       cudaGraphDestroy(g);
       GBR_CUDA(e, "graph instantiate");
-      graph_built_[set] = true;
-      graph_stream_[set] = stream;
+      graph_built_[gi] = true;
+      graph_stream_[gi] = stream;
     }
-    GBR_CUDA(cudaGraphLaunch(graph_exec_[set], stream), "graph launch");
+    GBR_CUDA(cudaGraphLaunch(graph_exec_[gi], stream), "graph launch");
   } else {
-    GBR_CUDA(cudaMemcpyAsync(d_cameras_.ptr, h_stage_.ptr, cam_bytes, cudaMemcpyHostToDevice, stream),
+    GBR_CUDA(cudaMemcpyAsync(d_cameras_.ptr, h_stage_[slot_].ptr, cam_bytes,
+                             cudaMemcpyHostToDevice, stream),
              "camera upload");
     if (gbr_status s = enqueue_step(stream, mode)) return s;
   }
-  GBR_CUDA(cudaEventRecord(upload_done_, stream), "event record");
-  upload_pending_ = true;
+  GBR_CUDA(cudaEventRecord(upload_done_[slot_], stream), "event record");
+  upload_pending_[slot_] = true;
   last_stream_ = stream;
   front_ = set;
   last_stats_.scenes = S;
@@ -1334,7 +1359,8 @@ gbr_status Renderer::image_into_async(uint32_t plane, const int32_t* rect, void*
     for (auto& e : copy_done_)
       GBR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy event");
   }
-  if (upload_pending_) GBR_CUDA(cudaStreamWaitEvent(copy_stream_, upload_done_, 0), "wait for draw");
+  if (upload_pending_[slot_])
+    GBR_CUDA(cudaStreamWaitEvent(copy_stream_, upload_done_[slot_], 0), "wait for draw");
   if (w && h)
     GBR_CUDA(cudaMemcpy2DAsync(dst, row_bytes, src + (size_t(rect[1]) * fb_w_ + rect[0]) * elem,
                                size_t(fb_w_) * elem, w * elem, h, cudaMemcpyDeviceToHost,

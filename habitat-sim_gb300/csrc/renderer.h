@@ -194,6 +194,7 @@ class Renderer {
   // device
   DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_, d_normal_;
   DeviceBuffer d_lights_, d_model_;  // lit renderers: world lights, per-draw model data
+  DeviceBuffer d_spill_;  // raster queue spill area, per CTA
   uint32_t max_lights_ = 0;
   DeviceBuffer d_meshes_, d_materials_, d_textures_, d_boxes_;
   DeviceBuffer d_scenes_, d_parents_, d_local_, d_draws_, d_cameras_;
@@ -203,12 +204,17 @@ class Renderer {
   bool double_buffer_ = false;
   int front_ = 0;                // set written by the last draw
   int draw_set_ = 0;             // set the draw being enqueued writes
+  gbr_status wait_uploads();     // both slots idle
   cudaStream_t copy_stream_ = nullptr;
   cudaEvent_t copy_done_[2] = {nullptr, nullptr};
   bool copy_pending_[2] = {false, false};
-  PinnedBuffer h_stage_;
-  cudaEvent_t upload_done_ = nullptr;
-  bool upload_pending_ = false;
+  // Host staging of the per-step uploads, two slots used by alternate draws so
+  // that the host stages draw k + 1 while draw k runs; upload_done_[slot]
+  // follows the whole step that last used the slot.
+  PinnedBuffer h_stage_[2];
+  cudaEvent_t upload_done_[2] = {nullptr, nullptr};
+  bool upload_pending_[2] = {false, false};
+  int slot_ = 1;  // slot of the last draw (the next draw takes the other)
   cudaStream_t last_stream_ = nullptr;
   cudaStream_t own_stream_ = nullptr;
 

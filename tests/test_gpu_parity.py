@@ -262,6 +262,44 @@ def test_huge_triangle_guard_band(pkg):
     assert (gpu.colorImage()[..., 3] == 255).all()
 
 
+@pytest.mark.parametrize("mode", [0, 1], ids=["per_scene", "batched"])
+def test_queue_overflow_many_big_triangles(pkg, mode):
+    """3072 viewport-sized triangles at random (and some equal) depths: one
+    round of 256 threads queues more large triangles than the shared queue
+    holds, so the rest go through the spill area; bit-exact against the
+    oracle, depth ties resolved by draw order."""
+    from oracle.model import OracleRenderer
+    rng = np.random.default_rng(11)
+    n = 3072
+    z = rng.uniform(-3.0, -1.0, n).astype(np.float32)
+    z[::7] = np.float32(-2.0)                          # coplanar groups: ties
+    cx, cy = rng.uniform(-0.5, 0.5, (2, n)).astype(np.float32)
+    pos = np.zeros((3 * n, 3), np.float32)
+    for k, (dx, dy) in enumerate([(-3.0, -3.0), (3.0, -3.0), (0.0, 3.0)]):
+        pos[k::3, 0] = (cx + dx) * -z
+        pos[k::3, 1] = (cy + dy) * -z
+        pos[k::3, 2] = z
+    col = rng.uniform(0, 1, (3 * n, 4)).astype(np.float32)
+    col[:, 3] = 1.0
+    idx = np.arange(3 * n, dtype=np.uint32)
+    proj = S.perspective(60.0, 1.0, 0.1, 10.0)
+    outs = []
+    for r in (gpu_factory(pkg, mode)((64, 64), (2, 1), 0), OracleRenderer((64, 64), (2, 1), 0)):
+        if hasattr(r, "setTuning"):
+            r.setTuning(threads=256, region_width=64, region_height=64)
+        m = r.addMesh(pos, col, None, None, idx)
+        r.addNodeHierarchyTemplate("stack", [(m, 0, 3 * n, 0, None)])
+        for s in range(2):
+            r.addNodeHierarchy(s, "stack")
+        r.updateCamera(0, proj, S.translation(0.0, 0.0, 0.0))
+        r.updateCamera(1, proj, S.translation(0.3, -0.2, 0.5))
+        r.draw()
+        outs.append(r)
+    gpu, cpu = outs
+    assert_parity([compare_scene(gpu, cpu, pkg, s) for s in range(2)])
+    assert (gpu.colorImage()[..., 3] == 255).all()
+
+
 def test_empty_and_cleared_scenes(pkg, procedural):
     wl = procedural.config0(seed=3, envs=4, resolution=32, room_subdiv=4, boxes=2)
     gpu = procedural.build_renderer(pkg, wl)
