@@ -1,12 +1,17 @@
 """GB300-native batch renderer: a drop-in for habitat-sim's
 ``esp::gfx_batch`` draw path (C ABI in ``include/gbr.h``, CUDA kernels for
-sm_103a in ``csrc/``)."""
+sm_103a in ``csrc/``), and the batch replay renderer driven by gfx-replay
+keyframes (C ABI in ``include/gbr_replay.h``)."""
 from .gfx_batch import (DrawMode, GbrError, Plane, RendererConfiguration, RendererFileFlags,
                         RendererFlags, RendererLightType, RendererStandalone,
                         RendererStandaloneConfiguration, RendererStandaloneFlags, SceneStats,
                         calculateDepthUnprojection, unprojectDepth, unprojectDepthDevice)
+from .replay import (CameraSensorSpec, Keyframe, Ray, ReplayRenderer, ReplayRendererConfiguration,
+                     SensorSubType, keyframes_to_string)
 
 __all__ = ["DrawMode", "GbrError", "Plane", "RendererConfiguration", "RendererFileFlags",
            "RendererFlags", "RendererLightType", "RendererStandalone",
            "RendererStandaloneConfiguration", "RendererStandaloneFlags", "SceneStats",
-           "calculateDepthUnprojection", "unprojectDepth", "unprojectDepthDevice"]
+           "calculateDepthUnprojection", "unprojectDepth", "unprojectDepthDevice",
+           "CameraSensorSpec", "Keyframe", "Ray", "ReplayRenderer", "ReplayRendererConfiguration",
+           "SensorSubType", "keyframes_to_string"]

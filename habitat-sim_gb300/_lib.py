@@ -1,4 +1,5 @@
-"""ctypes bindings of libgbr.so (the C ABI declared in include/gbr.h)."""
+"""ctypes bindings of libgbr.so (the C ABI declared in include/gbr.h and
+include/gbr_replay.h)."""
 import ctypes
 import os
 
@@ -60,6 +61,17 @@ class DrawStats(ctypes.Structure):
                 ("raster_ms", ctypes.c_float)]
 
 
+class ReplayConfig(ctypes.Structure):
+    _fields_ = [("num_environments", ctypes.c_uint32), ("gpu_device_id", ctypes.c_int32),
+                ("standalone", ctypes.c_int32), ("enable_frustum_culling", ctypes.c_int32),
+                ("enable_hbao", ctypes.c_int32), ("sensor_uuid", ctypes.c_char_p),
+                ("resolution", ctypes.c_int32 * 2), ("hfov_degrees", ctypes.c_float),
+                ("near_plane", ctypes.c_float), ("far_plane", ctypes.c_float),
+                ("orthographic", ctypes.c_int32), ("ortho_scale", ctypes.c_float),
+                ("max_light_count", ctypes.c_uint32), ("ambient_factor", ctypes.c_float),
+                ("draw_mode", ctypes.c_uint32), ("quiet", ctypes.c_uint32)]
+
+
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
 _I32 = ctypes.c_int32
@@ -119,6 +131,29 @@ PROTOTYPES = {
     "gbr_set_kernel_timing": (_ST, [_P, _I32]),
     "gbr_render_mesh_no_alloc": (_ST, [_P, _P, _P, _U32, _U32, c_float_p, c_float_p, _U32, _I32,
                                        _I32, _I32, _P, _P, _P, _P, _P]),
+    # include/gbr_replay.h
+    "gbr_replay_config_init": (None, [ctypes.POINTER(ReplayConfig)]),
+    "gbr_replay_create": (_ST, [ctypes.POINTER(ReplayConfig), ctypes.POINTER(_P)]),
+    "gbr_replay_destroy": (None, [_P]),
+    "gbr_replay_close": (_ST, [_P]),
+    "gbr_replay_renderer": (_ST, [_P, ctypes.POINTER(_P)]),
+    "gbr_replay_environment_grid_size": (_ST, [_I32, ctypes.POINTER(_I32)]),
+    "gbr_replay_preload_file": (_ST, [_P, ctypes.c_char_p]),
+    "gbr_replay_environment_count": (_ST, [_P, ctypes.POINTER(_U32)]),
+    "gbr_replay_sensor_size": (_ST, [_P, _U32, ctypes.POINTER(_I32)]),
+    "gbr_replay_clear_environment": (_ST, [_P, _U32]),
+    "gbr_replay_set_environment_keyframe": (_ST, [_P, _U32, ctypes.c_char_p, _U64]),
+    "gbr_replay_set_environment_keyframe_unwrapped": (_ST, [_P, _U32, ctypes.c_char_p, _U64]),
+    "gbr_replay_set_keyframes": (_ST, [_P, _U32, ctypes.c_char_p, _U64]),
+    "gbr_replay_set_keyframe_index": (_ST, [_P, _U32, _I32]),
+    "gbr_replay_keyframe_count": (_ST, [_P, _U32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
+    "gbr_replay_user_transform": (_ST, [_P, _U32, ctypes.c_char_p, c_float_p, c_float_p,
+                                        ctypes.POINTER(_I32)]),
+    "gbr_replay_set_sensor_transform": (_ST, [_P, _U32, ctypes.c_char_p, c_float_p]),
+    "gbr_replay_set_sensor_transforms_from_keyframe": (_ST, [_P, _U32, ctypes.c_char_p]),
+    "gbr_replay_render": (_ST, [_P, _P, _U32, ctypes.POINTER(_P), _U64, _U32, ctypes.POINTER(_P),
+                                _U64]),
+    "gbr_replay_unproject": (_ST, [_P, _U32, _I32, _I32, c_float_p, c_float_p]),
 }
 
 _lib = None

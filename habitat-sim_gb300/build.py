@@ -20,8 +20,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["kernels.cu"]
-CPP_SOURCES = ["renderer.cpp", "importer.cpp", "capi.cpp"]
-HEADERS = ["kernels.h", "records.h", "renderer.h", "importer.h"]
+CPP_SOURCES = ["renderer.cpp", "importer.cpp", "capi.cpp", "replay.cpp"]
+HEADERS = ["kernels.h", "records.h", "renderer.h", "importer.h", "json.h", "replay.h"]
 
 
 def _cuda_home():
@@ -47,7 +47,8 @@ def build(verbose=False):
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "gbr.h")]
+    headers = [os.path.join(CSRC, h) for h in HEADERS] + [
+        os.path.join(INCLUDE, h) for h in ("gbr.h", "gbr_replay.h")]
     jobs = []
     objs = []
     for src in CU_SOURCES:

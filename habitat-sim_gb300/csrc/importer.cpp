@@ -17,6 +17,7 @@
 //     Whole flag flattens the file with absolute transforms (:795-820);
 //     a file without scenes holds exactly one mesh (:663-690).
 #include "importer.h"
+#include "json.h"
 
 #include <algorithm>
 #include <cmath>
@@ -28,136 +29,6 @@
 
 namespace gbr {
 namespace {
-
-// ------------------------------------------------------------------ JSON
-struct Json {
-  enum Type { Null, Bool, Number, String, Array, Object } type = Null;
-  bool b = false;
-  double num = 0;
-  std::string str;
-  std::vector<Json> arr;
-  std::vector<std::pair<std::string, Json>> obj;
-
-  const Json* get(const char* key) const {
-    if (type != Object) return nullptr;
-    for (auto& kv : obj)
-      if (kv.first == key) return &kv.second;
-    return nullptr;
-  }
-  double numberOr(const char* key, double def) const {
-    const Json* j = get(key);
-    return j && j->type == Number ? j->num : def;
-  }
-  const Json& operator[](size_t i) const { return arr[i]; }
-  size_t size() const { return type == Array ? arr.size() : 0; }
-};
-
-struct JsonParser {
-  const char* p;
-  const char* end;
-  std::string err;
-
-  void ws() {
-    while (p < end && (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t')) ++p;
-  }
-  bool fail(const char* m) {
-    if (err.empty()) err = m;
-    return false;
-  }
-  bool parseString(std::string& s) {
-    if (p >= end || *p != '"') return fail("expected string");
-    ++p;
-    while (p < end && *p != '"') {
-      if (*p == '\\') {
-        ++p;
-        if (p >= end) return fail("bad escape");
-        char c = *p++;
-        switch (c) {
-          case 'n': s += '\n'; break;
-          case 't': s += '\t'; break;
-          case 'r': s += '\r'; break;
-          case 'b': s += '\b'; break;
-          case 'f': s += '\f'; break;
-          case 'u': {
-            if (end - p < 4) return fail("bad unicode escape");
-            unsigned cp = std::stoul(std::string(p, p + 4), nullptr, 16);
-            p += 4;
-            if (cp < 0x80) {
-              s += char(cp);
-            } else if (cp < 0x800) {
-              s += char(0xC0 | (cp >> 6));
-              s += char(0x80 | (cp & 63));
-            } else {
-              s += char(0xE0 | (cp >> 12));
-              s += char(0x80 | ((cp >> 6) & 63));
-              s += char(0x80 | (cp & 63));
-            }
-            break;
-          }
-          default: s += c;
-        }
-      } else {
-        s += *p++;
-      }
-    }
-    if (p >= end) return fail("unterminated string");
-    ++p;
-    return true;
-  }
-  bool parse(Json& j, int depth = 0) {
-    if (depth > 256) return fail("nesting too deep");
-    ws();
-    if (p >= end) return fail("unexpected end");
-    char c = *p;
-    if (c == '{') {
-      j.type = Json::Object;
-      ++p;
-      ws();
-      if (p < end && *p == '}') { ++p; return true; }
-      for (;;) {
-        ws();
-        std::string key;
-        if (!parseString(key)) return false;
-        ws();
-        if (p >= end || *p != ':') return fail("expected ':'");
-        ++p;
-        j.obj.emplace_back(std::move(key), Json{});
-        if (!parse(j.obj.back().second, depth + 1)) return false;
-        ws();
-        if (p < end && *p == ',') { ++p; continue; }
-        if (p < end && *p == '}') { ++p; return true; }
-        return fail("expected ',' or '}'");
-      }
-    }
-    if (c == '[') {
-      j.type = Json::Array;
-      ++p;
-      ws();
-      if (p < end && *p == ']') { ++p; return true; }
-      for (;;) {
-        j.arr.emplace_back();
-        if (!parse(j.arr.back(), depth + 1)) return false;
-        ws();
-        if (p < end && *p == ',') { ++p; continue; }
-        if (p < end && *p == ']') { ++p; return true; }
-        return fail("expected ',' or ']'");
-      }
-    }
-    if (c == '"') {
-      j.type = Json::String;
-      return parseString(j.str);
-    }
-    if (end - p >= 4 && !std::strncmp(p, "true", 4)) { j.type = Json::Bool; j.b = true; p += 4; return true; }
-    if (end - p >= 5 && !std::strncmp(p, "false", 5)) { j.type = Json::Bool; p += 5; return true; }
-    if (end - p >= 4 && !std::strncmp(p, "null", 4)) { p += 4; return true; }
-    const char* s = p;
-    while (p < end && (std::strchr("+-0123456789.eE", *p) != nullptr)) ++p;
-    if (s == p) return fail("unexpected character");
-    j.type = Json::Number;
-    j.num = std::strtod(std::string(s, p).c_str(), nullptr);
-    return true;
-  }
-};
 
 // --------------------------------------------------------------- inflate
 struct BitReader {

@@ -1363,7 +1363,7 @@ gbr_status Renderer::image_into_async(uint32_t plane, const int32_t* rect, void*
     GBR_CUDA(cudaStreamWaitEvent(copy_stream_, upload_done_[slot_], 0), "wait for draw");
   if (w && h)
     GBR_CUDA(cudaMemcpy2DAsync(dst, row_bytes, src + (size_t(rect[1]) * fb_w_ + rect[0]) * elem,
-                               size_t(fb_w_) * elem, w * elem, h, cudaMemcpyDeviceToHost,
+                               size_t(fb_w_) * elem, w * elem, h, cudaMemcpyDefault,
                                copy_stream_),
              "imageIntoAsync copy");
   GBR_CUDA(cudaEventRecord(copy_done_[front_], copy_stream_), "copy event");
@@ -1390,7 +1390,7 @@ gbr_status Renderer::image_into(uint32_t plane, const int32_t* rect, void* dst, 
   if (gbr_status s = sync_and_check()) return s;
   if (!w || !h) return GBR_OK;
   GBR_CUDA(cudaMemcpy2D(dst, row_bytes, src + (size_t(rect[1]) * fb_w_ + rect[0]) * elem,
-                        size_t(fb_w_) * elem, w * elem, h, cudaMemcpyDeviceToHost),
+                        size_t(fb_w_) * elem, w * elem, h, cudaMemcpyDefault),
            "imageInto copy");
   return GBR_OK;
 }
@@ -1405,7 +1405,7 @@ gbr_status Renderer::scene_image_into(uint32_t plane, uint32_t scene, void* dst,
     return fail(GBR_ERROR_INVALID_ARGUMENT, "sceneImageInto: row pitch too small");
   if (gbr_status s = sync_and_check()) return s;
   GBR_CUDA(cudaMemcpy2D(dst, row_bytes, src + size_t(sc.fb_offset) * elem, size_t(sc.pitch) * elem,
-                        size_t(sc.width) * elem, size_t(sc.height), cudaMemcpyDeviceToHost),
+                        size_t(sc.width) * elem, size_t(sc.height), cudaMemcpyDefault),
            "sceneImageInto copy");
   return GBR_OK;
 }

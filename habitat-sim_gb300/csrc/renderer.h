@@ -247,5 +247,6 @@ class Renderer {
 };
 
 void set_last_error(const std::string& msg);
+const char* last_error_cstr();
 
 }  // namespace gbr

@@ -193,7 +193,27 @@ class RendererStandalone:
         check(self._lib.gbr_framebuffer_size(self._h, size))
         self._fb = (int(size[0]), int(size[1]))
 
+    @classmethod
+    def _borrow(cls, handle, configuration, standalone_configuration, owner):
+        """A view of a renderer that `owner` (a replay renderer) created and
+        destroys: valid while the owner is open; close() only drops the view."""
+        self = cls.__new__(cls)
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p(handle)
+        self._owner = owner
+        self._config = configuration
+        self._standalone = standalone_configuration
+        self._quiet = bool(standalone_configuration.flags & RendererStandaloneFlags.QuietLog)
+        self._viewports = None
+        size = (ctypes.c_int64 * 2)()
+        check(self._lib.gbr_framebuffer_size(self._h, size))
+        self._fb = (int(size[0]), int(size[1]))
+        return self
+
     def close(self):
+        if getattr(self, "_owner", None) is not None:
+            self._h = None
+            return
         if getattr(self, "_h", None):
             self._lib.gbr_destroy(self._h)
             self._h = None

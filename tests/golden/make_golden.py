@@ -13,7 +13,10 @@ test data (meshes, textures, PNG screenshots), not source code:
 * ``data/test_assets/scenes/batch*.gltf|.bin|.ktx2`` -- the scenes the test
   feeds to ``Renderer::addFile`` (``GfxBatchRendererTest.cpp:100-220``);
 * ``data/test_assets/screenshots/GfxBatchRendererTest*.png`` -- the golden
-  colour images (``GfxBatchRendererTest.cpp:1514-1906``).
+  colour images (``GfxBatchRendererTest.cpp:1514-1906``);
+* ``data/test_assets/objects/*.glb`` -- the untextured binary glTF objects
+  that habitat-sim's replay tests instance through keyframes
+  (``BatchReplayRendererTest.cpp:400-487`` uses ``sphere.glb``).
 
 The tests read only the copies in this folder, so they run where the
 habitat-sim tree is absent.
@@ -41,6 +44,8 @@ SCENES = [
     "batch-four-squares-no-scene.gltf", "batch-four-squares-no-scene.bin",
 ]
 
+OBJECTS = ["sphere.glb", "transform_box.glb", "nested_box.glb", "5boxes.glb"]
+
 SCREENSHOTS = [
     "GfxBatchRendererTestDefaults.png",
     "GfxBatchRendererTestSingleMesh.png",
@@ -57,7 +62,7 @@ SCREENSHOTS = [
 
 def main(root):
     manifest = {}
-    for sub, names in (("scenes", SCENES), ("screenshots", SCREENSHOTS)):
+    for sub, names in (("scenes", SCENES), ("screenshots", SCREENSHOTS), ("objects", OBJECTS)):
         os.makedirs(os.path.join(HERE, sub), exist_ok=True)
         for name in names:
             src = os.path.join(root, "data", "test_assets", sub, name)

@@ -1,5 +1,5 @@
 """The C-ABI library without a GPU: it loads, exports every entry point that
-include/gbr.h declares, and its host-only functions and argument checks
+include/gbr.h and include/gbr_replay.h declare, and its host-only functions and argument checks
 behave (no kernel runs here)."""
 import ctypes
 import os
@@ -25,9 +25,13 @@ def lib(pkg):
 
 
 def declared_functions():
-    text = open(os.path.join(ROOT, "include", "gbr.h")).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(gbr_[a-z0-9_]+)\s*\(", text)))
+    names = set()
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names |= set(re.findall(r"\b(gbr_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
 
 
 def test_header_declares_entry_points():
