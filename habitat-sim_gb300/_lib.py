@@ -1,5 +1,5 @@
-"""ctypes bindings of libgbr.so (the C ABI declared in include/gbr.h and
-include/gbr_replay.h)."""
+"""ctypes bindings of libgbr.so (the C ABI declared in include/gbr.h,
+include/gbr_replay.h and include/gbr_noise.h)."""
 import ctypes
 import os
 
@@ -154,6 +154,17 @@ PROTOTYPES = {
     "gbr_replay_render": (_ST, [_P, _P, _U32, ctypes.POINTER(_P), _U64, _U32, ctypes.POINTER(_P),
                                 _U64]),
     "gbr_replay_unproject": (_ST, [_P, _U32, _I32, _I32, c_float_p, c_float_p]),
+    # include/gbr_noise.h
+    "gbr_redwood_noise_create": (_ST, [c_float_p, _I32, _I32, _I32, ctypes.c_float, _U64,
+                                       ctypes.POINTER(_P)]),
+    "gbr_redwood_noise_destroy": (None, [_P]),
+    "gbr_redwood_noise_simulate_device": (_ST, [_P, _P, _I32, _I32, _P, _P]),
+    "gbr_redwood_noise_simulate_host": (_ST, [_P, c_float_p, _I32, _I32, c_float_p]),
+    "gbr_redwood_noise_simulate_tiles": (_ST, [_P, _P, _P, ctypes.c_int64, _I32, _I32, _I32, _I32,
+                                               _P]),
+    "gbr_redwood_noise_set_state": (_ST, [_P, _U64, _U64]),
+    "gbr_redwood_noise_get_state": (_ST, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
+    "gbr_normal_quantile_table": (_ST, [c_float_p, _U32]),
 }
 
 _lib = None
