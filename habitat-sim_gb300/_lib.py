@@ -1,5 +1,5 @@
 """ctypes bindings of libgbr.so (the C ABI declared in include/gbr.h,
-include/gbr_replay.h and include/gbr_noise.h)."""
+include/gbr_replay.h, include/gbr_noise.h and include/gbr_hbao.h)."""
 import ctypes
 import os
 
@@ -59,6 +59,12 @@ class DrawStats(ctypes.Structure):
                 ("visible_draws", ctypes.c_uint64), ("triangles", ctypes.c_uint64),
                 ("kernel_launches", ctypes.c_uint64), ("prepare_ms", ctypes.c_float),
                 ("raster_ms", ctypes.c_float)]
+
+
+class HbaoConfig(ctypes.Structure):
+    _fields_ = [("intensity", ctypes.c_float), ("bias", ctypes.c_float),
+                ("radius", ctypes.c_float), ("blur_sharpness", ctypes.c_float),
+                ("no_blur", ctypes.c_int32), ("special_blur", ctypes.c_int32)]
 
 
 class ReplayConfig(ctypes.Structure):
@@ -165,6 +171,12 @@ PROTOTYPES = {
     "gbr_redwood_noise_set_state": (_ST, [_P, _U64, _U64]),
     "gbr_redwood_noise_get_state": (_ST, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     "gbr_normal_quantile_table": (_ST, [c_float_p, _U32]),
+    # include/gbr_hbao.h
+    "gbr_hbao_config_init": (None, [ctypes.POINTER(HbaoConfig)]),
+    "gbr_hbao_draw": (_ST, [_P, ctypes.POINTER(HbaoConfig), _P]),
+    "gbr_hbao_apply": (_ST, [ctypes.POINTER(HbaoConfig), c_float_p, _P, _P, _I32, _I32,
+                             ctypes.c_int64, _P]),
+    "gbr_hbao_jitter_table": (_ST, [c_float_p]),
 }
 
 _lib = None

@@ -19,9 +19,9 @@ LIB = os.path.join(BUILD, "libgbr.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["kernels.cu", "noise.cu"]
+CU_SOURCES = ["kernels.cu", "noise.cu", "hbao.cu"]
 CPP_SOURCES = ["renderer.cpp", "importer.cpp", "capi.cpp", "replay.cpp"]
-HEADERS = ["kernels.h", "records.h", "renderer.h", "importer.h", "json.h", "replay.h"]
+HEADERS = ["kernels.h", "records.h", "renderer.h", "importer.h", "json.h", "replay.h", "hbao.h"]
 
 
 def _cuda_home():
@@ -48,7 +48,7 @@ def build(verbose=False):
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, h) for h in HEADERS] + [
-        os.path.join(INCLUDE, h) for h in ("gbr.h", "gbr_replay.h", "gbr_noise.h")]
+        os.path.join(INCLUDE, h) for h in ("gbr.h", "gbr_replay.h", "gbr_noise.h", "gbr_hbao.h")]
     jobs = []
     objs = []
     for src in CU_SOURCES:

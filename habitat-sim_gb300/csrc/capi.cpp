@@ -427,4 +427,10 @@ gbr_status gbr_set_kernel_timing(gbr_renderer* r, int32_t enabled) {
   return R(r)->set_kernel_timing(enabled != 0);
 }
 
+gbr_status gbr_hbao_draw(gbr_renderer* r, const gbr_hbao_config* config, void* stream) {
+  GBR_HANDLE(r);
+  GBR_ARG(config);
+  return guarded([&] { return R(r)->hbao(*config, static_cast<cudaStream_t>(stream)); });
+}
+
 }  // extern "C"

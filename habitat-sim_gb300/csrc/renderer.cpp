@@ -17,6 +17,7 @@
 #include <memory>
 #include <numeric>
 
+#include "hbao.h"
 #include "importer.h"
 
 namespace gbr {
@@ -698,6 +699,7 @@ gbr_status Renderer::update_camera(uint32_t scene, const float* p, const float* 
   SceneState& sc = scenes_[scene];
   mat4_mul(p, v, sc.pv);
   std::memcpy(sc.view, v, 64);
+  std::memcpy(sc.proj, p, 64);
   // calculateDepthUnprojection (DepthUnprojection.cpp:98-101)
   sc.unprojection[0] = (p[2 * 4 + 2] - 1.0f) * 0.5f;
   sc.unprojection[1] = p[3 * 4 + 2] * 0.5f;
@@ -1368,6 +1370,45 @@ gbr_status Renderer::image_into_async(uint32_t plane, const int32_t* rect, void*
              "imageIntoAsync copy");
   GBR_CUDA(cudaEventRecord(copy_done_[front_], copy_stream_), "copy event");
   copy_pending_[front_] = true;
+  return GBR_OK;
+}
+
+// Hbao::drawEffect, classic (src/esp/gfx_batch/Hbao.cpp:874-935), over all
+// enabled scenes at once (three launches, csrc/hbao.cu).
+gbr_status Renderer::hbao(const gbr_hbao_config& c, cudaStream_t stream) {
+  if (!(cfg_.planes & GBR_PLANE_COLOR) || !(cfg_.planes & GBR_PLANE_LINEAR_DEPTH))
+    return fail(GBR_ERROR_STATE, "Hbao: the renderer needs its colour and linear-depth planes");
+  HbaoParams params;
+  std::string err;
+  if (!hbao_params(c, params, err)) return fail(GBR_ERROR_INVALID_ARGUMENT, err);
+  std::vector<HbaoScene> recs;
+  int max_pixels = 0;
+  for (const SceneState& sc : scenes_) {
+    if (!sc.enabled || sc.width <= 0 || sc.height <= 0) continue;
+    recs.push_back(hbao_scene(sc.proj, sc.width, sc.height, sc.fb_offset, sc.pitch, c.radius));
+    max_pixels = std::max(max_pixels, sc.width * sc.height);
+  }
+  if (recs.empty()) return GBR_OK;
+  cudaSetDevice(device_);
+  const size_t fb = size_t(fb_w_) * size_t(fb_h_);
+  if (!d_hbao_scenes_.reserve(recs.size() * sizeof(HbaoScene), false) || !d_hbao_ao_.reserve(2 * fb, false))
+    return fail(GBR_ERROR_OUT_OF_MEMORY, "Hbao: device allocation failed");
+  if (upload_pending_[slot_])  // after the last draw, whatever stream it ran on
+    GBR_CUDA(cudaStreamWaitEvent(stream, upload_done_[slot_], 0), "Hbao: wait for draw");
+  GBR_CUDA(cudaMemcpyAsync(d_hbao_scenes_.ptr, recs.data(), recs.size() * sizeof(HbaoScene),
+                           cudaMemcpyHostToDevice, stream),
+           "Hbao: records");
+  size_t elem;
+  uint32_t* color = static_cast<uint32_t*>(plane_ptr(GBR_PLANE_COLOR, &elem));
+  const float* depth = static_cast<const float*>(plane_ptr(GBR_PLANE_LINEAR_DEPTH, &elem));
+  uint8_t* q = static_cast<uint8_t*>(d_hbao_ao_.ptr);
+  GBR_CUDA(hbao_launch(d_hbao_scenes_.as<HbaoScene>(), int(recs.size()), max_pixels, depth, color, q, q + fb,
+                       params, stream),
+           "Hbao launch");
+  // Readbacks of this draw now follow the effect.
+  GBR_CUDA(cudaEventRecord(upload_done_[slot_], stream), "Hbao: event");
+  upload_pending_[slot_] = true;
+  last_stream_ = stream;
   return GBR_OK;
 }
 

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/gbr.h"
+#include "../../include/gbr_hbao.h"
 #include "kernels.h"
 #include "records.h"
 
@@ -72,6 +73,7 @@ struct SceneState {
   std::vector<BatchKey> batches;
   float pv[16];
   float view[16];
+  float proj[16] = {};
   float unprojection[2] = {0, 0};
   int32_t width = 0, height = 0;
   int64_t fb_offset = 0, pitch = 0;
@@ -130,6 +132,8 @@ class Renderer {
 
   // -- drawing
   gbr_status draw(cudaStream_t stream, uint32_t mode, bool use_graph);
+  // Ambient occlusion on the colour plane of every enabled scene of the last draw.
+  gbr_status hbao(const gbr_hbao_config& c, cudaStream_t stream);
   gbr_status image_into(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes);
   gbr_status image_into_async(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes);
   gbr_status readback_wait();
@@ -195,6 +199,7 @@ class Renderer {
   DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_, d_normal_;
   DeviceBuffer d_lights_, d_model_;  // lit renderers: world lights, per-draw model data
   DeviceBuffer d_spill_;  // raster queue spill area, per CTA
+  DeviceBuffer d_hbao_scenes_, d_hbao_ao_;  // ambient occlusion: per-scene records, two 8-bit planes
   uint32_t max_lights_ = 0;
   DeviceBuffer d_meshes_, d_materials_, d_textures_, d_boxes_;
   DeviceBuffer d_scenes_, d_parents_, d_local_, d_draws_, d_cameras_;

@@ -621,11 +621,6 @@ ReplayRenderer* ReplayRenderer::create(const gbr_replay_config& c, gbr_status& s
     set_last_error("BatchReplayRenderer: only the standalone renderer exists (no GL framebuffer to draw into)");
     return nullptr;
   }
-  if (c.enable_hbao) {
-    st = GBR_ERROR_STATE;
-    set_last_error("BatchReplayRenderer: HBAO is not available");
-    return nullptr;
-  }
   if (c.resolution[0] <= 0 || c.resolution[1] <= 0 || c.resolution[0] > 16384 || c.resolution[1] > 16384) {
     set_last_error("ReplayRenderer: bad sensor resolution");
     return nullptr;
@@ -776,6 +771,11 @@ gbr_status ReplayRenderer::render(void* stream, uint32_t nc, void* const* color,
   const uint32_t mode = cfg_.draw_mode;
   if (gbr_status s = renderer_->draw(static_cast<cudaStream_t>(stream), mode, mode == GBR_DRAW_BATCHED))
     return s;
+  if (cfg_.enable_hbao) {  // the classic replay renderer's HBAO (ClassicReplayRenderer.cpp:142, 326)
+    gbr_hbao_config hc;
+    gbr_hbao_config_init(&hc);
+    if (gbr_status s = renderer_->hbao(hc, static_cast<cudaStream_t>(stream))) return s;
+  }
   const int32_t w = cfg_.resolution[1], h = cfg_.resolution[0];
   for (uint32_t i = 0; i < n; ++i) {
     const int32_t x0 = int32_t(i % uint32_t(grid_[0])) * w, y0 = int32_t(i / uint32_t(grid_[0])) * h;

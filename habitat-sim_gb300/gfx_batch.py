@@ -135,6 +135,83 @@ class RendererStandaloneConfiguration:
         return self
 
 
+class HbaoConfiguration:
+    """``HbaoConfiguration`` (src/esp/gfx_batch/Hbao.h:30-141): intensity,
+    bias, radius (metres), blur sharpness, NoBlur; the classic algorithm."""
+
+    def __init__(self):
+        self.intensity = 0.732
+        self.bias = 0.05
+        self.radius = 1.84
+        self.blur_sharpness = 10.0
+        self.no_blur = False
+        self.special_blur = False
+
+    def setNoBlur(self, state):
+        self.no_blur = bool(state)
+        if state:
+            self.special_blur = False
+        return self
+
+    def setUseSpecialBlur(self, state):
+        self.special_blur = bool(state)
+        if state:
+            self.no_blur = False
+        return self
+
+    def setIntensity(self, v):
+        self.intensity = float(v)
+        return self
+
+    def setBias(self, v):
+        self.bias = float(v)
+        return self
+
+    def setRadius(self, v):
+        self.radius = float(v)
+        return self
+
+    def setBlurSharpness(self, v):
+        self.blur_sharpness = float(v)
+        return self
+
+    def scaleIntensity(self, m):
+        self.intensity *= m
+        return self
+
+    def scaleBias(self, m):
+        self.bias *= m
+        return self
+
+    def scaleRadius(self, m):
+        self.radius *= m
+        return self
+
+    def scaleBlurSharpness(self, m):
+        self.blur_sharpness *= m
+        return self
+
+    def _c(self):
+        c = _lib.HbaoConfig()
+        c.intensity, c.bias, c.radius = self.intensity, self.bias, self.radius
+        c.blur_sharpness = self.blur_sharpness
+        c.no_blur, c.special_blur = int(self.no_blur), int(self.special_blur)
+        return c
+
+
+def hbaoApply(configuration, projection, linear_depth, color, stream=None):
+    """HBAO on one caller image: ``linear_depth`` float32 [h, w] and ``color``
+    uint8 [h, w, 4] CUDA torch tensors (rows contiguous; colour modified in place)."""
+    lib = _lib.load()
+    p = _f32(projection, (4, 4))
+    h, w = linear_depth.shape
+    if tuple(color.shape[:2]) != (h, w) or color.stride(0) != 4 * linear_depth.stride(0):
+        raise ValueError("colour and depth must have the same size and row pitch")
+    c = (configuration or HbaoConfiguration())._c()
+    check(lib.gbr_hbao_apply(ctypes.byref(c), _fptr(p), linear_depth.data_ptr(), color.data_ptr(),
+                             w, h, linear_depth.stride(0), _stream_handle(stream)))
+
+
 class SceneStats:
     """``SceneStats`` (Renderer.h:745-779)."""
 
@@ -582,6 +659,13 @@ class RendererStandalone:
 
     def colorTensor(self):
         return self.deviceTensor(Plane.Color)
+
+    def drawHbao(self, configuration=None, stream=None):
+        """``Hbao::drawEffect`` (classic) on every enabled scene of the last
+        draw: colour darkened in place from linear depth and each scene's
+        projection; asynchronous on `stream`."""
+        c = (configuration or HbaoConfiguration())._c()
+        check(self._lib.gbr_hbao_draw(self._h, ctypes.byref(c), _stream_handle(stream)))
 
     def depthTensor(self):
         return self.deviceTensor(Plane.Depth)

@@ -32,7 +32,8 @@ typedef struct gbr_replay_config {
   int32_t gpu_device_id;       /* default 0                                   */
   int32_t standalone;          /* must be 1: no GL framebuffer to draw into   */
   int32_t enable_frustum_culling; /* accepted; culling is always exact        */
-  int32_t enable_hbao;         /* must be 0                                   */
+  int32_t enable_hbao;         /* 1: ambient occlusion on the colour images
+                                  (gbr_hbao.h, default configuration)          */
   const char* sensor_uuid;     /* sensor name, default "rgba_camera"          */
   int32_t resolution[2];       /* {height, width}, default {128, 128}         */
   float hfov_degrees;          /* default 90                                  */

@@ -185,10 +185,6 @@ def test_replay_config_defaults_and_errors(lib, pkg):
     assert c.draw_mode == 1 and c.max_light_count == 0
     out = ctypes.c_void_p()
     assert lib.gbr_replay_create(None, ctypes.byref(out)) == 1
-    c.enable_hbao = 1
-    assert lib.gbr_replay_create(ctypes.byref(c), ctypes.byref(out)) == 7
-    assert b"HBAO" in lib.gbr_last_error()
-    c.enable_hbao = 0
     c.standalone = 0
     assert lib.gbr_replay_create(ctypes.byref(c), ctypes.byref(out)) == 7
     c.standalone = 1
