@@ -62,6 +62,8 @@ def parse():
     p.add_argument("--workload", default="config1", choices=["config1", "config2", "config3"],
                    help="config1 (the metric's workload) by default; config2/config3 for reference")
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--no-replay", action="store_true")
+    p.add_argument("--no-postprocess", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--serving-scenes", type=int, default=256)
     p.add_argument("--serving-requests", type=int, default=20000)
@@ -227,6 +229,97 @@ def serving_leg(pkg, args):
                                **keep(st))
     srv.close()
     return out
+
+
+def postprocess_leg(pkg, r, wl, stream, reps=10):
+    """Device time of the depth-noise model and of ambient occlusion over
+    every env of the last draw (CUDA events on the launching stream)."""
+    import torch
+    from habitat_sim_gb300 import noise
+    px = sum(w * h for (w, h) in wl.viewports)
+    m = noise.RedwoodNoiseModelGPUImpl(noise.load_model(), torch.cuda.current_device(), 1.0, seed=1)
+    dst = torch.empty_like(r.linearDepthTensor())
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    noise_ms = timed(lambda: m.apply_to_renderer(r, dst, stream.cuda_stream))
+    hbao_ms = timed(lambda: r.drawHbao(stream=stream))
+    m.close()
+    return {"pixels": px,
+            "redwood_noise": {"ms": noise_ms, "Gpx_per_s": px / noise_ms / 1e6,
+                              "GB_per_s": 8 * px / noise_ms / 1e6,
+                              "bytes_per_pixel": 8, "launches": 1},
+            "hbao": {"ms": hbao_ms, "Gpx_per_s": px / hbao_ms / 1e6,
+                     "GB_per_s": 24 * px / hbao_ms / 1e6, "bytes_per_pixel": 24, "launches": 3,
+                     "note": "bytes: depth read by each of the 3 passes, 8-bit AO written and "
+                             "read twice, colour read and written; the AO pass's 36 neighbour "
+                             "depth reads per pixel are served by L1/L2"}}
+
+
+def replay_leg(pkg, procedural, wl, steps=5, warmup=2):
+    """The replay path (BatchReplayRenderer through keyframes): every env is
+    created from a scene keyframe, then each step applies one serialized
+    camera keyframe per env (C++ parse + apply + camera from the user
+    transform) and renders every env's colour and metres depth into pinned
+    host images."""
+    import torch
+    cfg = pkg.ReplayRendererConfiguration()
+    cfg.num_environments = wl.envs
+    w, h = wl.viewports[0]
+    cfg.sensor_specifications = [pkg.CameraSensorSpec(resolution=(h, w), hfov=float(wl.hfov[0]),
+                                                      near=procedural.NEAR, far=procedural.FAR)]
+    cfg.quiet = True
+    rr = pkg.ReplayRenderer.create_batch_replay_renderer(cfg)
+    procedural.add_resources(rr.renderer, wl)
+    t0 = time.perf_counter()
+    scene_kf = [procedural.scene_keyframe(pkg, wl, s).to_string() for s in range(len(wl.instances))]
+    for e in range(wl.envs):
+        rr.set_environment_keyframe(e, scene_kf[wl.scene_of_env[e]])
+    load_s = time.perf_counter() - t0
+    n = warmup + steps
+    cams = []
+    for i in range(n):
+        _, views = procedural.camera_poses(wl, 2000 + i)
+        cams.append([procedural.camera_keyframe(pkg, views[e]).to_string() for e in range(wl.envs)])
+    big_c = torch.empty((wl.envs, h, w, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    big_d = torch.empty((wl.envs, h, w), dtype=torch.float32, pin_memory=True).numpy()
+    colors, depths = list(big_c), list(big_d)
+    apply_s, render_s = [], []
+
+    def step(i):
+        t = time.perf_counter()
+        for e in range(wl.envs):
+            rr.set_environment_keyframe(e, cams[i][e])
+            rr.set_sensor_transforms_from_keyframe(e, "sensor_")
+        t1 = time.perf_counter()
+        rr.render(colors, depths)
+        return t1 - t, time.perf_counter() - t1
+
+    for i in range(warmup):
+        step(i)
+    for i in range(warmup, n):
+        a, b = step(i)
+        apply_s.append(a)
+        render_s.append(b)
+    total = sum(apply_s) + sum(render_s)
+    rr.close()
+    return {"value": wl.envs * steps / total, "unit": "frames/s", "envs": wl.envs, "steps": steps,
+            "ms_per_step": 1e3 * total / steps,
+            "keyframe_apply_ms": 1e3 * statistics.mean(apply_s),
+            "render_ms": 1e3 * statistics.mean(render_s),
+            "scene_load_s": load_s,
+            "d2h_bytes_per_step": int(big_c.nbytes + big_d.nbytes),
+            "timing": "host clock: per env set_environment_keyframe + "
+                      "set_sensor_transforms_from_keyframe, then render() into pinned host images"}
 
 
 def run_reference_impl(args):
@@ -444,7 +537,11 @@ def main():
             if line.startswith("dram_bytes_per_launch:"):
                 traffic = float(line.split(":")[1])
 
+    post = None if args.no_postprocess else postprocess_leg(pkg, r, wl, stream)
     serving = None if args.no_serving else serving_leg(pkg, args)
+    replay = None
+    if not args.no_replay and wl.uniform:
+        replay = replay_leg(pkg, procedural, wl)
 
     cpu_baseline = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -496,6 +593,8 @@ def main():
             "parity": parity,
             "cpu_baseline": cpu_baseline,
             "serving": serving,
+            "replay": replay,
+            "postprocess": post,
         }
         print(json.dumps(line))
     r.close()

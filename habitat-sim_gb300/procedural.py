@@ -442,8 +442,9 @@ def camera_poses(wl, step=0):
 
 
 # ----------------------------------------------------------------- builders
-def populate(r, wl, envs=None):
-    """Add the workload's resources and per-env hierarchies to renderer r."""
+def add_resources(r, wl):
+    """Add the workload's textures, meshes, materials and named hierarchy
+    templates to renderer r (no scene content)."""
     tex = [r.addTexture(t["pixels"], t["filter"], t["wrap_s"], t["wrap_t"]) for t in wl.textures]
     meshes = [r.addMesh(m["positions"], m["colors"], m["texcoords"], m["object_ids"], m["indices"])
               for m in wl.meshes]
@@ -451,12 +452,56 @@ def populate(r, wl, envs=None):
     for name, views in wl.templates:
         r.addNodeHierarchyTemplate(name, [(meshes[m], off, cnt, mats[mt], None)
                                           for (m, off, cnt, mt) in views])
+
+
+def populate(r, wl, envs=None):
+    """Add the workload's resources and per-env hierarchies to renderer r."""
+    add_resources(r, wl)
     env_list = range(wl.envs) if envs is None else envs
     for slot, e in enumerate(env_list):
         for (tmpl, bake, sid) in wl.instances[wl.scene_of_env[e]]:
             node = r.addNodeHierarchy(slot, tmpl, bake)
             if sid:
                 r.setSemanticId(slot, node, sid)
+
+
+def scene_keyframe(pkg, wl, scene):
+    """The gfx-replay keyframe that creates one scene's instances: a load
+    and a creation per instance (hierarchy template name, uniform scale), a
+    state update with the instance's translation and yaw, and its semantic
+    id as metadata."""
+    k = pkg.Keyframe()
+    for name, _ in wl.templates:
+        k.load(name)
+    for key, (tmpl, bake, sid) in enumerate(wl.instances[scene]):
+        b = np.eye(4) if bake is None else np.asarray(bake, np.float64)
+        scale = float(np.linalg.norm(b[1, :3]))
+        yaw = math.atan2(float(b[2, 0]), float(b[0, 0]))
+        k.create(key, tmpl, scale=(scale, scale, scale))
+        k.update(key, tuple(float(v) for v in b[3, :3]), (0.0, math.sin(yaw / 2), 0.0, math.cos(yaw / 2)))
+        if sid:
+            k.set_metadata(key, sid, sid)
+    return k
+
+
+def camera_keyframe(pkg, view, name="sensor_rgba_camera"):
+    """A keyframe carrying only the camera pose (the inverse of `view`) as
+    the user transform `name`."""
+    m = np.linalg.inv(np.asarray(view, np.float64).T)     # row-major camera-to-world
+    r = m[:3, :3]
+    w = math.sqrt(max(0.0, 1.0 + r[0, 0] + r[1, 1] + r[2, 2])) / 2
+    if w > 1e-6:
+        q = ((r[2, 1] - r[1, 2]) / (4 * w), (r[0, 2] - r[2, 0]) / (4 * w), (r[1, 0] - r[0, 1]) / (4 * w), w)
+    else:   # 180-degree turn: largest diagonal element
+        i = int(np.argmax(np.diag(r)))
+        j, k_ = (i + 1) % 3, (i + 2) % 3
+        s = math.sqrt(max(0.0, 1.0 + r[i, i] - r[j, j] - r[k_, k_])) * 2
+        qv = [0.0, 0.0, 0.0]
+        qv[i] = s / 4
+        qv[j] = (r[j, i] + r[i, j]) / s
+        qv[k_] = (r[k_, i] + r[i, k_]) / s
+        q = (qv[0], qv[1], qv[2], (r[k_, j] - r[j, k_]) / s)
+    return pkg.Keyframe().user_transform(name, tuple(m[:3, 3]), q)
 
 
 def grid_for(n):
