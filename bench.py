@@ -265,7 +265,7 @@ def postprocess_leg(pkg, r, wl, stream, reps=10):
                              "depth reads per pixel are served by L1/L2"}}
 
 
-def replay_leg(pkg, procedural, wl, steps=5, warmup=2):
+def replay_leg(pkg, procedural, wl, tuning, steps=5, warmup=2):
     """The replay path (BatchReplayRenderer through keyframes): every env is
     created from a scene keyframe, then each step applies one serialized
     camera keyframe per env (C++ parse + apply + camera from the user
@@ -279,6 +279,7 @@ def replay_leg(pkg, procedural, wl, steps=5, warmup=2):
                                                       near=procedural.NEAR, far=procedural.FAR)]
     cfg.quiet = True
     rr = pkg.ReplayRenderer.create_batch_replay_renderer(cfg)
+    rr.renderer.setTuning(**tuning)      # the batched leg's (autotuned) launch shape
     procedural.add_resources(rr.renderer, wl)
     t0 = time.perf_counter()
     scene_kf = [procedural.scene_keyframe(pkg, wl, s).to_string() for s in range(len(wl.instances))]
@@ -292,7 +293,6 @@ def replay_leg(pkg, procedural, wl, steps=5, warmup=2):
         cams.append([procedural.camera_keyframe(pkg, views[e]).to_string() for e in range(wl.envs)])
     big_c = torch.empty((wl.envs, h, w, 4), dtype=torch.uint8, pin_memory=True).numpy()
     big_d = torch.empty((wl.envs, h, w), dtype=torch.float32, pin_memory=True).numpy()
-    colors, depths = list(big_c), list(big_d)
     apply_s, render_s = [], []
 
     def step(i):
@@ -301,7 +301,7 @@ def replay_leg(pkg, procedural, wl, steps=5, warmup=2):
             rr.set_environment_keyframe(e, cams[i][e])
             rr.set_sensor_transforms_from_keyframe(e, "sensor_")
         t1 = time.perf_counter()
-        rr.render(colors, depths)
+        rr.render(big_c, big_d)
         return t1 - t, time.perf_counter() - t1
 
     for i in range(warmup):
@@ -541,7 +541,7 @@ def main():
     serving = None if args.no_serving else serving_leg(pkg, args)
     replay = None
     if not args.no_replay and wl.uniform:
-        replay = replay_leg(pkg, procedural, wl)
+        replay = replay_leg(pkg, procedural, wl, r.tuning())
 
     cpu_baseline = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -125,6 +125,7 @@ PROTOTYPES = {
     "gbr_color_image_into": (_ST, [_P, ctypes.POINTER(_I32), _P, _U64]),
     "gbr_image_into_async": (_ST, [_P, _U32, ctypes.POINTER(_I32), _P, _U64]),
     "gbr_readback_wait": (_ST, [_P]),
+    "gbr_scenes_into_async": (_ST, [_P, _U32, _U32, _U32, _P]),
     "gbr_depth_image_into": (_ST, [_P, ctypes.POINTER(_I32), _P, _U64]),
     "gbr_scene_image_into": (_ST, [_P, _U32, _U32, _P, _U64]),
     "gbr_plane_device_pointer": (_ST, [_P, _U32, ctypes.POINTER(_P), ctypes.POINTER(_U64)]),

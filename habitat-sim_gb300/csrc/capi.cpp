@@ -427,6 +427,13 @@ gbr_status gbr_set_kernel_timing(gbr_renderer* r, int32_t enabled) {
   return R(r)->set_kernel_timing(enabled != 0);
 }
 
+gbr_status gbr_scenes_into_async(gbr_renderer* r, uint32_t plane, uint32_t first, uint32_t count,
+                                 void* dst) {
+  GBR_HANDLE(r);
+  GBR_ARG(dst);
+  return guarded([&] { return R(r)->scenes_into_async(plane, first, count, dst); });
+}
+
 gbr_status gbr_hbao_draw(gbr_renderer* r, const gbr_hbao_config* config, void* stream) {
   GBR_HANDLE(r);
   GBR_ARG(config);

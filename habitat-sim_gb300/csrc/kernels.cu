@@ -28,6 +28,8 @@
 //     the unclipped triangle (Olano & Greer 1997).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstdint>
 
 #include "kernels.h"
@@ -1307,7 +1309,47 @@ __global__ void unproject_kernel(float a, float b, float* depth, uint64_t rows, 
   }
 }
 
+// Tiles of a plane packed one after another: scene i of the tile grid
+// (tile (i % tiles_x, i / tiles_x), w x h elements of 4 bytes) goes to
+// dst[i * w * h ...], rows kept in order.  One thread per 16 bytes when the
+// rows are 16-byte multiples, else per element.
+template <int Vec>
+__global__ void gather_tiles_kernel(const uint32_t* __restrict__ src, int64_t pitch, int w, int h,
+                                    int tiles_x, uint32_t first, uint64_t units, uint32_t* dst) {
+  const int per_row = w / Vec;
+  for (uint64_t u = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; u < units;
+       u += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t row = u / per_row;            // scene-major rows
+    const int c = int(u % per_row) * Vec;
+    const uint32_t scene = first + uint32_t(row / h);
+    const int y = int(row % h);
+    const int64_t sx = int64_t(scene % uint32_t(tiles_x)) * w, sy = int64_t(scene / uint32_t(tiles_x)) * h;
+    const uint32_t* from = src + (sy + y) * pitch + sx + c;
+    uint32_t* to = dst + row * uint64_t(w) + c;
+    if (Vec == 4)
+      *reinterpret_cast<uint4*>(to) = __ldg(reinterpret_cast<const uint4*>(from));
+    else
+      *to = __ldg(from);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_gather_tiles(const void* src, int64_t pitch, int w, int h, int tiles_x, uint32_t first,
+                                uint32_t count, void* dst, cudaStream_t stream) {
+  const bool vec = (w % 4 == 0) && (pitch % 4 == 0) && (reinterpret_cast<uintptr_t>(src) % 16 == 0) &&
+                   (reinterpret_cast<uintptr_t>(dst) % 16 == 0);
+  const uint64_t units = uint64_t(count) * h * (vec ? w / 4 : w);
+  if (units == 0) return cudaSuccess;
+  const unsigned blocks = unsigned(std::min<uint64_t>((units + 255) / 256, 152ull * 32));
+  if (vec)
+    gather_tiles_kernel<4><<<blocks, 256, 0, stream>>>(static_cast<const uint32_t*>(src), pitch, w, h,
+                                                       tiles_x, first, units, static_cast<uint32_t*>(dst));
+  else
+    gather_tiles_kernel<1><<<blocks, 256, 0, stream>>>(static_cast<const uint32_t*>(src), pitch, w, h,
+                                                       tiles_x, first, units, static_cast<uint32_t*>(dst));
+  return cudaGetLastError();
+}
 
 cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStream_t stream) {
   if (scene_count == 0) return cudaSuccess;

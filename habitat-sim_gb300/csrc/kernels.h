@@ -94,5 +94,10 @@ cudaError_t launch_raster(const RasterParams& p, int threads, uint32_t grid, siz
 cudaError_t raster_max_ctas_per_sm(int threads, size_t smem, int* out);
 cudaError_t launch_unproject(float a, float b, float* depth, uint64_t rows, uint64_t cols,
                              uint64_t row_stride, cudaStream_t stream);
+// Packs scenes [first, first + count) of a tile-grid plane of 4-byte
+// elements (row pitch `pitch` elements, tiles w x h, tiles_x per row) into
+// dst, one scene after another.
+cudaError_t launch_gather_tiles(const void* src, int64_t pitch, int w, int h, int tiles_x, uint32_t first,
+                                uint32_t count, void* dst, cudaStream_t stream);
 
 }  // namespace gbr

@@ -111,9 +111,23 @@ __global__ void __launch_bounds__(256) redwood_kernel(TileArgs a) {
                                   __fmul_rn(w, __ldg(cell + min(max(i2, 0), 4))));
         const float ud = f < 1e-5f ? 0.0f : __fdiv_rn(d, f);
         if (ud != 0.0f) {
-          const double q = (double(35.130f) / double(ud) +
-                            double(__fmul_rn(__fmul_rn(n2, 0.027778f), a.mult))) * 8.0;
-          const float denom = float(round(q));
+          // round((35.130 / d' + noise) * 8) is defined in double.  The float
+          // evaluation differs from it by less than `margin` (three roundings
+          // of at most 2^-24 relative each), so it rounds to the same integer
+          // unless it lies within the margin of a half; only those pixels
+          // take the double path (FP64 throughput is low on this part).
+          const float nz = __fmul_rn(__fmul_rn(n2, 0.027778f), a.mult);
+          const float inv = __fdiv_rn(35.130f, ud);
+          const float qf = __fmul_rn(__fadd_rn(inv, nz), 8.0f);
+          const float margin = __fmul_rn(1e-6f, __fadd_rn(fabsf(qf), __fmul_rn(8.0f, fabsf(nz))));
+          const float frac = fabsf(__fsub_rn(qf, truncf(qf)));
+          float denom;
+          if (fabsf(__fsub_rn(frac, 0.5f)) > margin && isfinite(qf)) {
+            denom = roundf(qf);
+          } else {
+            const double q = (double(35.130f) / double(ud) + double(nz)) * 8.0;
+            denom = float(round(q));
+          }
           out = denom > 1e-5f ? __fdiv_rn(35.130f * 8.0f, denom) : 0.0f;
         }
       }

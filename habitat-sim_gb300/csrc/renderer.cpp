@@ -1412,6 +1412,50 @@ gbr_status Renderer::hbao(const gbr_hbao_config& c, cudaStream_t stream) {
   return GBR_OK;
 }
 
+gbr_status Renderer::scenes_into_async(uint32_t plane, uint32_t first, uint32_t count, void* dst) {
+  size_t elem;
+  const char* src = static_cast<const char*>(plane_ptr(plane, &elem));
+  if (!src) return fail(GBR_ERROR_INVALID_ARGUMENT, "scenesIntoAsync: plane not enabled");
+  if (uint64_t(first) + count > scenes_.size())
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "scenesIntoAsync: scene range out of bounds");
+  if (count == 0) return GBR_OK;
+  const SceneState& s0 = scenes_[first];
+  for (uint32_t i = first; i < first + count; ++i)
+    if (scenes_[i].width != s0.width || scenes_[i].height != s0.height)
+      return fail(GBR_ERROR_INVALID_ARGUMENT, "scenesIntoAsync: the scenes differ in size");
+  const size_t bytes = size_t(count) * size_t(s0.width) * size_t(s0.height) * elem;
+  cudaSetDevice(device_);
+  if (!copy_stream_) {
+    GBR_CUDA(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking), "copy stream");
+    for (auto& e : copy_done_)
+      GBR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy event");
+  }
+  if (upload_pending_[slot_])
+    GBR_CUDA(cudaStreamWaitEvent(copy_stream_, upload_done_[slot_], 0), "wait for draw");
+  if (ragged_) {  // scenes are consecutive blocks: one copy
+    GBR_CUDA(cudaMemcpyAsync(dst, src + size_t(s0.fb_offset) * elem, bytes, cudaMemcpyDefault, copy_stream_),
+             "scenesIntoAsync copy");
+  } else {
+    cudaPointerAttributes attr{};
+    const bool device_dst = cudaPointerGetAttributes(&attr, dst) == cudaSuccess &&
+                            attr.type == cudaMemoryTypeDevice && attr.device == device_;
+    cudaGetLastError();  // a host pointer is not an error
+    void* packed = dst;
+    if (!device_dst) {
+      if (!d_gather_.reserve(bytes, false)) return fail(GBR_ERROR_OUT_OF_MEMORY, "scenesIntoAsync: staging");
+      packed = d_gather_.ptr;
+    }
+    GBR_CUDA(launch_gather_tiles(src, fb_w_, cfg_.tile_size[0], cfg_.tile_size[1], cfg_.tile_count[0], first,
+                                 count, packed, copy_stream_),
+             "scenesIntoAsync gather");
+    if (!device_dst)
+      GBR_CUDA(cudaMemcpyAsync(dst, packed, bytes, cudaMemcpyDeviceToHost, copy_stream_), "scenesIntoAsync copy");
+  }
+  GBR_CUDA(cudaEventRecord(copy_done_[front_], copy_stream_), "copy event");
+  copy_pending_[front_] = true;
+  return GBR_OK;
+}
+
 gbr_status Renderer::readback_wait() {
   if (!copy_stream_) return GBR_OK;
   cudaSetDevice(device_);

@@ -137,6 +137,9 @@ class Renderer {
   gbr_status image_into(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes);
   gbr_status image_into_async(uint32_t plane, const int32_t* rect, void* dst, uint64_t row_bytes);
   gbr_status readback_wait();
+  // Scenes [first, first + count) of a plane packed one after another into
+  // dst (host or device), asynchronously on the copy stream.
+  gbr_status scenes_into_async(uint32_t plane, uint32_t first, uint32_t count, void* dst);
   gbr_status scene_image_into(uint32_t plane, uint32_t scene, void* dst, uint64_t row_bytes);
   gbr_status plane_pointer(uint32_t plane, void** out, uint64_t* bytes);
   gbr_status plane_dlpack(uint32_t plane, void** out);
@@ -199,6 +202,7 @@ class Renderer {
   DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_, d_normal_;
   DeviceBuffer d_lights_, d_model_;  // lit renderers: world lights, per-draw model data
   DeviceBuffer d_spill_;  // raster queue spill area, per CTA
+  DeviceBuffer d_gather_;  // packed scenes on their way to host memory
   DeviceBuffer d_hbao_scenes_, d_hbao_ao_;  // ambient occlusion: per-scene records, two 8-bit planes
   uint32_t max_lights_ = 0;
   DeviceBuffer d_meshes_, d_materials_, d_textures_, d_boxes_;

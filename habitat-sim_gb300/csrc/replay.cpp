@@ -777,12 +777,26 @@ gbr_status ReplayRenderer::render(void* stream, uint32_t nc, void* const* color,
     if (gbr_status s = renderer_->hbao(hc, static_cast<cudaStream_t>(stream))) return s;
   }
   const int32_t w = cfg_.resolution[1], h = cfg_.resolution[0];
-  for (uint32_t i = 0; i < n; ++i) {
+  // Destinations that are one packed array (environment i at base + i
+  // images, rows without padding) take one gather and one copy per plane.
+  auto packed = [&](void* const* d, uint32_t count, uint64_t row, size_t elem) {
+    if (!count || row != uint64_t(w) * elem) return false;
+    const size_t image = size_t(h) * row;
+    for (uint32_t i = 1; i < count; ++i)
+      if (static_cast<char*>(d[i]) != static_cast<char*>(d[0]) + i * image) return false;
+    return true;
+  };
+  const bool pc = packed(color, nc, crow, 4), pd = packed(depth, nd, drow, 4);
+  if (pc)
+    if (gbr_status s = renderer_->scenes_into_async(GBR_PLANE_COLOR, 0, n, color[0])) return s;
+  if (pd)
+    if (gbr_status s = renderer_->scenes_into_async(GBR_PLANE_LINEAR_DEPTH, 0, n, depth[0])) return s;
+  for (uint32_t i = 0; i < n && (!pc || !pd); ++i) {
     const int32_t x0 = int32_t(i % uint32_t(grid_[0])) * w, y0 = int32_t(i / uint32_t(grid_[0])) * h;
     const int32_t rect[4] = {x0, y0, x0 + w, y0 + h};
-    if (nc)
+    if (nc && !pc)
       if (gbr_status s = renderer_->image_into_async(GBR_PLANE_COLOR, rect, color[i], crow)) return s;
-    if (nd)
+    if (nd && !pd)
       if (gbr_status s = renderer_->image_into_async(GBR_PLANE_LINEAR_DEPTH, rect, depth[i], drow)) return s;
   }
   return renderer_->readback_wait();

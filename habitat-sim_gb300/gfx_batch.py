@@ -596,6 +596,21 @@ class RendererStandalone:
     def readbackWait(self):
         check(self._lib.gbr_readback_wait(self._h))
 
+    def scenesIntoAsync(self, plane, first, count, out):
+        """Start packing scenes [first, first + count) of a plane of the last
+        draw into ``out`` -- a C-contiguous [count, h, w(, 4)] numpy array
+        (host; pinned for full speed) or CUDA torch tensor -- and return at
+        once; ``readbackWait()`` waits."""
+        if hasattr(out, "data_ptr"):
+            if not out.is_contiguous():
+                raise GbrError(1, "out must be contiguous")
+            ptr = out.data_ptr()
+        else:
+            if not out.flags.c_contiguous:
+                raise GbrError(1, "out must be C-contiguous")
+            ptr = out.ctypes.data
+        check(self._lib.gbr_scenes_into_async(self._h, int(plane), int(first), int(count), ptr))
+
     def colorImageInto(self, rectangle, image):
         """``colorImageInto`` (RendererStandalone.cpp:168-180); rectangle is
         ((x0, y0), (x1, y1)), image a uint8 [y1-y0, x1-x0, 4] array."""

@@ -271,17 +271,16 @@ class ReplayRenderer:
         ``color_images[i]`` ([h, w, 4] or [h, w, 3] uint8) and its depth in
         metres to ``depth_images[i]`` ([h, w] float32).  Destinations are
         numpy arrays or CUDA torch tensors with contiguous rows; either list
-        may be empty.  Returns when the copies are complete."""
-        if isinstance(color_images, (list, tuple)) is False and color_images is not None:
-            color_images = list(color_images)
-        if isinstance(depth_images, (list, tuple)) is False and depth_images is not None:
-            depth_images = list(depth_images)
-        color_images = list(color_images or ())
-        depth_images = list(depth_images or ())
+        may be empty.  One packed array per output ([environments, h, w, 4]
+        uint8, [environments, h, w] float32) is the fast form: one gather and
+        one copy per plane.  Returns when the copies are complete."""
         h, w = self._res
+        cptr, crow = self._packed(color_images, (h, w, 4), np.uint8, "color")
+        dptr, drow = self._packed(depth_images, (h, w), np.float32, "depth")
+        color_images = [] if cptr is not None else list(color_images or ())
+        depth_images = [] if dptr is not None else list(depth_images or ())
         rgb_fixups = []
-        cptr = []
-        crow = 0
+        cptr = cptr if cptr is not None else []
         for i, img in enumerate(color_images):
             ptr, row, channels = self._dst(img, h, w, (3, 4), np.uint8, "color")
             if channels == 3:
@@ -292,8 +291,7 @@ class ReplayRenderer:
                 raise ValueError("color images must share one row pitch")
             crow = row
             cptr.append(ptr)
-        dptr = []
-        drow = 0
+        dptr = dptr if dptr is not None else []
         for i, img in enumerate(depth_images):
             ptr, row, _ = self._dst(img, h, w, (1,), np.float32, "depth")
             if i and row != drow:
@@ -308,6 +306,22 @@ class ReplayRenderer:
         check(self._lib.gbr_replay_render(self._h, s, len(cptr), carr, crow, len(dptr), darr, drow))
         for img, tmp in rgb_fixups:
             img[...] = tmp[..., :3]
+
+    def _packed(self, images, shape, dtype, what):
+        """Pointers of every environment's image when `images` is one packed
+        [environments, ...] array or tensor (validated once), else (None, 0)."""
+        if images is None or isinstance(images, (list, tuple)) or getattr(images, "ndim", 0) != len(shape) + 1:
+            return None, 0
+        if images.shape[0] != self._n:
+            raise ValueError(f"expected {self._n} {what} images, got {images.shape[0]}")
+        ptr, row, _ = self._dst(images[0], *shape[:2], (shape[2] if len(shape) == 3 else 1,), dtype, what)
+        if hasattr(images, "data_ptr"):
+            contiguous, base, step = images.is_contiguous(), images.data_ptr(), images.stride(0) * images.element_size()
+        else:
+            contiguous, base, step = images.flags.c_contiguous, images.ctypes.data, images.strides[0]
+        if not contiguous:
+            raise ValueError(f"packed {what} images must be contiguous")
+        return [base + i * step for i in range(self._n)], row
 
     @staticmethod
     def _dst(img, h, w, channels, dtype, what):

@@ -243,6 +243,14 @@ gbr_status gbr_image_into_async(gbr_renderer* r, uint32_t plane, const int32_t r
                                 uint64_t dst_row_bytes);
 /* Wait for every readback enqueued so far (not for later draws). */
 gbr_status gbr_readback_wait(gbr_renderer* r);
+/* Asynchronous batched readback: scenes [first, first + count) of a plane
+ * of the last draw, all of one size, packed one after another (scene after
+ * scene, rows bottom-up, width elements per row) into dst -- host memory
+ * (through one device-side gather and one copy) or device memory on the
+ * renderer's GPU (gathered in place).  Same lifetime rule as
+ * gbr_image_into_async. */
+gbr_status gbr_scenes_into_async(gbr_renderer* r, uint32_t plane, uint32_t first, uint32_t count,
+                                 void* dst);
 
 /* Renderer::sceneStats (Renderer.cpp:1356-1375). */
 typedef struct gbr_scene_stats_info {

@@ -415,6 +415,36 @@ def test_double_buffer_async_readback(pkg, procedural, graph):
                           rag.sceneImage(pkg.Plane.Color, 3))
 
 
+@pytest.mark.parametrize("ragged", [False, True], ids=["tiles", "ragged"])
+def test_scenes_into_async(pkg, procedural, ragged):
+    """Packed batched readback into host arrays and device tensors equals
+    the per-scene readback, for a sub-range of scenes."""
+    import torch
+    wl = procedural.config0(seed=7, envs=7, resolution=40, room_subdiv=4, boxes=3)
+    if ragged:
+        wl.viewports = [(40, 40)] * wl.envs
+        wl.uniform = False
+    r = procedural.build_renderer(pkg, wl)
+    procedural.set_cameras(r, wl, procedural.camera_poses(wl, 2))
+    r.draw()
+    first, count = 2, 5
+    for plane, dt, shape in ((pkg.Plane.Color, np.uint8, (40, 40, 4)),
+                             (pkg.Plane.LinearDepth, np.float32, (40, 40)),
+                             (pkg.Plane.Semantic, np.uint32, (40, 40))):
+        host = np.zeros((count,) + shape, dt)
+        r.scenesIntoAsync(plane, first, count, host)
+        tdt = {np.uint8: torch.uint8, np.float32: torch.float32, np.uint32: torch.int32}[dt]
+        dev = torch.zeros((count,) + shape, dtype=tdt, device="cuda")
+        r.scenesIntoAsync(plane, first, count, dev)
+        r.readbackWait()
+        for i in range(count):
+            want = r.sceneImage(plane, first + i)
+            assert np.array_equal(host[i], want)
+            assert np.array_equal(dev[i].cpu().numpy().view(dt), want)
+    with pytest.raises(pkg.GbrError):
+        r.scenesIntoAsync(pkg.Plane.Color, 5, 5, np.zeros((5, 40, 40, 4), np.uint8))
+
+
 def test_unproject_device_matches_host(pkg):
     import torch
     p = S.perspective(60.0, 1.0, 0.01, 10.0)

@@ -178,6 +178,41 @@ def test_replay_tensor_destinations(pkg):
     gpu.close()
 
 
+def test_replay_packed_destinations(pkg):
+    """Views of one packed array (host or device) take the gather path and
+    give the same images as separate destinations."""
+    import torch
+    n, res = 5, (24, 40)
+    gpu, _ = make_pair(pkg, n, res)
+    for e in range(n):
+        k, _ = scene_keyframes(pkg, e)
+        gpu.set_environment_keyframe(e, k.to_string())
+        gpu.set_sensor_transforms_from_keyframe(e, "sensor_")
+    sep_c = [np.zeros(res + (4,), np.uint8) for _ in range(n)]
+    sep_d = [np.zeros(res, np.float32) for _ in range(n)]
+    gpu.render(sep_c, sep_d)
+    big_c = np.zeros((n,) + res + (4,), np.uint8)
+    big_d = np.zeros((n,) + res, np.float32)
+    gpu.render(list(big_c), list(big_d))
+    dev_c = torch.zeros((n,) + res + (4,), dtype=torch.uint8, device="cuda")
+    dev_d = torch.zeros((n,) + res, dtype=torch.float32, device="cuda")
+    gpu.render(list(dev_c), list(dev_d))
+    for e in range(n):
+        assert np.array_equal(big_c[e], sep_c[e]) and np.array_equal(big_d[e], sep_d[e])
+        assert np.array_equal(dev_c[e].cpu().numpy(), sep_c[e])
+        assert np.array_equal(dev_d[e].cpu().numpy(), sep_d[e])
+    # The packed arrays themselves (validated once, one gather per plane).
+    big_c[...] = 0
+    dev_d.zero_()
+    gpu.render(big_c, dev_d)
+    for e in range(n):
+        assert np.array_equal(big_c[e], sep_c[e])
+        assert np.array_equal(dev_d[e].cpu().numpy(), sep_d[e])
+    with pytest.raises(ValueError):
+        gpu.render(np.zeros((n - 1,) + res + (4,), np.uint8))
+    gpu.close()
+
+
 def test_unproject_matches_classic_rays(pkg):
     """testUnproject's rays (BatchReplayRendererTest.cpp:210-255): sensor at
     (1, 2, 3), 512 x 384 (height x width), hfov 90."""
