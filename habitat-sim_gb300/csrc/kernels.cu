@@ -595,11 +595,18 @@ __device__ __forceinline__ float4 lerp_clip(const float4& in, const float4& out,
                      fma_(t, __fsub_rn(out.z, in.z), in.z), fma_(t, __fsub_rn(out.w, in.w), in.w));
 }
 
-__device__ __noinline__ void clip_and_emit(const float4* c3, uint32_t ordinal, const Ctx& c,
-                                           float gx, float gy) {
+// Out of line, the vertices taken by value: an array address passed to the
+// call would place the caller's vertices in local memory for every triangle,
+// not only for the few that are clipped.  (The context stays a reference: it
+// is stored once per work item, and copying it for the call costs registers.)
+__device__ __noinline__ void clip_and_emit(float4 v0, float4 v1, float4 v2, uint32_t ordinal,
+                                           const Ctx& c) {
+  const float gx = c.gx, gy = c.gy;
   float4 poly[9], next[9];
   int n = 3;
-  for (int i = 0; i < 3; ++i) poly[i] = c3[i];
+  poly[0] = v0;
+  poly[1] = v1;
+  poly[2] = v2;
   for (int p = 0; p < 5 && n >= 3; ++p) {
     int m = 0;
     for (int i = 0; i < n; ++i) {
@@ -637,7 +644,7 @@ __device__ __forceinline__ void triangle(const float4* cv, uint32_t ordinal, con
   if (!need_clip)
     emit(cv, ordinal, c);
   else
-    clip_and_emit(cv, ordinal, c, gx, gy);
+    clip_and_emit(cv[0], cv[1], cv[2], ordinal, c);
 }
 
 // Largest d in [0, n) with ordinal(d) <= g.
@@ -730,17 +737,23 @@ __device__ __forceinline__ uint32_t unorm8(float c) {
 // N = the normalised interpolation of the vertices' normal-matrix normals,
 // the fragment's world position the interpolation of theirs.  Alpha is the
 // diffuse alpha.
-__device__ __noinline__ uint32_t lit_color(const RasterParams& p, const MaterialRec& mat,
-                                           const float tc[4], const float vc[4],
+// Out of line (the unlit path keeps its registers) and taking its inputs by
+// value: an address passed to a call would place the caller's arrays in
+// local memory for every shaded pixel.
+__device__ __noinline__ uint32_t lit_color(const float4* __restrict__ vertex_normals, float ambient_factor,
+                                           const MaterialRec& mat, float4 tc4, float4 vc4,
                                            const WorldLight* lights, uint32_t nl,
-                                           const ModelRec* model, const uint32_t v[3],
-                                           const float4 q[3], float b0, float b1, float b2,
+                                           const ModelRec* model, uint32_t v0, uint32_t v1, uint32_t v2,
+                                           float4 q0, float4 q1, float4 q2, float b0, float b1, float b2,
                                            bool normals) {
 #define GBR_INTERP(a0, a1, a2) fma_(b2, (a2), fma_(b1, (a1), __fmul_rn(b0, (a0))))
+  const float tc[4] = {tc4.x, tc4.y, tc4.z, tc4.w}, vc[4] = {vc4.x, vc4.y, vc4.z, vc4.w};
+  const uint32_t v[3] = {v0, v1, v2};
+  const float4 q[3] = {q0, q1, q2};
   float amb[4], dif[4], rgb[3];
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    amb[c] = __fmul_rn(__fmul_rn(__fmul_rn(mat.color[c], p.ambient_factor), tc[c]), vc[c]);
+    amb[c] = __fmul_rn(__fmul_rn(__fmul_rn(mat.color[c], ambient_factor), tc[c]), vc[c]);
     dif[c] = __fmul_rn(__fmul_rn(mat.color[c], tc[c]), vc[c]);
   }
 #pragma unroll
@@ -754,7 +767,7 @@ __device__ __noinline__ uint32_t lit_color(const RasterParams& p, const Material
     float wp[3][3], wn[3][3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const float4 n = __ldg(&p.normals[v[k]]);
+      const float4 n = __ldg(&vertex_normals[v[k]]);
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
         float t = A[9 + r];
@@ -888,8 +901,9 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
   }
 #undef GBR_INTERP
   if (p.max_lights > 0 && mat.phong) {
-    color = lit_color(p, mat, tc, vc, lights, nl, model, v, q, b0, b1, b2,
-                      (flags & kMeshNormals) != 0u);
+    color = lit_color(p.normals, p.ambient_factor, mat, make_float4(tc[0], tc[1], tc[2], tc[3]),
+                      make_float4(vc[0], vc[1], vc[2], vc[3]), lights, nl, model, v[0], v[1], v[2], q[0],
+                      q[1], q[2], b0, b1, b2, (flags & kMeshNormals) != 0u);
   } else {
     uint32_t packed = 0;
 #pragma unroll
