@@ -27,7 +27,9 @@ class MeshData(ctypes.Structure):
 class TextureData(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("layers", ctypes.c_int32),
                 ("rgba8", ctypes.c_void_p), ("filter", ctypes.c_int32),
-                ("wrap_s", ctypes.c_int32), ("wrap_t", ctypes.c_int32)]
+                ("wrap_s", ctypes.c_int32), ("wrap_t", ctypes.c_int32),
+                ("min_filter", ctypes.c_int32), ("mip_filter", ctypes.c_int32),
+                ("levels", ctypes.c_int32), ("generate_mipmap", ctypes.c_int32)]
 
 
 class MaterialData(ctypes.Structure):

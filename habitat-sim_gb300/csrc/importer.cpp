@@ -377,6 +377,7 @@ bool decode_ktx2(const uint8_t* d, size_t n, ImportedTexture& out, std::string& 
       if (ch == 3) out.rgba[i * 4 + 3] = 255;
     }
   } else if (vk >= 131 && vk <= 134) {
+    out.compressed = true;
     const uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
     if (len < uint64_t(nl) * bw * bh * 8) { err = "short KTX2 BC1 level"; return false; }
     size_t q = 0;
@@ -603,16 +604,20 @@ bool import_gltf(const std::string& path, bool whole, const std::string& name, b
           else
             ok = decode_png(blob.data(), blob.size(), t, err);
           if (!ok) { error = "can't import image of " + path + ": " + err; return false; }
-          int mag = 9729, ws = 10497, wt = 10497;
+          int mag = 9729, minf = 9987, ws = 10497, wt = 10497;
           const Json* smps = doc.j.get("samplers");
           if (smp >= 0 && smps && size_t(smp) < smps->size()) {
             const Json& s = (*smps)[size_t(smp)];
             mag = int(s.numberOr("magFilter", 9729));
+            minf = int(s.numberOr("minFilter", 9987));
             ws = int(s.numberOr("wrapS", 10497));
             wt = int(s.numberOr("wrapT", 10497));
           }
           auto wrap = [](int g) { return g == 33071 ? 1 : g == 33648 ? 2 : 0; };
           t.filter = mag == 9728 ? 0 : 1;
+          // minFilter: NEAREST / LINEAR, then {NEAREST, LINEAR}_MIPMAP_{NEAREST, LINEAR}.
+          t.min_filter = (minf == 9728 || minf == 9984 || minf == 9986) ? 0 : 1;
+          t.mip_filter = (minf == 9984 || minf == 9985) ? 1 : (minf == 9986 || minf == 9987) ? 2 : 0;
           t.wrap_s = wrap(ws);
           t.wrap_t = wrap(wt);
           out.textures.push_back(std::move(t));

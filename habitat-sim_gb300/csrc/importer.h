@@ -11,6 +11,9 @@ struct ImportedTexture {
   std::vector<uint8_t> rgba;  // layers*height*width*4, row 0 = bottom
   int filter = 1;             // 0 nearest, 1 linear (the magnification filter)
   int wrap_s = 0, wrap_t = 0; // 0 repeat, 1 clamp, 2 mirrored repeat
+  int min_filter = 1;         // minification within a level: 0 nearest, 1 linear
+  int mip_filter = 2;         // 0 base level only, 1 nearest level, 2 linear
+  bool compressed = false;    // decoded from a block-compressed image (no generated mips)
 };
 
 struct ImportedMesh {

@@ -687,15 +687,20 @@ __device__ __forceinline__ float chan(uint32_t t, int c, const float* unorm) {
   return unorm[(t >> (8 * c)) & 255u];
 }
 
-__device__ void sample(const TextureRec& t, const uint32_t* texels, int layer, float s, float u,
-                       const float* unorm, float out[4]) {
-  const int L = layer < 0 ? 0 : (layer >= t.layers ? t.layers - 1 : layer);
-  const float fw = float(t.width), fh = float(t.height);
-  const uint32_t* base = texels + t.offset + size_t(L) * t.height * t.width;
-  if (t.filter == 0) {
-    const int x = wrap(int(floorf(clampc(__fmul_rn(s, fw)))), t.width, t.wrap_s);
-    const int y = wrap(int(floorf(clampc(__fmul_rn(u, fh)))), t.height, t.wrap_t);
-    const uint32_t v = __ldg(base + size_t(y) * t.width + x);
+// One level of a texture (level k is max(1, w >> k) x max(1, h >> k); the
+// levels follow one another, each holding every layer), filtered nearest (0)
+// or bilinear (1) at texel centres with the texture's wrap modes.
+__device__ __forceinline__ void sample_level(const TextureRec& t, const uint32_t* texels, int L, int level, int filter,
+                             float s, float u, const float* unorm, float out[4]) {
+  const int tw = max(1, t.width >> level), th = max(1, t.height >> level);
+  size_t off = t.offset;
+  for (int k = 0; k < level; ++k) off += size_t(max(1, t.width >> k)) * size_t(max(1, t.height >> k)) * t.layers;
+  const float fw = float(tw), fh = float(th);
+  const uint32_t* base = texels + off + size_t(L) * th * tw;
+  if (filter == 0) {
+    const int x = wrap(int(floorf(clampc(__fmul_rn(s, fw)))), tw, t.wrap_s);
+    const int y = wrap(int(floorf(clampc(__fmul_rn(u, fh)))), th, t.wrap_t);
+    const uint32_t v = __ldg(base + size_t(y) * tw + x);
 #pragma unroll
     for (int c = 0; c < 4; ++c) out[c] = chan(v, c, unorm);
     return;
@@ -704,12 +709,12 @@ __device__ void sample(const TextureRec& t, const uint32_t* texels, int layer, f
   const float fy = clampc(__fsub_rn(__fmul_rn(u, fh), 0.5f));
   const float flx = floorf(fx), fly = floorf(fy);
   const float a = __fsub_rn(fx, flx), b = __fsub_rn(fy, fly);
-  const int x0 = wrap(int(flx), t.width, t.wrap_s), x1 = wrap(int(flx) + 1, t.width, t.wrap_s);
-  const int y0 = wrap(int(fly), t.height, t.wrap_t), y1 = wrap(int(fly) + 1, t.height, t.wrap_t);
-  const uint32_t v00 = __ldg(base + size_t(y0) * t.width + x0);
-  const uint32_t v10 = __ldg(base + size_t(y0) * t.width + x1);
-  const uint32_t v01 = __ldg(base + size_t(y1) * t.width + x0);
-  const uint32_t v11 = __ldg(base + size_t(y1) * t.width + x1);
+  const int x0 = wrap(int(flx), tw, t.wrap_s), x1 = wrap(int(flx) + 1, tw, t.wrap_s);
+  const int y0 = wrap(int(fly), th, t.wrap_t), y1 = wrap(int(fly) + 1, th, t.wrap_t);
+  const uint32_t v00 = __ldg(base + size_t(y0) * tw + x0);
+  const uint32_t v10 = __ldg(base + size_t(y0) * tw + x1);
+  const uint32_t v01 = __ldg(base + size_t(y1) * tw + x0);
+  const uint32_t v11 = __ldg(base + size_t(y1) * tw + x1);
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     const float t00 = chan(v00, c, unorm), t10 = chan(v10, c, unorm), t01 = chan(v01, c, unorm),
@@ -717,6 +722,70 @@ __device__ void sample(const TextureRec& t, const uint32_t* texels, int layer, f
     const float lo = fma_(a, __fsub_rn(t10, t00), t00);
     const float hi = fma_(a, __fsub_rn(t11, t01), t01);
     out[c] = fma_(b, __fsub_rn(hi, lo), lo);
+  }
+}
+
+__device__ __forceinline__ int clamp_layer(const TextureRec& t, int layer) {
+  return layer < 0 ? 0 : (layer >= t.layers ? t.layers - 1 : layer);
+}
+
+// Level-0 sampling with the magnification filter (textures whose
+// minification is the same and that have no mip levels).
+__device__ __forceinline__ void sample(const TextureRec& t, const uint32_t* texels, int layer, float s, float u,
+                                       const float* unorm, float out[4]) {
+  sample_level(t, texels, clamp_layer(t, layer), 0, t.filter, s, u, unorm, out);
+}
+
+// log2 by the atanh series of the mantissa normalised to [sqrt(1/2), sqrt(2))
+// (every operation one float rounding, so the oracle reproduces it).
+__device__ __forceinline__ float series_log2(float x) {
+  int e;
+  float m = frexpf(x, &e);
+  if (m < 0.7071067690849304f) {
+    m = __fmul_rn(m, 2.0f);
+    e -= 1;
+  }
+  const float t = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+  const float t2 = __fmul_rn(t, t);
+  float q = 0.1111111119389534f;
+  q = __fadd_rn(__fmul_rn(q, t2), 0.1428571492433548f);
+  q = __fadd_rn(__fmul_rn(q, t2), 0.20000000298023224f);
+  q = __fadd_rn(__fmul_rn(q, t2), 0.3333333432674408f);
+  q = __fadd_rn(__fmul_rn(q, t2), 1.0f);
+  return __fadd_rn(float(e), __fmul_rn(__fmul_rn(t, q), 2.885390043258667f));
+}
+
+// Texture lookup at level-of-detail lambda = log2(rho) (OpenGL 4.6, 8.14):
+// magnification (level 0, magnification filter) up to c = 0.5 for a linear
+// magnification with a nearest-mipmap minification, else 0; then the base
+// level, the nearest level ceil(lambda + 1/2) - 1, or the two levels around
+// lambda blended by its fraction, each with the minification filter.
+__device__ __forceinline__ void sample_lod(const TextureRec& t, const uint32_t* texels, int layer, float s, float u,
+                           float lambda, const float* unorm, float out[4]) {
+  const int L = clamp_layer(t, layer);
+  const float c = (t.filter == 1 && t.min_filter == 0 && t.mip_filter != 0) ? 0.5f : 0.0f;
+  if (!(lambda > c)) {
+    sample_level(t, texels, L, 0, t.filter, s, u, unorm, out);
+    return;
+  }
+  const int q = t.levels - 1;
+  if (t.mip_filter == 0) {
+    sample_level(t, texels, L, 0, t.min_filter, s, u, unorm, out);
+  } else if (t.mip_filter == 1) {
+    int d = lambda <= 0.5f ? 0 : int(ceilf(__fadd_rn(lambda, 0.5f))) - 1;
+    if (d > q) d = q;
+    sample_level(t, texels, L, d, t.min_filter, s, u, unorm, out);
+  } else if (lambda >= float(q)) {
+    sample_level(t, texels, L, q, t.min_filter, s, u, unorm, out);
+  } else {
+    const float fl = floorf(lambda);
+    const int d1 = int(fl);
+    const float f = __fsub_rn(lambda, fl);
+    float hi[4];
+    sample_level(t, texels, L, d1, t.min_filter, s, u, unorm, out);
+    sample_level(t, texels, L, d1 + 1, t.min_filter, s, u, unorm, hi);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = fma_(f, __fsub_rn(hi[k], out[k]), out[k]);
   }
 }
 
@@ -814,9 +883,16 @@ __device__ __noinline__ uint32_t lit_color(const float4* __restrict__ vertex_nor
 }
 
 // Shade the winning triangle `t` of visible draw `rec` at pixel (px, py).
-__device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec, uint32_t t,
-                      int px, int py, const float* unorm, const WorldLight* lights, uint32_t nl,
-                      const ModelRec* model, uint32_t& color, float& lin, uint32_t& sid) {
+// Mode 0: every texture sampled at level 0 with its magnification filter
+// (no texture of the launch needs a level of detail).  Mode 1: textures that
+// need one (mip levels or a minification filter other than the magnification
+// one) are not sampled and the call returns false; the caller shades those
+// pixels again with Mode 2, the level-of-detail path, in a separate loop, so
+// that the derivative code does not add to the common path's registers.
+template <int Mode>
+__device__ __forceinline__ bool shade(const RasterParams& p, int W, int H, const VisibleRec* rec, uint32_t t,
+                                      int px, int py, const float* unorm, const WorldLight* lights, uint32_t nl,
+                                      const ModelRec* model, uint32_t& color, float& lin, uint32_t& sid) {
   // The record in 16-byte loads: mvp, zrow, (vertex_base, first_index,
   // tri_count, material), (semantic_id, ordinal, flags, chunk).
   const float4* r4 = reinterpret_cast<const float4*>(rec);
@@ -856,15 +932,15 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
   }
   const float sx = __fdiv_rn(float(2 * px + 1 - W), float(W));
   const float sy = __fdiv_rn(float(2 * py + 1 - H), float(H));
-  float l[3];
+  float l[3], ex[3], ey[3], ez[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     const float4 a = c[(i + 1) % 3];
     const float4 b = c[(i + 2) % 3];
-    const float ex = __fsub_rn(__fmul_rn(a.y, b.w), __fmul_rn(a.w, b.y));
-    const float ey = __fsub_rn(__fmul_rn(a.w, b.x), __fmul_rn(a.x, b.w));
-    const float ez = __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x));
-    l[i] = fma_(ex, sx, fma_(ey, sy, ez));
+    ex[i] = __fsub_rn(__fmul_rn(a.y, b.w), __fmul_rn(a.w, b.y));
+    ey[i] = __fsub_rn(__fmul_rn(a.w, b.x), __fmul_rn(a.x, b.w));
+    ez[i] = __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x));
+    l[i] = fma_(ex[i], sx, fma_(ey[i], sy, ez[i]));
   }
   const float s = __fadd_rn(__fadd_rn(l[0], l[1]), l[2]);
   const float inv = __frcp_rn(s);
@@ -886,8 +962,11 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
   const int tex = mat.texture;
   if (!(p.flags & 1u) && tex > 0 && tex < p.texture_count) {
     float u = 0.0f, w = 0.0f;
+    float2 t0 = make_float2(0.0f, 0.0f), t1 = t0, t2 = t0;
     if (flags & kMeshTexcoords) {
-      const float2 t0 = __ldg(&p.uv[v[0]]), t1 = __ldg(&p.uv[v[1]]), t2 = __ldg(&p.uv[v[2]]);
+      t0 = __ldg(&p.uv[v[0]]);
+      t1 = __ldg(&p.uv[v[1]]);
+      t2 = __ldg(&p.uv[v[2]]);
       u = GBR_INTERP(t0.x, t1.x, t2.x);
       w = GBR_INTERP(t0.y, t1.y, t2.y);
     }
@@ -897,7 +976,42 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
     float tt = mat.m[7];
     tt = fma_(mat.m[1], u, tt);
     tt = fma_(mat.m[4], w, tt);
-    sample(p.textures[tex], p.texels, mat.layer, ts, tt, unorm, tc);
+    const TextureRec& tr = p.textures[tex];
+    if (Mode == 0 || (tr.mip_filter == 0 && tr.min_filter == tr.filter)) {
+      sample(tr, p.texels, mat.layer, ts, tt, unorm, tc);
+    } else if (Mode == 1) {
+      return false;
+    } else {
+      // Level of detail from the derivatives of the level-0 texel coordinates
+      // across the pixel's 2x2 quad: the quad's pixel pair in this row (x)
+      // and in this column (y), each evaluated like the pixel itself.
+      auto st_at = [&](int x, int y, float& os, float& ot) {
+        const float qx = __fdiv_rn(float(2 * x + 1 - W), float(W));
+        const float qy = __fdiv_rn(float(2 * y + 1 - H), float(H));
+        const float a0 = fma_(ex[0], qx, fma_(ey[0], qy, ez[0]));
+        const float a1 = fma_(ex[1], qx, fma_(ey[1], qy, ez[1]));
+        const float a2 = fma_(ex[2], qx, fma_(ey[2], qy, ez[2]));
+        const float is = __frcp_rn(__fadd_rn(__fadd_rn(a0, a1), a2));
+        const float c0 = __fmul_rn(a0, is), c1 = __fmul_rn(a1, is), c2 = __fmul_rn(a2, is);
+        const float uu = fma_(c2, t2.x, fma_(c1, t1.x, __fmul_rn(c0, t0.x)));
+        const float ww = fma_(c2, t2.y, fma_(c1, t1.y, __fmul_rn(c0, t0.y)));
+        os = fma_(mat.m[3], ww, fma_(mat.m[0], uu, mat.m[6]));
+        ot = fma_(mat.m[4], ww, fma_(mat.m[1], uu, mat.m[7]));
+      };
+      float sa, ta, sb, tb, sc, tcc, sd, td;
+      st_at(px & ~1, py, sa, ta);
+      st_at((px & ~1) + 1, py, sb, tb);
+      st_at(px, py & ~1, sc, tcc);
+      st_at(px, (py & ~1) + 1, sd, td);
+      const float fw = float(tr.width), fh = float(tr.height);
+      const float dux = __fmul_rn(__fsub_rn(sb, sa), fw), dvx = __fmul_rn(__fsub_rn(tb, ta), fh);
+      const float duy = __fmul_rn(__fsub_rn(sd, sc), fw), dvy = __fmul_rn(__fsub_rn(td, tcc), fh);
+      const float rx = __fsqrt_rn(__fadd_rn(__fmul_rn(dux, dux), __fmul_rn(dvx, dvx)));
+      const float ry = __fsqrt_rn(__fadd_rn(__fmul_rn(duy, duy), __fmul_rn(dvy, dvy)));
+      const float rho = fmaxf(rx, ry);
+      const float lambda = rho > 0.0f ? (rho < 3.0e38f ? series_log2(rho) : 128.0f) : -1.0f;
+      sample_lod(tr, p.texels, mat.layer, ts, tt, lambda, unorm, tc);
+    }
   }
 #undef GBR_INTERP
   if (p.max_lights > 0 && mat.phong) {
@@ -914,6 +1028,7 @@ __device__ void shade(const RasterParams& p, int W, int H, const VisibleRec* rec
     color = packed;
   }
   sid = (flags & kMeshObjectId) ? __float_as_uint(__ldg(&p.pos[v[2]]).w) : u6.x;
+  return true;
 }
 
 // Largest k in [0, n) with order[k].y (first cluster in processing order) <= g.
@@ -1008,7 +1123,7 @@ __device__ __forceinline__ bool chunk_keep(const float* mvp, const ChunkBox& b, 
   return false;
 }
 
-template <int T>
+template <int T, bool Lod>
 __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SmemLayout L = smem_layout(T, p.region_px, p.prefix_cap);
@@ -1290,6 +1405,11 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
     const uint32_t nlights =
         p.lights ? min(p.cameras[p.cameras[wi.scene].source].light_count, p.max_lights) : 0u;
     const WorldLight* lights = p.lights ? p.lights + size_t(wi.scene) * p.max_lights : nullptr;
+    // Pixels whose texture needs a level of detail are marked in their key
+    // (bit 63: depth bits of a drawn pixel are below 0x3f800000) and shaded in
+    // a second loop by the same thread.
+    constexpr uint64_t kDeferred = 1ull << 63;
+    bool deferred = false;
     for (int i = threadIdx.x; i < npx; i += T) {
       const int px = c.rx0 + i % c.rw, py = c.ry0 + i / c.rw;
       const uint64_t key = keys[i];
@@ -1300,13 +1420,36 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
         const uint32_t ord = uint32_t(key);
         dep = __uint_as_float(uint32_t(key >> 32));
         const uint32_t di = find_draw(prefix, vis, cached, nvis, ord);
-        shade(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, s_unorm, lights,
-              nlights, p.model ? p.model + vis_base + di : nullptr, col, lin, sid);
+        if (!shade<Lod ? 1 : 0>(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, s_unorm,
+                                lights, nlights, p.model ? p.model + vis_base + di : nullptr, col, lin, sid)) {
+          keys[i] = key | kDeferred;
+          deferred = true;
+          continue;
+        }
       }
       if (p.out.color) p.out.color[o] = col;
       if (p.out.depth) p.out.depth[o] = dep;
       if (p.out.linear) p.out.linear[o] = lin;
       if (p.out.semantic) p.out.semantic[o] = sid;
+    }
+    if (Lod && __syncthreads_or(deferred)) {
+      for (int i = threadIdx.x; i < npx; i += T) {
+        const uint64_t key = keys[i];
+        if (key == kEmptyKey || !(key & kDeferred)) continue;
+        const int px = c.rx0 + i % c.rw, py = c.ry0 + i / c.rw;
+        const int64_t o = sc.fb_offset + int64_t(py) * sc.pitch + px;
+        const uint32_t ord = uint32_t(key);
+        const float dep = __uint_as_float(uint32_t((key & ~kDeferred) >> 32));
+        const uint32_t di = find_draw(prefix, vis, cached, nvis, ord);
+        uint32_t col, sid;
+        float lin;
+        shade<2>(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, s_unorm, lights, nlights,
+                 p.model ? p.model + vis_base + di : nullptr, col, lin, sid);
+        if (p.out.color) p.out.color[o] = col;
+        if (p.out.depth) p.out.depth[o] = dep;
+        if (p.out.linear) p.out.linear[o] = lin;
+        if (p.out.semantic) p.out.semantic[o] = sid;
+      }
     }
   }
 }
@@ -1396,10 +1539,13 @@ cudaError_t raster_configure(int threads, size_t* max_dynamic, size_t* static_by
 #define GBR_CFG(T)                                                                             \
   {                                                                                            \
     cudaFuncAttributes fa;                                                                     \
-    e = cudaFuncGetAttributes(&fa, raster_kernel<T>);                                          \
+    e = cudaFuncGetAttributes(&fa, raster_kernel<T, false>);                                   \
     if (e != cudaSuccess) return e;                                                            \
     const size_t dyn = size_t(optin) > fa.sharedSizeBytes ? size_t(optin) - fa.sharedSizeBytes : 0; \
-    e = cudaFuncSetAttribute(raster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+    e = cudaFuncSetAttribute(raster_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             int(dyn));                                                        \
+    if (e != cudaSuccess) return e;                                                            \
+    e = cudaFuncSetAttribute(raster_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                              int(dyn));                                                        \
     if (e != cudaSuccess) return e;                                                            \
     *max_dynamic = dyn;                                                                        \
@@ -1413,7 +1559,7 @@ cudaError_t raster_configure(int threads, size_t* max_dynamic, size_t* static_by
 cudaError_t raster_max_ctas_per_sm(int threads, size_t smem, int* out) {
 #define GBR_OCC(T)                                                                                \
   {                                                                                               \
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, raster_kernel<T>, T, smem); \
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, raster_kernel<T, false>, T, smem); \
     if (e != cudaSuccess) return e;                                                               \
   }
   GBR_RASTER_SWITCH(threads, GBR_OCC)
@@ -1424,7 +1570,11 @@ cudaError_t raster_max_ctas_per_sm(int threads, size_t smem, int* out) {
 cudaError_t launch_raster(const RasterParams& p, int threads, uint32_t grid, size_t smem,
                           cudaStream_t stream) {
   if (grid == 0) return cudaSuccess;
-#define GBR_LAUNCH(T) raster_kernel<T><<<grid, T, smem, stream>>>(p);
+#define GBR_LAUNCH(T)                                           \
+  if (p.any_lod)                                                \
+    raster_kernel<T, true><<<grid, T, smem, stream>>>(p);       \
+  else                                                          \
+    raster_kernel<T, false><<<grid, T, smem, stream>>>(p);
   GBR_RASTER_SWITCH(threads, GBR_LAUNCH)
 #undef GBR_LAUNCH
   return cudaGetLastError();

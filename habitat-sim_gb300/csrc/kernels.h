@@ -80,6 +80,7 @@ struct RasterParams {
   const float4* normals;
   uint32_t max_lights;
   float ambient_factor;
+  int any_lod;  // some texture has mip levels or a minification filter of its own
 };
 
 cudaError_t launch_prepare(const PrepareParams& p, uint32_t scene_count, cudaStream_t stream);

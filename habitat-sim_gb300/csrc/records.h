@@ -6,7 +6,7 @@
 //              color[v]  float4 RGBA                        16 B / vertex
 //              uv[v]     float2                              8 B / vertex
 //              index[i]  uint32                              4 B / index
-//   textures   texel[t]  uint32 RGBA8, layer-major, row 0 bottom
+//   textures   texel[t]  uint32 RGBA8, level-major then layer-major, row 0 bottom
 //   tables     MeshRec, MaterialRec, TextureRec
 //   scenes     SceneRec[s]; per node parent (int32) + local 4x4 (64 B);
 //              DrawRec[] (64 B) in draw-batch order; CameraRec[s] (96 B) followed
@@ -52,11 +52,16 @@ struct MaterialRec {
 };
 
 struct TextureRec {
-  uint64_t offset;  // in texels
+  uint64_t offset;     // in texels: level 0 of every layer, then level 1, ...
   int32_t width, height, layers;
-  int32_t filter;   // 0 nearest, 1 linear
+  int32_t filter;      // magnification: 0 nearest, 1 linear
   int32_t wrap_s, wrap_t;
+  int32_t min_filter;  // minification within a level: 0 nearest, 1 linear
+  int32_t mip_filter;  // 0 base level only, 1 nearest level, 2 linear between levels
+  int32_t levels;
+  int32_t pad;
 };
+static_assert(sizeof(TextureRec) == 48, "TextureRec layout");
 
 struct SceneRec {
   int32_t width, height;

@@ -19,6 +19,7 @@
 
 #include "hbao.h"
 #include "importer.h"
+#include "mips.h"
 
 namespace gbr {
 
@@ -366,16 +367,27 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
 gbr_status Renderer::add_texture(const gbr_texture_data& t, uint32_t* id) {
   if (t.width <= 0 || t.height <= 0 || t.layers <= 0 || !t.rgba8)
     return fail(GBR_ERROR_INVALID_ARGUMENT, "addTexture: empty texture");
-  if (t.filter < 0 || t.filter > 1 || t.wrap_s < 0 || t.wrap_s > 2 || t.wrap_t < 0 || t.wrap_t > 2)
+  if (t.filter < 0 || t.filter > 1 || t.wrap_s < 0 || t.wrap_s > 2 || t.wrap_t < 0 || t.wrap_t > 2 ||
+      t.min_filter < 0 || t.min_filter > 2 || t.mip_filter < 0 || t.mip_filter > 2)
     return fail(GBR_ERROR_INVALID_ARGUMENT, "addTexture: bad filter or wrap mode");
+  int levels = std::max(1, t.levels);
+  if (levels > mip_max_levels(t.width, t.height))
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "addTexture: more levels than the size allows");
+  std::vector<uint8_t> chain;
+  const uint8_t* data = t.rgba8;
+  if (t.generate_mipmap && levels == 1) {
+    levels = mip_chain_levels(t.width, t.height);
+    chain = generate_mips(t.rgba8, t.width, t.height, t.layers, levels);
+    data = chain.data();
+  }
   cudaSetDevice(device_);
-  const size_t n = size_t(t.width) * t.height * t.layers;
+  const size_t n = mip_texels(t.width, t.height, t.layers, levels);
   const uint64_t off = texel_pool_.alloc(n);
   if (!d_texels_.reserve(texel_pool_.end * 4, true)) {
     texel_pool_.release(off, n);
     return fail(GBR_ERROR_OUT_OF_MEMORY, "addTexture: out of device memory");
   }
-  GBR_CUDA(cudaMemcpy(d_texels_.as<char>() + off * 4, t.rgba8, n * 4, cudaMemcpyHostToDevice),
+  GBR_CUDA(cudaMemcpy(d_texels_.as<char>() + off * 4, data, n * 4, cudaMemcpyHostToDevice),
            "addTexture upload");
   TextureRec rec{};
   rec.offset = off;
@@ -385,6 +397,9 @@ gbr_status Renderer::add_texture(const gbr_texture_data& t, uint32_t* id) {
   rec.filter = t.filter;
   rec.wrap_s = t.wrap_s;
   rec.wrap_t = t.wrap_t;
+  rec.min_filter = t.min_filter == 0 ? t.filter : t.min_filter - 1;
+  rec.mip_filter = t.mip_filter;
+  rec.levels = levels;
   textures_.push_back(rec);
   texture_live_.push_back(true);
   tables_dirty_ = true;
@@ -509,10 +524,13 @@ gbr_status Renderer::add_file(const char* filename, uint32_t flags, const char* 
   const uint32_t texture_offset = uint32_t(textures_.size());
   const uint32_t mesh_offset = uint32_t(meshes_.size());
   const uint32_t material_offset = uint32_t(materials_.size());
-  // GenerateMipmap: mip levels are not sampled (see sample() in kernels.cu),
-  // so the flag changes nothing in the output.
+  // GenerateMipmap: a full chain for single-level images that were not block
+  // compressed (Renderer.cpp:445-477); the sampler's minification and mipmap
+  // filters come from the file.
   for (auto& t : f.textures) {
-    gbr_texture_data td{t.width, t.height, t.layers, t.rgba.data(), t.filter, t.wrap_s, t.wrap_t};
+    const int gen = (flags & GBR_FILE_GENERATE_MIPMAP) && !t.compressed ? 1 : 0;
+    gbr_texture_data td{t.width, t.height, t.layers, t.rgba.data(), t.filter, t.wrap_s, t.wrap_t,
+                        t.min_filter + 1, t.mip_filter, 1, gen};
     uint32_t id;
     gbr_status s = add_texture(td, &id);
     if (s != GBR_OK) return s;
@@ -806,7 +824,7 @@ gbr_status Renderer::remove_texture(uint32_t texture) {
     return fail(GBR_ERROR_INVALID_ARGUMENT, "removeTexture: no texture " + std::to_string(texture));
   if (gbr_status s = quiesce()) return s;
   const TextureRec& t = textures_[texture];
-  texel_pool_.release(t.offset, uint64_t(t.width) * t.height * t.layers);
+  texel_pool_.release(t.offset, mip_texels(t.width, t.height, t.layers, t.levels));
   texture_live_[texture] = false;
   structure_dirty_ = true;
   return GBR_OK;
@@ -1203,6 +1221,10 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   rp.occlusion = tuning_.occlusion_culling;
   rp.max_lights = max_lights_;
   rp.ambient_factor = cfg_.ambient_factor;
+  rp.any_lod = 0;
+  for (size_t i = 0; i < textures_.size(); ++i)
+    if (texture_live_[i] && (textures_[i].mip_filter != 0 || textures_[i].min_filter != textures_[i].filter))
+      rp.any_lod = 1;
   if (max_lights_ > 0) {
     rp.lights = pp.lights;
     rp.model = pp.model;

@@ -367,13 +367,29 @@ class RendererStandalone:
         check(self._lib.gbr_add_mesh(self._h, ctypes.byref(md), ctypes.byref(out)))
         return out.value
 
-    def addTexture(self, pixels, filter=1, wrapS=0, wrapT=0):
-        """pixels: uint8 [layers, h, w, 4] or [h, w, 4], row 0 = bottom."""
-        p = np.ascontiguousarray(pixels, np.uint8)
-        if p.ndim == 3:
-            p = p[None]
-        td = _lib.TextureData(p.shape[2], p.shape[1], p.shape[0], p.ctypes.data, int(filter),
-                              int(wrapS), int(wrapT))
+    def addTexture(self, pixels, filter=1, wrapS=0, wrapT=0, minFilter=0, mipFilter=0, levels=None,
+                   generateMipmap=False):
+        """pixels: uint8 [layers, h, w, 4] or [h, w, 4], row 0 = bottom -- or,
+        with ``levels``, a list of such arrays, level 0 first (level k is
+        max(1, w >> k) x max(1, h >> k)).  ``filter`` is the magnification
+        filter (0 nearest, 1 bilinear); ``minFilter`` 0 = as ``filter``,
+        1 nearest, 2 linear; ``mipFilter`` 0 base level only, 1 nearest
+        level, 2 linear between levels; ``generateMipmap`` derives the chain
+        from a single level."""
+        if levels is not None:
+            chain = [np.ascontiguousarray(l, np.uint8) for l in pixels]
+            chain = [c[None] if c.ndim == 3 else c for c in chain]
+            p = chain[0]
+            data = np.concatenate([c.reshape(-1) for c in chain])
+            nlev = len(chain)
+        else:
+            p = np.ascontiguousarray(pixels, np.uint8)
+            if p.ndim == 3:
+                p = p[None]
+            data, nlev = p, 1
+        td = _lib.TextureData(p.shape[2], p.shape[1], p.shape[0], data.ctypes.data, int(filter),
+                              int(wrapS), int(wrapT), int(minFilter), int(mipFilter), nlev,
+                              1 if generateMipmap else 0)
         out = ctypes.c_uint32()
         check(self._lib.gbr_add_texture(self._h, ctypes.byref(td), ctypes.byref(out)))
         return out.value

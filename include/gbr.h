@@ -127,9 +127,19 @@ gbr_status gbr_add_mesh(gbr_renderer* r, const gbr_mesh_data* mesh, uint32_t* ou
 
 typedef struct gbr_texture_data {
   int32_t width, height, layers;
-  const uint8_t* rgba8;       /* layers*height*width*4 bytes, row 0 bottom  */
-  int32_t filter;             /* 0 nearest, 1 bilinear                      */
+  const uint8_t* rgba8;       /* RGBA8, row 0 bottom: level 0 of every layer,
+                                 then level 1 of every layer, ...            */
+  int32_t filter;             /* magnification: 0 nearest, 1 bilinear       */
   int32_t wrap_s, wrap_t;     /* 0 repeat, 1 clamp to edge, 2 mirrored      */
+  int32_t min_filter;         /* minification within a level: 0 = as filter,
+                                 1 nearest, 2 linear                        */
+  int32_t mip_filter;         /* 0 base level only, 1 nearest level,
+                                 2 linear between levels                    */
+  int32_t levels;             /* levels in rgba8 (0 or 1: one); level k is
+                                 max(1, w >> k) x max(1, h >> k)            */
+  int32_t generate_mipmap;    /* 1 with one level: derive the chain down to
+                                 min(w, h) = 1 (RendererFileFlag::
+                                 GenerateMipmap, Renderer.cpp:445-477)       */
 } gbr_texture_data;
 gbr_status gbr_add_texture(gbr_renderer* r, const gbr_texture_data* texture,
                            uint32_t* out_texture_id);

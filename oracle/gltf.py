@@ -327,16 +327,22 @@ def load_gltf(path, whole=False, name=None, no_textures=False):
                     with open(os.path.join(base, img["uri"]), "rb") as f:
                         blob = f.read()
                     mime = "image/ktx2" if img["uri"].endswith(".ktx2") else "image/png"
+                compressed = False
                 if mime == "image/ktx2" or blob[:4] == b"\xabKTX":
                     pixels, _ = decode_ktx2(blob)
+                    compressed = struct.unpack("<I", blob[12:16])[0] in (131, 132, 133, 134)
                 else:
                     pixels = decode_png(blob)[None]
                 smp = doc["samplers"][tex["sampler"]] if "sampler" in tex else {}
                 dedup[key] = len(out.textures)
+                minf = smp.get("minFilter", 9987)    # absent: linear, linear between levels
                 out.textures.append(dict(
                     pixels=pixels,
                     mag=FILTER_NEAREST if smp.get("magFilter", GL_LINEAR) == GL_NEAREST
                     else FILTER_LINEAR,
+                    min=FILTER_NEAREST if minf in (9728, 9984, 9986) else FILTER_LINEAR,
+                    mip=1 if minf in (9984, 9985) else (2 if minf in (9986, 9987) else 0),
+                    compressed=bool(compressed),
                     wrap_s=_WRAP[smp.get("wrapS", GL_REPEAT)],
                     wrap_t=_WRAP[smp.get("wrapT", GL_REPEAT)]))
             texture_map[ti] = (dedup[key], layer)

@@ -37,7 +37,32 @@ BACKGROUND = 0xFF1F1F1F
 class _Tex(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
                 ("layers", ctypes.c_int32), ("filter", ctypes.c_int32),
-                ("wrap_s", ctypes.c_int32), ("wrap_t", ctypes.c_int32)]
+                ("wrap_s", ctypes.c_int32), ("wrap_t", ctypes.c_int32),
+                ("min_filter", ctypes.c_int32), ("mip_filter", ctypes.c_int32),
+                ("levels", ctypes.c_int32)]
+
+
+def mip_chain_levels(w, h):
+    """floor(log2(min(w, h))) + 1 (Renderer.cpp:445-450, 493-498)."""
+    return int(min(w, h)).bit_length()
+
+
+def generate_mips(level0, levels):
+    """Levels 1.. of a uint8 [layers, h, w, 4] texture: each texel the mean
+    (a + b + c + d + 2) >> 2 of the 2 x 2 texels above it (indices clamped to
+    the finer level).  Returns the list of levels, level 0 first."""
+    out = [np.ascontiguousarray(level0, np.uint8)]
+    for _ in range(1, levels):
+        p = out[-1].astype(np.uint32)
+        _, ph, pw, _ = p.shape
+        nh, nw = max(1, ph // 2), max(1, pw // 2)
+        y0 = np.minimum(2 * np.arange(nh), ph - 1)
+        y1 = np.minimum(2 * np.arange(nh) + 1, ph - 1)
+        x0 = np.minimum(2 * np.arange(nw), pw - 1)
+        x1 = np.minimum(2 * np.arange(nw) + 1, pw - 1)
+        s = (p[:, y0][:, :, x0] + p[:, y0][:, :, x1] + p[:, y1][:, :, x0] + p[:, y1][:, :, x1] + 2) >> 2
+        out.append(s.astype(np.uint8))
+    return out
 
 
 class _Mesh(ctypes.Structure):
@@ -161,8 +186,10 @@ class OracleRenderer:
         view_offset = len(self.mesh_views)
         material_offset = len(self.materials)
         for t in f.textures:
-            self.textures.append(dict(pixels=np.ascontiguousarray(t["pixels"]), filter=t["mag"],
-                                      wrap_s=t["wrap_s"], wrap_t=t["wrap_t"]))
+            gen = bool(flags & FILE_GENERATE_MIPMAP) and not t.get("compressed", False)
+            self.add_texture(t["pixels"], t["mag"], t["wrap_s"], t["wrap_t"],
+                             min_filter=t.get("min", t["mag"]) + 1, mip_filter=t.get("mip", 0),
+                             generate_mipmap=gen)
         for m in f.meshes:
             self.add_mesh(m["positions"], m["colors"], m["texcoords"], m["object_ids"],
                           m["indices"], m.get("normals"))
@@ -196,11 +223,26 @@ class OracleRenderer:
             indices=np.ascontiguousarray(indices, np.uint32).reshape(-1)))
         return len(self.meshes) - 1
 
-    def add_texture(self, pixels, filter=1, wrap_s=0, wrap_t=0):
-        p = np.ascontiguousarray(pixels, np.uint8)
-        if p.ndim == 3:
-            p = p[None]
-        self.textures.append(dict(pixels=p, filter=filter, wrap_s=wrap_s, wrap_t=wrap_t))
+    def add_texture(self, pixels, filter=1, wrap_s=0, wrap_t=0, min_filter=0, mip_filter=0,
+                    levels=None, generate_mipmap=False):
+        """pixels: uint8 [layers, h, w, 4] (level 0), or a list of levels when
+        `levels` is given; min_filter 0 = as `filter`, 1 nearest, 2 linear;
+        mip_filter 0 base level, 1 nearest level, 2 linear between levels."""
+        if levels is not None:
+            chain = [np.ascontiguousarray(l, np.uint8) for l in pixels]
+            chain = [c[None] if c.ndim == 3 else c for c in chain]
+        else:
+            p = np.ascontiguousarray(pixels, np.uint8)
+            if p.ndim == 3:
+                p = p[None]
+            chain = [p]
+            if generate_mipmap:
+                chain = generate_mips(p, mip_chain_levels(p.shape[2], p.shape[1]))
+        self.textures.append(dict(
+            pixels=chain[0], data=np.concatenate([c.reshape(-1) for c in chain]),
+            filter=filter, wrap_s=wrap_s, wrap_t=wrap_t,
+            min_filter=filter if min_filter == 0 else min_filter - 1, mip_filter=int(mip_filter),
+            levels=len(chain)))
         return len(self.textures) - 1
 
     def add_material(self, color=(1, 1, 1, 1), texture=0, layer=0, matrix=None, shaded=False):
@@ -321,9 +363,11 @@ class OracleRenderer:
         tex = (_Tex * len(self.textures))()
         for i, t in enumerate(self.textures):
             p = t["pixels"]
-            keep.append(p)
-            tex[i] = _Tex(p.ctypes.data, p.shape[2], p.shape[1], p.shape[0], t["filter"],
-                          t["wrap_s"], t["wrap_t"])
+            d = t.get("data", p.reshape(-1))
+            keep.append(d)
+            tex[i] = _Tex(d.ctypes.data, p.shape[2], p.shape[1], p.shape[0], t["filter"],
+                          t["wrap_s"], t["wrap_t"], t.get("min_filter", t["filter"]),
+                          t.get("mip_filter", 0), t.get("levels", 1))
         meshes = (_Mesh * max(1, len(self.meshes)))()
         for i, m in enumerate(self.meshes):
             meshes[i] = _Mesh(_ptr(m["positions"]), _ptr(m["colors"]), _ptr(m["texcoords"]),
@@ -395,8 +439,9 @@ def unproject_depth(unprojection, depth):
 # Procedural call surface shared with the GPU renderer's Python API.
 OracleRenderer.addMesh = lambda self, positions, colors=None, texcoords=None, objectIds=None, \
     indices=None: self.add_mesh(positions, colors, texcoords, objectIds, indices)
-OracleRenderer.addTexture = lambda self, pixels, filter=1, wrapS=0, wrapT=0: \
-    self.add_texture(pixels, filter, wrapS, wrapT)
+OracleRenderer.addTexture = lambda self, pixels, filter=1, wrapS=0, wrapT=0, minFilter=0, \
+    mipFilter=0, levels=None, generateMipmap=False: \
+    self.add_texture(pixels, filter, wrapS, wrapT, minFilter, mipFilter, levels, generateMipmap)
 OracleRenderer.addMaterial = lambda self, color=(1, 1, 1, 1), texture=0, layer=0, matrix=None: \
     self.add_material(color, texture, layer, matrix)
 OracleRenderer.addNodeHierarchyTemplate = lambda self, name, views: \

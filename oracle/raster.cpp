@@ -66,10 +66,13 @@
 extern "C" {
 
 struct OracleTexture {
-  const uint8_t* data;  // layers * h * w * 4, row 0 = bottom
+  const uint8_t* data;  // level 0 of every layer (layers * h * w * 4), then level 1, ...; row 0 = bottom
   int32_t width, height, layers;
-  int32_t filter;       // 0 nearest, 1 linear
+  int32_t filter;       // magnification: 0 nearest, 1 linear
   int32_t wrap_s, wrap_t;  // 0 repeat, 1 clamp to edge, 2 mirrored repeat
+  int32_t min_filter;   // minification within a level: 0 nearest, 1 linear
+  int32_t mip_filter;   // 0 base level only, 1 nearest level, 2 linear between levels
+  int32_t levels;
 };
 
 struct OracleMesh {
@@ -191,31 +194,90 @@ inline float clampc(float f) {
   return f;
 }
 
-inline float texel(const OracleTexture& t, int layer, int x, int y, int c) {
-  size_t i = ((size_t(layer) * t.height + y) * t.width + x) * 4 + c;
+// Texel of level `level` (level k is max(1, w >> k) x max(1, h >> k); the
+// levels follow one another, each holding every layer).
+inline float texel(const OracleTexture& t, size_t level_off, int tw, int th, int layer, int x, int y, int c) {
+  size_t i = level_off + ((size_t(layer) * th + y) * tw + x) * 4 + c;
   return float(t.data[i]) / 255.0f;
 }
 
-void sample(const OracleTexture& t, int layer, float s, float u, float out[4]) {
-  int L = layer < 0 ? 0 : (layer >= t.layers ? t.layers - 1 : layer);
-  float fw = float(t.width), fh = float(t.height);
-  if (t.filter == 0) {
-    int x = wrap(int(std::floor(clampc(s * fw))), t.width, t.wrap_s);
-    int y = wrap(int(std::floor(clampc(u * fh))), t.height, t.wrap_t);
-    for (int c = 0; c < 4; ++c) out[c] = texel(t, L, x, y, c);
+void sample_level(const OracleTexture& t, int L, int level, int filter, float s, float u, float out[4]) {
+  const int tw = std::max(1, t.width >> level), th = std::max(1, t.height >> level);
+  size_t off = 0;
+  for (int k = 0; k < level; ++k)
+    off += size_t(std::max(1, t.width >> k)) * size_t(std::max(1, t.height >> k)) * t.layers * 4;
+  float fw = float(tw), fh = float(th);
+  if (filter == 0) {
+    int x = wrap(int(std::floor(clampc(s * fw))), tw, t.wrap_s);
+    int y = wrap(int(std::floor(clampc(u * fh))), th, t.wrap_t);
+    for (int c = 0; c < 4; ++c) out[c] = texel(t, off, tw, th, L, x, y, c);
     return;
   }
   float fx = clampc(s * fw - 0.5f), fy = clampc(u * fh - 0.5f);
   float flx = std::floor(fx), fly = std::floor(fy);
   float a = fx - flx, b = fy - fly;
-  int x0 = wrap(int(flx), t.width, t.wrap_s), x1 = wrap(int(flx) + 1, t.width, t.wrap_s);
-  int y0 = wrap(int(fly), t.height, t.wrap_t), y1 = wrap(int(fly) + 1, t.height, t.wrap_t);
+  int x0 = wrap(int(flx), tw, t.wrap_s), x1 = wrap(int(flx) + 1, tw, t.wrap_s);
+  int y0 = wrap(int(fly), th, t.wrap_t), y1 = wrap(int(fly) + 1, th, t.wrap_t);
   for (int c = 0; c < 4; ++c) {
-    float t00 = texel(t, L, x0, y0, c), t10 = texel(t, L, x1, y0, c);
-    float t01 = texel(t, L, x0, y1, c), t11 = texel(t, L, x1, y1, c);
+    float t00 = texel(t, off, tw, th, L, x0, y0, c), t10 = texel(t, off, tw, th, L, x1, y0, c);
+    float t01 = texel(t, off, tw, th, L, x0, y1, c), t11 = texel(t, off, tw, th, L, x1, y1, c);
     float lo = fma_(a, t10 - t00, t00);
     float hi = fma_(a, t11 - t01, t01);
     out[c] = fma_(b, hi - lo, lo);
+  }
+}
+
+inline int clamp_layer(const OracleTexture& t, int layer) {
+  return layer < 0 ? 0 : (layer >= t.layers ? t.layers - 1 : layer);
+}
+
+void sample(const OracleTexture& t, int layer, float s, float u, float out[4]) {
+  sample_level(t, clamp_layer(t, layer), 0, t.filter, s, u, out);
+}
+
+// log2 by the atanh series of the mantissa normalised to [sqrt(1/2), sqrt(2)).
+float series_log2(float x) {
+  int e;
+  float m = std::frexp(x, &e);
+  if (m < 0.7071067690849304f) {
+    m = m * 2.0f;
+    e -= 1;
+  }
+  const float t = (m - 1.0f) / (m + 1.0f);
+  const float t2 = t * t;
+  float q = 0.1111111119389534f;
+  q = q * t2 + 0.1428571492433548f;
+  q = q * t2 + 0.20000000298023224f;
+  q = q * t2 + 0.3333333432674408f;
+  q = q * t2 + 1.0f;
+  return float(e) + (t * q) * 2.885390043258667f;
+}
+
+// Level-of-detail selection of OpenGL 4.6, 8.14 (see the kernel's sample_lod).
+void sample_lod(const OracleTexture& t, int layer, float s, float u, float lambda, float out[4]) {
+  const int L = clamp_layer(t, layer);
+  const float c = (t.filter == 1 && t.min_filter == 0 && t.mip_filter != 0) ? 0.5f : 0.0f;
+  if (!(lambda > c)) {
+    sample_level(t, L, 0, t.filter, s, u, out);
+    return;
+  }
+  const int q = t.levels - 1;
+  if (t.mip_filter == 0) {
+    sample_level(t, L, 0, t.min_filter, s, u, out);
+  } else if (t.mip_filter == 1) {
+    int d = lambda <= 0.5f ? 0 : int(std::ceil(lambda + 0.5f)) - 1;
+    if (d > q) d = q;
+    sample_level(t, L, d, t.min_filter, s, u, out);
+  } else if (lambda >= float(q)) {
+    sample_level(t, L, q, t.min_filter, s, u, out);
+  } else {
+    const float fl = std::floor(lambda);
+    const int d1 = int(fl);
+    const float f = lambda - fl;
+    float hi[4];
+    sample_level(t, L, d1, t.min_filter, s, u, out);
+    sample_level(t, L, d1 + 1, t.min_filter, s, u, hi);
+    for (int k = 0; k < 4; ++k) out[k] = fma_(f, hi[k] - out[k], out[k]);
   }
 }
 
@@ -310,7 +372,53 @@ void shade(const Frame& f, const OracleScene& sc, const OracleDraw& dr, const Tr
     const float* M = mat.matrix;
     float ts = M[6]; ts = fma_(M[0], u, ts); ts = fma_(M[3], v, ts);
     float tt = M[7]; tt = fma_(M[1], u, tt); tt = fma_(M[4], v, tt);
-    sample(f.tex[mat.texture], mat.layer, ts, tt, tc);
+    const OracleTexture& tex = f.tex[mat.texture];
+    if (tex.mip_filter == 0 && tex.min_filter == tex.filter) {
+      sample(tex, mat.layer, ts, tt, tc);
+    } else {
+      // Level of detail from the texel-coordinate derivatives across the
+      // pixel's 2x2 quad: the quad's pixel pair in this row (x) and column (y).
+      float ex[3], ey[3], ez[3];
+      for (int i = 0; i < 3; ++i) {
+        const V4& a = tri.c[(i + 1) % 3];
+        const V4& b = tri.c[(i + 2) % 3];
+        ex[i] = a.y * b.w - a.w * b.y;
+        ey[i] = a.w * b.x - a.x * b.w;
+        ez[i] = a.x * b.y - a.y * b.x;
+      }
+      float t0[2] = {0, 0}, t1[2] = {0, 0}, t2[2] = {0, 0};
+      if (m.texcoords)
+        for (int k = 0; k < 2; ++k) {
+          t0[k] = m.texcoords[tri.vi[0] * 2 + k];
+          t1[k] = m.texcoords[tri.vi[1] * 2 + k];
+          t2[k] = m.texcoords[tri.vi[2] * 2 + k];
+        }
+      auto st_at = [&](int x, int y, float& os, float& ot) {
+        const float qx = float(2 * x + 1 - sc.width) / float(sc.width);
+        const float qy = float(2 * y + 1 - sc.height) / float(sc.height);
+        const float a0 = fma_(ex[0], qx, fma_(ey[0], qy, ez[0]));
+        const float a1 = fma_(ex[1], qx, fma_(ey[1], qy, ez[1]));
+        const float a2 = fma_(ex[2], qx, fma_(ey[2], qy, ez[2]));
+        const float is = 1.0f / ((a0 + a1) + a2);
+        const float c0 = a0 * is, c1 = a1 * is, c2 = a2 * is;
+        const float uu = fma_(c2, t2[0], fma_(c1, t1[0], c0 * t0[0]));
+        const float ww = fma_(c2, t2[1], fma_(c1, t1[1], c0 * t0[1]));
+        os = fma_(M[3], ww, fma_(M[0], uu, M[6]));
+        ot = fma_(M[4], ww, fma_(M[1], uu, M[7]));
+      };
+      float sa, ta, sb, tb, scc, tcc, sd, td;
+      st_at(px & ~1, py, sa, ta);
+      st_at((px & ~1) + 1, py, sb, tb);
+      st_at(px, py & ~1, scc, tcc);
+      st_at(px, (py & ~1) + 1, sd, td);
+      const float fw = float(tex.width), fh = float(tex.height);
+      const float dux = (sb - sa) * fw, dvx = (tb - ta) * fh;
+      const float duy = (sd - scc) * fw, dvy = (td - tcc) * fh;
+      const float rx = std::sqrt(dux * dux + dvx * dvx), ry = std::sqrt(duy * duy + dvy * dvy);
+      const float rho = std::fmax(rx, ry);
+      const float lambda = rho > 0.0f ? (rho < 3.0e38f ? series_log2(rho) : 128.0f) : -1.0f;
+      sample_lod(tex, mat.layer, ts, tt, lambda, tc);
+    }
   }
   uint32_t packed = 0;
   if (mat.phong && f.max_lights > 0) {

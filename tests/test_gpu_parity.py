@@ -445,6 +445,40 @@ def test_scenes_into_async(pkg, procedural, ragged):
         r.scenesIntoAsync(pkg.Plane.Color, 5, 5, np.zeros((5, 40, 40, 4), np.uint8))
 
 
+@pytest.mark.parametrize("kw", [
+    dict(filter=1, minFilter=1, mipFilter=1, generateMipmap=True),
+    dict(filter=1, minFilter=2, mipFilter=1, generateMipmap=True),
+    dict(filter=0, minFilter=1, mipFilter=2, generateMipmap=True),
+    dict(filter=1, minFilter=2, mipFilter=2, generateMipmap=True),
+    dict(filter=1, minFilter=1, mipFilter=0),
+    dict(filter=0, minFilter=2, mipFilter=2, levels=True),
+], ids=["nn", "ln", "nl", "ll", "min_nearest_no_mips", "given_levels"])
+def test_mipmapped_floor_matches_oracle(pkg, kw):
+    """A checkered floor receding to the horizon (minified far away): level
+    of detail, level selection and filtering bit-exact against the oracle."""
+    from oracle.model import OracleRenderer, generate_mips
+    from test_mipmaps_host import floor_scene
+    kw = dict(kw)
+    if kw.pop("levels", False):
+        y, x = np.mgrid[0:64, 0:64]
+        rng = np.random.default_rng(3)
+        base = rng.integers(0, 256, (1, 64, 64, 4), dtype=np.uint8)
+        chain = [c[0] for c in generate_mips(base, 5)]   # 5 of the 7 possible levels
+        kw.update(levels=True)
+    outs = []
+    for r in (gpu_factory(pkg, 1)((96, 96), (1, 1), 0), OracleRenderer((96, 96), (1, 1), 0)):
+        if kw.get("levels"):
+            k2 = dict(kw)
+            k2["levels"] = len(chain)
+            floor_scene(r, k2, pixels=chain)
+        else:
+            floor_scene(r, kw)
+        r.draw()
+        outs.append(r)
+    gpu, cpu = outs
+    assert_parity([compare_scene(gpu, cpu, pkg, 0)])
+
+
 def test_unproject_device_matches_host(pkg):
     import torch
     p = S.perspective(60.0, 1.0, 0.01, 10.0)
