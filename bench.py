@@ -75,6 +75,31 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
+def barrier_sync(world):
+    """All ranks at the same point with their GPU work finished."""
+    import torch
+    if world > 1:
+        torch.distributed.barrier()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(value, world, device="cuda"):
+    """The largest `value` over all ranks (every rank gets it).  Replicas
+    render the same per-GPU work, so the job's time is the slowest rank's."""
+    if world == 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_frames_per_s(envs_per_rank, steps, world, total_ms_max):
+    """Whole-job throughput: the frames of every rank over the slowest rank's time."""
+    return envs_per_rank * steps * world / (total_ms_max / 1e3)
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -414,9 +439,7 @@ def main():
     sampler = ClockSampler(local_rank)
     sampler.start()
     time.sleep(0.3)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
+    barrier_sync(world)
     step_ms, raster_ms, prepare_ms = [], [], []
     tri = None
     for k in range(args.steps):
@@ -427,15 +450,10 @@ def main():
         raster_ms.append(st["raster_ms"])
         prepare_ms.append(st["prepare_ms"])
         tri = st["triangles"]
-    torch.cuda.synchronize()
+    barrier_sync(world)
     clocks = sampler.stop()
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    frames = wl.envs * args.steps * world
-    value = frames / (total_ms / 1e3)
+    total_ms = max_over_ranks(sum(step_ms), world)
+    value = job_frames_per_s(wl.envs, args.steps, world, total_ms)
 
     # ---- plain per-scene path
     plain_ms = []
