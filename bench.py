@@ -318,33 +318,41 @@ def replay_leg(pkg, procedural, wl, tuning, steps=5, warmup=2):
         cams.append([procedural.camera_keyframe(pkg, views[e]).to_string() for e in range(wl.envs)])
     big_c = torch.empty((wl.envs, h, w, 4), dtype=torch.uint8, pin_memory=True).numpy()
     big_d = torch.empty((wl.envs, h, w), dtype=torch.float32, pin_memory=True).numpy()
-    apply_s, render_s = [], []
 
-    def step(i):
+    def step(i, batch):
         t = time.perf_counter()
-        for e in range(wl.envs):
-            rr.set_environment_keyframe(e, cams[i][e])
-            rr.set_sensor_transforms_from_keyframe(e, "sensor_")
+        if batch:
+            rr.set_environment_keyframes_batch(cams[i], sensor_prefix="sensor_")
+        else:
+            for e in range(wl.envs):
+                rr.set_environment_keyframe(e, cams[i][e])
+                rr.set_sensor_transforms_from_keyframe(e, "sensor_")
         t1 = time.perf_counter()
         rr.render(big_c, big_d)
         return t1 - t, time.perf_counter() - t1
 
-    for i in range(warmup):
-        step(i)
-    for i in range(warmup, n):
-        a, b = step(i)
-        apply_s.append(a)
-        render_s.append(b)
-    total = sum(apply_s) + sum(render_s)
+    out = {}
+    for batch in (False, True):
+        apply_s, render_s = [], []
+        for i in range(warmup):
+            step(i, batch)
+        for i in range(warmup, n):
+            a, b = step(i, batch)
+            apply_s.append(a)
+            render_s.append(b)
+        total = sum(apply_s) + sum(render_s)
+        out[batch] = {"value": wl.envs * steps / total, "ms_per_step": 1e3 * total / steps,
+                      "keyframe_apply_ms": 1e3 * statistics.mean(apply_s),
+                      "render_ms": 1e3 * statistics.mean(render_s)}
     rr.close()
-    return {"value": wl.envs * steps / total, "unit": "frames/s", "envs": wl.envs, "steps": steps,
-            "ms_per_step": 1e3 * total / steps,
-            "keyframe_apply_ms": 1e3 * statistics.mean(apply_s),
-            "render_ms": 1e3 * statistics.mean(render_s),
-            "scene_load_s": load_s,
-            "d2h_bytes_per_step": int(big_c.nbytes + big_d.nbytes),
-            "timing": "host clock: per env set_environment_keyframe + "
-                      "set_sensor_transforms_from_keyframe, then render() into pinned host images"}
+    res = dict(out[False])
+    res.update({"unit": "frames/s", "envs": wl.envs, "steps": steps, "scene_load_s": load_s,
+                "d2h_bytes_per_step": int(big_c.nbytes + big_d.nbytes),
+                "timing": "host clock: per env set_environment_keyframe + "
+                          "set_sensor_transforms_from_keyframe, then render() into pinned host images"})
+    res["batched_keyframes"] = dict(out[True], timing="host clock: one set_environment_keyframes_batch "
+                                    "call (parse + apply + sensor transforms for every env), then render()")
+    return res
 
 
 def run_reference_impl(args):

@@ -154,6 +154,8 @@ PROTOTYPES = {
     "gbr_replay_set_environment_keyframe": (_ST, [_P, _U32, ctypes.c_char_p, _U64]),
     "gbr_replay_set_environment_keyframe_unwrapped": (_ST, [_P, _U32, ctypes.c_char_p, _U64]),
     "gbr_replay_set_keyframes": (_ST, [_P, _U32, ctypes.c_char_p, _U64]),
+    "gbr_replay_set_environment_keyframes": (_ST, [_P, _U32, _U32, ctypes.POINTER(ctypes.c_char_p),
+                                                  ctypes.POINTER(_U64), ctypes.c_char_p]),
     "gbr_replay_set_keyframe_index": (_ST, [_P, _U32, _I32]),
     "gbr_replay_keyframe_count": (_ST, [_P, _U32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
     "gbr_replay_user_transform": (_ST, [_P, _U32, ctypes.c_char_p, c_float_p, c_float_p,

@@ -17,12 +17,14 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <array>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <thread>
 
 #include "renderer.h"
 
@@ -730,6 +732,71 @@ gbr_status ReplayRenderer::set_keyframes_json(uint32_t env, const char* json, ui
   return GBR_OK;
 }
 
+// setEnvironmentKeyframe (+ setSensorTransformsFromKeyframe) for environments
+// first .. first + count - 1 in one call.  Every document is parsed before any
+// is applied, so a malformed one leaves all environments unchanged; large
+// batches are parsed on several host threads (the parser keeps no shared
+// state).  The keyframes are then applied in environment order, exactly as
+// the per-environment calls would.
+gbr_status ReplayRenderer::set_keyframe_batch(uint32_t first, uint32_t count, const char* const* json,
+                                              const uint64_t* length, const char* sensor_prefix) {
+  if (!renderer_) return fail(GBR_ERROR_STATE, "setEnvironmentKeyframes: the replay renderer is closed");
+  if (uint64_t(first) + count > players_.size())
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "setEnvironmentKeyframes: environments " + std::to_string(first) +
+                                                " + " + std::to_string(count) + " exceed the environment count " +
+                                                std::to_string(players_.size()));
+  std::vector<Keyframe> ks(count);
+  std::vector<std::string> errs(count);
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < count; ++i) total += json[i] ? length[i] : 0;
+  auto parse_range = [&](uint32_t b, uint32_t e) {
+    for (uint32_t i = b; i < e; ++i) {
+      if (!json[i]) {
+        errs[i] = "null keyframe";
+        continue;
+      }
+      Json doc;
+      JsonParser jp{json[i], json[i] + length[i], {}};
+      if (!jp.parse(doc)) {
+        errs[i] = "bad JSON: " + jp.err;
+        continue;
+      }
+      const Json* obj = doc.get("keyframe");
+      if (!obj) {
+        errs[i] = "no \"keyframe\" member";
+        continue;
+      }
+      parse_keyframe(*obj, ks[i], errs[i]);
+    }
+  };
+  // Threads pay off once the batch is a few hundred kilobytes of JSON.
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned nt = total < (256u << 10) ? 1u : std::min({hw, 16u, std::max(1u, count / 32u)});
+  if (nt <= 1) {
+    parse_range(0, count);
+  } else {
+    std::vector<std::thread> pool;
+    const uint32_t per = (count + nt - 1) / nt;
+    for (unsigned t = 1; t < nt; ++t) {
+      const uint32_t b = std::min(count, t * per), e = std::min(count, b + per);
+      if (b < e) pool.emplace_back(parse_range, b, e);
+    }
+    parse_range(0, std::min(count, per));
+    for (auto& th : pool) th.join();
+  }
+  for (uint32_t i = 0; i < count; ++i)
+    if (!errs[i].empty())
+      return fail(GBR_ERROR_INVALID_ARGUMENT,
+                  "setEnvironmentKeyframes: environment " + std::to_string(first + i) + ": " + errs[i]);
+  const std::string prefix = sensor_prefix ? sensor_prefix : "";
+  for (uint32_t i = 0; i < count; ++i) {
+    if (gbr_status s = players_[first + i]->set_single_keyframe(std::move(ks[i]))) return s;
+    if (sensor_prefix)
+      if (gbr_status s = set_sensor_from_keyframe(first + i, prefix)) return s;
+  }
+  return GBR_OK;
+}
+
 gbr_status ReplayRenderer::set_sensor_transform(uint32_t env, const float m[16]) {
   if (gbr_status s = check_env(env, "setSensorTransform")) return s;
   float view[16];
@@ -955,6 +1022,18 @@ gbr_status gbr_replay_set_environment_keyframe_unwrapped(gbr_replay* r, uint32_t
                                                          uint64_t length) {
   GBR_ARG(json);
   return guarded(r, [&](ReplayRenderer& rr) { return rr.set_keyframe_json(env, json, length, false); });
+}
+
+gbr_status gbr_replay_set_environment_keyframes(gbr_replay* r, uint32_t first_env, uint32_t count,
+                                                const char* const* json, const uint64_t* length,
+                                                const char* sensor_prefix) {
+  if (count) {
+    GBR_ARG(json);
+    GBR_ARG(length);
+  }
+  return guarded(r, [&](ReplayRenderer& rr) {
+    return rr.set_keyframe_batch(first_env, count, json, length, sensor_prefix);
+  });
 }
 
 gbr_status gbr_replay_set_keyframes(gbr_replay* r, uint32_t env, const char* json, uint64_t length) {

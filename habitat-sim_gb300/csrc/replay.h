@@ -161,6 +161,8 @@ class ReplayRenderer {
   gbr_status clear_environment(uint32_t env);
   gbr_status set_keyframe_json(uint32_t env, const char* json, uint64_t n, bool wrapped);
   gbr_status set_keyframes_json(uint32_t env, const char* json, uint64_t n);
+  gbr_status set_keyframe_batch(uint32_t first, uint32_t count, const char* const* json,
+                                const uint64_t* length, const char* sensor_prefix);
   Player& player(uint32_t env) { return *players_[env]; }
   gbr_status set_sensor_transform(uint32_t env, const float m[16]);
   gbr_status set_sensor_from_keyframe(uint32_t env, const std::string& prefix);

@@ -211,6 +211,20 @@ class ReplayRenderer:
         data = _cstr(keyframe)
         check(self._lib.gbr_replay_set_environment_keyframe(self._h, int(env_index), data, len(data)))
 
+    def set_environment_keyframes_batch(self, keyframes, first_env=0, sensor_prefix=None):
+        """``set_environment_keyframe(first_env + i, keyframes[i])`` for every
+        i in one native call, then, when ``sensor_prefix`` is given,
+        ``set_sensor_transforms_from_keyframe`` for each.  Every keyframe is
+        parsed before any is applied: a malformed one raises and changes
+        nothing."""
+        data = [_cstr(k) for k in keyframes]
+        n = len(data)
+        ptrs = (ctypes.c_char_p * n)(*data)
+        lens = (ctypes.c_uint64 * n)(*map(len, data))
+        check(self._lib.gbr_replay_set_environment_keyframes(
+            self._h, int(first_env), n, ptrs, lens,
+            None if sensor_prefix is None else _cstr(sensor_prefix)))
+
     def set_environment_keyframe_unwrapped(self, env_index, keyframe):
         data = _cstr(keyframe)
         check(self._lib.gbr_replay_set_environment_keyframe_unwrapped(self._h, int(env_index), data,

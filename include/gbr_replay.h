@@ -82,6 +82,17 @@ gbr_status gbr_replay_set_environment_keyframe(gbr_replay* r, uint32_t env, cons
 /* setEnvironmentKeyframeUnwrapped (:68-73): the keyframe object itself. */
 gbr_status gbr_replay_set_environment_keyframe_unwrapped(gbr_replay* r, uint32_t env,
                                                          const char* json, uint64_t length);
+/* setEnvironmentKeyframe for environments first_env .. first_env + count - 1
+ * in one call (json[i], length[i] go to environment first_env + i), followed,
+ * when sensor_prefix is not NULL, by setSensorTransformsFromKeyframe(env,
+ * sensor_prefix) for each (AbstractReplayRenderer.cpp:61-66, 83-92).  All documents
+ * are parsed before any is applied: a malformed one returns
+ * GBR_ERROR_INVALID_ARGUMENT naming its environment and changes nothing.
+ * Large batches are parsed on several host threads.  Same results as the
+ * per-environment calls in environment order. */
+gbr_status gbr_replay_set_environment_keyframes(gbr_replay* r, uint32_t first_env, uint32_t count,
+                                                const char* const* json, const uint64_t* length,
+                                                const char* sensor_prefix);
 /* Player::readKeyframesFromJsonDocument + setKeyframeIndex(-1)
  * (Player.cpp:103-106, 142-152): a {"keyframes": [...]} document for the
  * environment's player; nothing is applied until gbr_replay_set_keyframe_index. */

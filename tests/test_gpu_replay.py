@@ -213,6 +213,65 @@ def test_replay_packed_destinations(pkg):
     gpu.close()
 
 
+def test_replay_keyframe_batch(pkg):
+    """One set_environment_keyframes_batch call equals the per-environment
+    setEnvironmentKeyframe + setSensorTransformsFromKeyframe calls; a
+    malformed keyframe anywhere in the batch changes no environment."""
+    n, res = 5, (24, 32)
+    one, _ = make_pair(pkg, n, res)
+    bat, _ = make_pair(pkg, n, res)
+    ks = [scene_keyframes(pkg, e) for e in range(n)]
+    for e in range(n):
+        one.set_environment_keyframe(e, ks[e][0].to_string())
+        one.set_environment_keyframe(e, ks[e][1].to_string())
+        one.set_sensor_transforms_from_keyframe(e, "sensor_")
+    bat.set_environment_keyframes_batch([k.to_string() for k, _ in ks])
+    bat.set_environment_keyframes_batch([k2.to_string() for _, k2 in ks], sensor_prefix="sensor_")
+    a = [np.zeros(res + (4,), np.uint8) for _ in range(n)]
+    b = [np.zeros(res + (4,), np.uint8) for _ in range(n)]
+    one.render(a)
+    bat.render(b)
+    for e in range(n):
+        assert np.array_equal(a[e], b[e])
+        assert np.array_equal(one.renderer.transformations(e), bat.renderer.transformations(e))
+    before = [bat.renderer.transformations(e).copy() for e in range(n)]
+    moved = [pkg.Keyframe().update(0, (0.0, 0.0, -9.0)).to_string() for _ in range(3)]
+    with pytest.raises(pkg.GbrError, match="environment 4: bad JSON"):
+        bat.set_environment_keyframes_batch(moved + ["{\"keyframe\": ["], first_env=1)
+    for e in range(n):
+        assert np.array_equal(bat.renderer.transformations(e), before[e])
+    with pytest.raises(pkg.GbrError, match="exceed the environment count"):
+        bat.set_environment_keyframes_batch(moved, first_env=3)
+    bat.set_environment_keyframes_batch([])
+    one.close()
+    bat.close()
+
+
+def test_replay_keyframe_batch_threads(pkg):
+    """A batch large enough to be parsed on several host threads (padded
+    documents) applies the same keyframes as the per-environment calls."""
+    n, res = 96, (8, 8)
+    one, _ = make_pair(pkg, n, res)
+    bat, _ = make_pair(pkg, n, res)
+    docs = []
+    for e in range(n):
+        k, _ = scene_keyframes(pkg, e % 7)
+        docs.append(k.to_string() + " " * 4096)
+    for e in range(n):
+        one.set_environment_keyframe(e, docs[e])
+        one.set_sensor_transforms_from_keyframe(e, "sensor_")
+    bat.set_environment_keyframes_batch(docs, sensor_prefix="sensor_")
+    a = np.zeros((n,) + res + (4,), np.uint8)
+    b = np.zeros((n,) + res + (4,), np.uint8)
+    one.render(a)
+    bat.render(b)
+    assert np.array_equal(a, b)
+    for e in range(n):
+        assert np.array_equal(one.renderer.transformations(e), bat.renderer.transformations(e))
+    one.close()
+    bat.close()
+
+
 def test_unproject_matches_classic_rays(pkg):
     """testUnproject's rays (BatchReplayRendererTest.cpp:210-255): sensor at
     (1, 2, 3), 512 x 384 (height x width), hfov 90."""
