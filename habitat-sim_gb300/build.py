@@ -21,7 +21,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["kernels.cu", "noise.cu", "hbao.cu"]
 CPP_SOURCES = ["renderer.cpp", "importer.cpp", "capi.cpp", "replay.cpp"]
-HEADERS = ["kernels.h", "records.h", "renderer.h", "importer.h", "json.h", "replay.h", "hbao.h"]
+HEADERS = ["kernels.h", "records.h", "renderer.h", "importer.h", "json.h", "replay.h", "hbao.h", "mips.h",
+           "trace.h"]
 
 
 def _cuda_home():

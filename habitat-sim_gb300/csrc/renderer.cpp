@@ -20,6 +20,7 @@
 #include "hbao.h"
 #include "importer.h"
 #include "mips.h"
+#include "trace.h"
 
 namespace gbr {
 
@@ -286,6 +287,7 @@ Renderer::~Renderer() {
 
 // ----------------------------------------------------------- resources
 gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
+  TraceRange trace_("gbr.add_mesh");
   if (!m.positions || (m.index_count && !m.indices))
     return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: positions and indices are required");
   for (uint32_t i = 0; i < m.index_count; ++i)
@@ -365,6 +367,7 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
 }
 
 gbr_status Renderer::add_texture(const gbr_texture_data& t, uint32_t* id) {
+  TraceRange trace_("gbr.add_texture");
   if (t.width <= 0 || t.height <= 0 || t.layers <= 0 || !t.rgba8)
     return fail(GBR_ERROR_INVALID_ARGUMENT, "addTexture: empty texture");
   if (t.filter < 0 || t.filter > 1 || t.wrap_s < 0 || t.wrap_s > 2 || t.wrap_t < 0 || t.wrap_t > 2 ||
@@ -511,6 +514,7 @@ void Renderer::build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32
 }
 
 gbr_status Renderer::add_file(const char* filename, uint32_t flags, const char* name) {
+  TraceRange trace_("gbr.add_file");
   if (!filename) return fail(GBR_ERROR_INVALID_ARGUMENT, "addFile: null filename");
   ImportedFile f;
   std::string err;
@@ -1267,6 +1271,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
 }
 
 gbr_status Renderer::draw(cudaStream_t stream, uint32_t mode, bool use_graph) {
+  TraceRange trace_("gbr.draw");
   cudaSetDevice(device_);
   if (use_graph && mode == GBR_DRAW_BATCHED && stream == nullptr) stream = own_stream_;
   if (structure_dirty_)
@@ -1368,6 +1373,7 @@ void* Renderer::plane_ptr(uint32_t plane, size_t* elem) const {
 
 gbr_status Renderer::image_into_async(uint32_t plane, const int32_t* rect, void* dst,
                                       uint64_t row_bytes) {
+  TraceRange trace_("gbr.image_into");
   size_t elem;
   const char* src = static_cast<const char*>(plane_ptr(plane, &elem));
   if (!src) return fail(GBR_ERROR_INVALID_ARGUMENT, "imageIntoAsync: plane not enabled");
@@ -1398,6 +1404,7 @@ gbr_status Renderer::image_into_async(uint32_t plane, const int32_t* rect, void*
 // Hbao::drawEffect, classic (src/esp/gfx_batch/Hbao.cpp:874-935), over all
 // enabled scenes at once (three launches, csrc/hbao.cu).
 gbr_status Renderer::hbao(const gbr_hbao_config& c, cudaStream_t stream) {
+  TraceRange trace_("gbr.hbao");
   if (!(cfg_.planes & GBR_PLANE_COLOR) || !(cfg_.planes & GBR_PLANE_LINEAR_DEPTH))
     return fail(GBR_ERROR_STATE, "Hbao: the renderer needs its colour and linear-depth planes");
   HbaoParams params;
@@ -1435,6 +1442,7 @@ gbr_status Renderer::hbao(const gbr_hbao_config& c, cudaStream_t stream) {
 }
 
 gbr_status Renderer::scenes_into_async(uint32_t plane, uint32_t first, uint32_t count, void* dst) {
+  TraceRange trace_("gbr.scenes_into");
   size_t elem;
   const char* src = static_cast<const char*>(plane_ptr(plane, &elem));
   if (!src) return fail(GBR_ERROR_INVALID_ARGUMENT, "scenesIntoAsync: plane not enabled");
@@ -1479,6 +1487,7 @@ gbr_status Renderer::scenes_into_async(uint32_t plane, uint32_t first, uint32_t 
 }
 
 gbr_status Renderer::readback_wait() {
+  TraceRange trace_("gbr.readback_wait");
   if (!copy_stream_) return GBR_OK;
   cudaSetDevice(device_);
   GBR_CUDA(cudaStreamSynchronize(copy_stream_), "readback wait");

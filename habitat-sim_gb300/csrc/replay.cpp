@@ -27,6 +27,7 @@
 #include <thread>
 
 #include "renderer.h"
+#include "trace.h"
 
 namespace gbr {
 namespace replay {
@@ -698,6 +699,7 @@ gbr_status ReplayRenderer::clear_environment(uint32_t env) {
 }
 
 gbr_status ReplayRenderer::set_keyframe_json(uint32_t env, const char* json, uint64_t n, bool wrapped) {
+  TraceRange trace_("replay.set_keyframe");
   if (gbr_status s = check_env(env, "setEnvironmentKeyframe")) return s;
   Json doc;
   JsonParser jp{json, json + n, {}};
@@ -740,6 +742,7 @@ gbr_status ReplayRenderer::set_keyframes_json(uint32_t env, const char* json, ui
 // the per-environment calls would.
 gbr_status ReplayRenderer::set_keyframe_batch(uint32_t first, uint32_t count, const char* const* json,
                                               const uint64_t* length, const char* sensor_prefix) {
+  TraceRange trace_("replay.set_keyframes_batch");
   if (!renderer_) return fail(GBR_ERROR_STATE, "setEnvironmentKeyframes: the replay renderer is closed");
   if (uint64_t(first) + count > players_.size())
     return fail(GBR_ERROR_INVALID_ARGUMENT, "setEnvironmentKeyframes: environments " + std::to_string(first) +
@@ -823,6 +826,7 @@ gbr_status ReplayRenderer::set_sensor_from_keyframe(uint32_t env, const std::str
 
 gbr_status ReplayRenderer::render(void* stream, uint32_t nc, void* const* color, uint64_t crow, uint32_t nd,
                                   void* const* depth, uint64_t drow) {
+  TraceRange trace_("replay.render");
   if (!renderer_) return fail(GBR_ERROR_STATE, "render: the replay renderer is closed");
   const uint32_t n = env_count();
   if (nc && nc != n)
