@@ -734,6 +734,64 @@ gbr_status ReplayRenderer::set_keyframes_json(uint32_t env, const char* json, ui
   return GBR_OK;
 }
 
+WorkerPool::WorkerPool(unsigned threads) {
+  for (unsigned t = 0; t < threads; ++t) threads_.emplace_back([this] { work(); });
+}
+
+WorkerPool::~WorkerPool() {
+  {
+    std::lock_guard<std::mutex> lk(m_);
+    stop_ = true;
+  }
+  start_.notify_all();
+  for (auto& t : threads_) t.join();
+}
+
+void WorkerPool::drain() {
+  for (;;) {
+    const uint32_t b = next_.fetch_add(chunk_);
+    if (b >= count_) return;
+    (*fn_)(b, std::min(count_, b + chunk_));
+  }
+}
+
+void WorkerPool::work() {
+  uint64_t seen = 0;
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(m_);
+      start_.wait(lk, [&] { return stop_ || generation_ != seen; });
+      if (stop_) return;
+      seen = generation_;
+    }
+    drain();
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      --pending_;
+    }
+    done_.notify_all();
+  }
+}
+
+void WorkerPool::run(uint32_t count, uint32_t chunk, const std::function<void(uint32_t, uint32_t)>& fn) {
+  {
+    std::lock_guard<std::mutex> lk(m_);
+    fn_ = &fn;
+    count_ = count;
+    chunk_ = std::max(1u, chunk);
+    next_.store(0);
+    pending_ = unsigned(threads_.size());
+    ++generation_;
+  }
+  start_.notify_all();
+  drain();
+  // Every worker takes part in every generation, so none can still be
+  // reading fn_ once they have all reported back.
+  std::unique_lock<std::mutex> lk(m_);
+  done_.wait(lk, [&] { return pending_ == 0; });
+  fn_ = nullptr;
+}
+
 // setEnvironmentKeyframe (+ setSensorTransformsFromKeyframe) for environments
 // first .. first + count - 1 in one call.  Every document is parsed before any
 // is applied, so a malformed one leaves all environments unchanged; large
@@ -750,42 +808,39 @@ gbr_status ReplayRenderer::set_keyframe_batch(uint32_t first, uint32_t count, co
                                                 std::to_string(players_.size()));
   std::vector<Keyframe> ks(count);
   std::vector<std::string> errs(count);
-  uint64_t total = 0;
-  for (uint32_t i = 0; i < count; ++i) total += json[i] ? length[i] : 0;
-  auto parse_range = [&](uint32_t b, uint32_t e) {
+  // Runs on worker threads too: nothing may escape it.
+  const std::function<void(uint32_t, uint32_t)> parse_range = [&](uint32_t b, uint32_t e) {
     for (uint32_t i = b; i < e; ++i) {
       if (!json[i]) {
         errs[i] = "null keyframe";
         continue;
       }
-      Json doc;
-      JsonParser jp{json[i], json[i] + length[i], {}};
-      if (!jp.parse(doc)) {
-        errs[i] = "bad JSON: " + jp.err;
-        continue;
+      try {
+        Json doc;
+        JsonParser jp{json[i], json[i] + length[i], {}};
+        if (!jp.parse(doc)) {
+          errs[i] = "bad JSON: " + jp.err;
+          continue;
+        }
+        const Json* obj = doc.get("keyframe");
+        if (!obj) {
+          errs[i] = "no \"keyframe\" member";
+          continue;
+        }
+        parse_keyframe(*obj, ks[i], errs[i]);
+      } catch (const std::exception& ex) {
+        errs[i] = std::string("parse failed: ") + ex.what();
       }
-      const Json* obj = doc.get("keyframe");
-      if (!obj) {
-        errs[i] = "no \"keyframe\" member";
-        continue;
-      }
-      parse_keyframe(*obj, ks[i], errs[i]);
     }
   };
-  // Threads pay off once the batch is a few hundred kilobytes of JSON.
+  // Parsing costs about a microsecond per small keyframe: batches of a few
+  // hundred keyframes and more are split over the worker threads.
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const unsigned nt = total < (256u << 10) ? 1u : std::min({hw, 16u, std::max(1u, count / 32u)});
-  if (nt <= 1) {
-    parse_range(0, count);
+  if (count >= 256 && hw > 1) {
+    if (!pool_) pool_.reset(new WorkerPool(std::min(hw, 16u) - 1));
+    pool_->run(count, 32, parse_range);
   } else {
-    std::vector<std::thread> pool;
-    const uint32_t per = (count + nt - 1) / nt;
-    for (unsigned t = 1; t < nt; ++t) {
-      const uint32_t b = std::min(count, t * per), e = std::min(count, b + per);
-      if (b < e) pool.emplace_back(parse_range, b, e);
-    }
-    parse_range(0, std::min(count, per));
-    for (auto& th : pool) th.join();
+    parse_range(0, count);
   }
   for (uint32_t i = 0; i < count; ++i)
     if (!errs[i].empty())
