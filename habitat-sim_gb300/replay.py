@@ -219,10 +219,17 @@ class ReplayRenderer:
         nothing."""
         data = [_cstr(k) for k in keyframes]
         n = len(data)
-        ptrs = (ctypes.c_char_p * n)(*data)
-        lens = (ctypes.c_uint64 * n)(*map(len, data))
+        # One joined buffer and numpy-built pointer/length arrays: building
+        # ctypes arrays element by element costs about a microsecond each.
+        lens = np.fromiter(map(len, data), np.uint64, n)
+        buf = np.frombuffer(b"".join(data), np.uint8) if n else np.zeros(1, np.uint8)
+        ptrs = np.zeros(n, np.uint64)
+        if n:
+            np.cumsum(lens[:-1], out=ptrs[1:])
+            ptrs += np.uint64(buf.ctypes.data)
         check(self._lib.gbr_replay_set_environment_keyframes(
-            self._h, int(first_env), n, ptrs, lens,
+            self._h, int(first_env), n, ptrs.ctypes.data_as(ctypes.POINTER(ctypes.c_char_p)),
+            lens.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
             None if sensor_prefix is None else _cstr(sensor_prefix)))
 
     def set_environment_keyframe_unwrapped(self, env_index, keyframe):
