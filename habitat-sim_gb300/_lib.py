@@ -173,6 +173,7 @@ PROTOTYPES = {
     "gbr_redwood_noise_simulate_host": (_ST, [_P, c_float_p, _I32, _I32, c_float_p]),
     "gbr_redwood_noise_simulate_tiles": (_ST, [_P, _P, _P, ctypes.c_int64, _I32, _I32, _I32, _I32,
                                                _P]),
+    "gbr_redwood_noise_simulate_images": (_ST, [_P, _P, _P, ctypes.POINTER(ctypes.c_int64), _I32, _P]),
     "gbr_redwood_noise_set_state": (_ST, [_P, _U64, _U64]),
     "gbr_redwood_noise_get_state": (_ST, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     "gbr_normal_quantile_table": (_ST, [c_float_p, _U32]),

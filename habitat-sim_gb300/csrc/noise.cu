@@ -74,66 +74,98 @@ struct TileArgs {
   uint32_t key0, key1, call0, call1;
 };
 
-__global__ void __launch_bounds__(256) redwood_kernel(TileArgs a) {
-  const int pixels = a.tw * a.th;
-  const float ymax = float(a.th - 1), xmax = float(a.tw - 1);
-  for (int img = blockIdx.y; img < a.count; img += gridDim.y) {
-    const long long ox = (long long)(img % a.tiles_x) * a.tw, oy = (long long)(img / a.tiles_x) * a.th;
-    const float* src = a.src + oy * a.pitch + ox;
-    float* dst = a.dst + oy * a.pitch + ox;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < pixels; idx += gridDim.x * blockDim.x) {
-      uint32_t c[4] = {uint32_t(idx), uint32_t(img), a.call0, a.call1};
-      philox4x32_10(c, a.key0, a.key1);
-      const float n0 = normal_variate(c[0], a.table), n1 = normal_variate(c[1], a.table),
-                  n2 = normal_variate(c[2], a.table);
-      const int r = idx / a.tw, col = idx % a.tw;
-      const int y = int(__fadd_rn(fminf(fmaxf(__fadd_rn(float(r), __fmul_rn(__fmul_rn(n0, 0.25f), a.mult)),
-                                              0.0f),
-                                        ymax),
-                                  0.5f));
-      const int x = int(__fadd_rn(fminf(fmaxf(__fadd_rn(float(col), __fmul_rn(__fmul_rn(n1, 0.25f), a.mult)),
-                                              0.0f),
-                                        xmax),
-                                  0.5f));
-      const float d = src[(long long)(y - y % 2) * a.pitch + (x - x % 2)];
-      float out = 0.0f;
-      if (!(d >= 10.0f)) {
-        // Remap to the model's 640 x 480 sensor (a 1-pixel axis maps to 0).
-        const int ux = xmax > 0.0f ? int(__fadd_rn(__fmul_rn(__fdiv_rn(float(x), xmax), 639.0f), 0.5f)) : 0;
-        const int uy = ymax > 0.0f ? int(__fadd_rn(__fmul_rn(__fdiv_rn(float(y), ymax), 479.0f), 0.5f)) : 0;
-        const int i2 = int(__fdiv_rn(__fadd_rn(d, 1.0f), 2.0f));
-        const int i1 = i2 - 1;
-        const float w = __fdiv_rn(__fsub_rn(d, __fadd_rn(__fmul_rn(float(i1), 2.0f), 1.0f)), 2.0f);
-        const float* cell = a.model + ((uy / 6) * kModelCols + ux / 8) * kModelDims;
-        // Bins clamped to 0..4 (the reference clamps the upper bin only from
-        // above: equal for every depth >= 0).
-        const float f = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, w), __ldg(cell + min(max(i1, 0), 4))),
-                                  __fmul_rn(w, __ldg(cell + min(max(i2, 0), 4))));
-        const float ud = f < 1e-5f ? 0.0f : __fdiv_rn(d, f);
-        if (ud != 0.0f) {
-          // round((35.130 / d' + noise) * 8) is defined in double.  The float
-          // evaluation differs from it by less than `margin` (three roundings
-          // of at most 2^-24 relative each), so it rounds to the same integer
-          // unless it lies within the margin of a half; only those pixels
-          // take the double path (FP64 throughput is low on this part).
-          const float nz = __fmul_rn(__fmul_rn(n2, 0.027778f), a.mult);
-          const float inv = __fdiv_rn(35.130f, ud);
-          const float qf = __fmul_rn(__fadd_rn(inv, nz), 8.0f);
-          const float margin = __fmul_rn(1e-6f, __fadd_rn(fabsf(qf), __fmul_rn(8.0f, fabsf(nz))));
-          const float frac = fabsf(__fsub_rn(qf, truncf(qf)));
-          float denom;
-          if (fabsf(__fsub_rn(frac, 0.5f)) > margin && isfinite(qf)) {
-            denom = roundf(qf);
-          } else {
-            const double q = (double(35.130f) / double(ud) + double(nz)) * 8.0;
-            denom = float(round(q));
-          }
-          out = denom > 1e-5f ? __fdiv_rn(35.130f * 8.0f, denom) : 0.0f;
-        }
+// One output pixel (row-major index idx) of image img, whose top-left pixel
+// is src / dst with `pitch` floats per row and tw x th pixels.
+__device__ __forceinline__ void noise_pixel(const TileArgs& a, int img, int idx, const float* src, float* dst,
+                                            long long pitch, int tw, int th) {
+  const float ymax = float(th - 1), xmax = float(tw - 1);
+  uint32_t c[4] = {uint32_t(idx), uint32_t(img), a.call0, a.call1};
+  philox4x32_10(c, a.key0, a.key1);
+  const float n0 = normal_variate(c[0], a.table), n1 = normal_variate(c[1], a.table),
+              n2 = normal_variate(c[2], a.table);
+  const int r = idx / tw, col = idx % tw;
+  const int y = int(__fadd_rn(fminf(fmaxf(__fadd_rn(float(r), __fmul_rn(__fmul_rn(n0, 0.25f), a.mult)),
+                                          0.0f),
+                                    ymax),
+                              0.5f));
+  const int x = int(__fadd_rn(fminf(fmaxf(__fadd_rn(float(col), __fmul_rn(__fmul_rn(n1, 0.25f), a.mult)),
+                                          0.0f),
+                                    xmax),
+                              0.5f));
+  const float d = src[(long long)(y - y % 2) * pitch + (x - x % 2)];
+  float out = 0.0f;
+  if (!(d >= 10.0f)) {
+    // Remap to the model's 640 x 480 sensor (a 1-pixel axis maps to 0).
+    const int ux = xmax > 0.0f ? int(__fadd_rn(__fmul_rn(__fdiv_rn(float(x), xmax), 639.0f), 0.5f)) : 0;
+    const int uy = ymax > 0.0f ? int(__fadd_rn(__fmul_rn(__fdiv_rn(float(y), ymax), 479.0f), 0.5f)) : 0;
+    const int i2 = int(__fdiv_rn(__fadd_rn(d, 1.0f), 2.0f));
+    const int i1 = i2 - 1;
+    const float w = __fdiv_rn(__fsub_rn(d, __fadd_rn(__fmul_rn(float(i1), 2.0f), 1.0f)), 2.0f);
+    const float* cell = a.model + ((uy / 6) * kModelCols + ux / 8) * kModelDims;
+    // Bins clamped to 0..4 (the reference clamps the upper bin only from
+    // above: equal for every depth >= 0).
+    const float f = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, w), __ldg(cell + min(max(i1, 0), 4))),
+                              __fmul_rn(w, __ldg(cell + min(max(i2, 0), 4))));
+    const float ud = f < 1e-5f ? 0.0f : __fdiv_rn(d, f);
+    if (ud != 0.0f) {
+      // round((35.130 / d' + noise) * 8) is defined in double.  The float
+      // evaluation differs from it by less than `margin` (three roundings
+      // of at most 2^-24 relative each), so it rounds to the same integer
+      // unless it lies within the margin of a half; only those pixels
+      // take the double path (FP64 throughput is low on this part).
+      const float nz = __fmul_rn(__fmul_rn(n2, 0.027778f), a.mult);
+      const float inv = __fdiv_rn(35.130f, ud);
+      const float qf = __fmul_rn(__fadd_rn(inv, nz), 8.0f);
+      const float margin = __fmul_rn(1e-6f, __fadd_rn(fabsf(qf), __fmul_rn(8.0f, fabsf(nz))));
+      const float frac = fabsf(__fsub_rn(qf, truncf(qf)));
+      float denom;
+      if (fabsf(__fsub_rn(frac, 0.5f)) > margin && isfinite(qf)) {
+        denom = roundf(qf);
+      } else {
+        const double q = (double(35.130f) / double(ud) + double(nz)) * 8.0;
+        denom = float(round(q));
       }
-      dst[(long long)r * a.pitch + col] = out;
+      out = denom > 1e-5f ? __fdiv_rn(35.130f * 8.0f, denom) : 0.0f;
     }
   }
+  dst[(long long)r * pitch + col] = out;
+}
+
+// Images as the tiles of a grid: blockIdx.y walks images, x their pixels.
+__global__ void __launch_bounds__(256) redwood_kernel(TileArgs a) {
+  const int pixels = a.tw * a.th;
+  for (int img = blockIdx.y; img < a.count; img += gridDim.y) {
+    const long long base =
+        (long long)(img / a.tiles_x) * a.th * a.pitch + (long long)(img % a.tiles_x) * a.tw;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < pixels; idx += gridDim.x * blockDim.x)
+      noise_pixel(a, img, idx, a.src + base, a.dst + base, a.pitch, a.tw, a.th);
+  }
+}
+
+// Images anywhere in the plane: layout[4i..4i+3] = {offset, pitch, width,
+// height} of image i, and blocks[i] .. blocks[i+1]-1 are the 256-pixel
+// blocks of image i (a prefix sum), so the grid has one block per 256
+// pixels of the batch whatever the mix of sizes.
+__global__ void __launch_bounds__(256) redwood_images_kernel(TileArgs a, const long long* layout,
+                                                             const long long* blocks) {
+  __shared__ int s_img;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = a.count;  // blocks[lo] <= blockIdx.x < blocks[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (blocks[mid] <= (long long)blockIdx.x)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    s_img = lo;
+  }
+  __syncthreads();
+  const int img = s_img;
+  const long long base = layout[4 * img], pitch = layout[4 * img + 1];
+  const int tw = int(layout[4 * img + 2]), th = int(layout[4 * img + 3]);
+  const int idx = int((long long)blockIdx.x - blocks[img]) * 256 + int(threadIdx.x);
+  if (idx < tw * th) noise_pixel(a, img, idx, a.src + base, a.dst + base, pitch, tw, th);
 }
 
 // Standard normal quantile in double: Halley steps on erfc from the
@@ -186,6 +218,9 @@ struct gbr_redwood_noise {
   float* in = nullptr;
   float* out = nullptr;
   size_t cap = 0;  // floats in `in` and `out`
+  long long* layout = nullptr;  // device copy of the last per-image layout
+  size_t layout_cap = 0;        // int64 values it holds
+  cudaEvent_t layout_read = nullptr;  // recorded after the launch that reads it
   int sms = 1;
 };
 
@@ -203,8 +238,8 @@ struct DeviceScope {
   }
 };
 
-gbr_status launch(gbr_redwood_noise* m, const float* src, float* dst, long long pitch, int tw, int th,
-                  int tiles_x, int count, cudaStream_t stream) {
+TileArgs make_args(gbr_redwood_noise* m, const float* src, float* dst, long long pitch, int tw, int th,
+                   int tiles_x, int count) {
   TileArgs a;
   a.src = src;
   a.dst = dst;
@@ -221,6 +256,12 @@ gbr_status launch(gbr_redwood_noise* m, const float* src, float* dst, long long 
   a.call0 = uint32_t(m->counter);
   a.call1 = uint32_t(m->counter >> 32);
   ++m->counter;
+  return a;
+}
+
+gbr_status launch(gbr_redwood_noise* m, const float* src, float* dst, long long pitch, int tw, int th,
+                  int tiles_x, int count, cudaStream_t stream) {
+  const TileArgs a = make_args(m, src, dst, pitch, tw, th, tiles_x, count);
   const int pixels = tw * th;
   const int per_image = std::max(1, std::min((pixels + 255) / 256, 8 * m->sms));
   const int images = std::max(1, std::min(count, 65535));
@@ -279,6 +320,8 @@ void gbr_redwood_noise_destroy(gbr_redwood_noise* m) {
   cudaFree(m->table);
   cudaFree(m->in);
   cudaFree(m->out);
+  cudaFree(m->layout);
+  if (m->layout_read) cudaEventDestroy(m->layout_read);
   delete m;
 }
 
@@ -293,6 +336,54 @@ gbr_status gbr_redwood_noise_simulate_tiles(gbr_redwood_noise* m, const float* s
   if (count == 0) return GBR_OK;
   DeviceScope scope(m->device);
   return launch(m, src, dst, pitch, tw, th, tiles_x, count, static_cast<cudaStream_t>(stream));
+}
+
+gbr_status gbr_redwood_noise_simulate_images(gbr_redwood_noise* m, const float* src, float* dst,
+                                             const int64_t* layout, int32_t count, void* stream) {
+  if (!m || !src || !dst || (count > 0 && !layout)) return fail(GBR_ERROR_INVALID_ARGUMENT, "null argument");
+  if (count < 0) return fail(GBR_ERROR_INVALID_ARGUMENT, "RedwoodNoiseModel: negative image count");
+  if (src == dst) return fail(GBR_ERROR_INVALID_ARGUMENT, "RedwoodNoiseModel: input and output must differ");
+  // Host copy: the layout, then the prefix sum of 256-pixel blocks per image.
+  std::vector<long long> host(size_t(count) * 5 + 1);
+  long long blocks = 0;
+  for (int32_t i = 0; i < count; ++i) {
+    const int64_t off = layout[4 * i], pitch = layout[4 * i + 1], w = layout[4 * i + 2], h = layout[4 * i + 3];
+    if (off < 0 || w <= 0 || h <= 0 || pitch < w || w * h > (int64_t(1) << 31) - 1)
+      return fail(GBR_ERROR_INVALID_ARGUMENT,
+                  "RedwoodNoiseModel: bad layout of image " + std::to_string(i));
+    for (int k = 0; k < 4; ++k) host[4 * size_t(i) + k] = layout[4 * i + k];
+    host[4 * size_t(count) + i] = blocks;
+    blocks += (w * h + 255) / 256;
+  }
+  host[5 * size_t(count)] = blocks;
+  if (blocks > (1LL << 31) - 1)
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "RedwoodNoiseModel: too many pixels in one batch");
+  if (count == 0) return GBR_OK;
+  DeviceScope scope(m->device);
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!m->layout_read)
+    if (cudaError_t e = cudaEventCreateWithFlags(&m->layout_read, cudaEventDisableTiming))
+      return cuda_fail(e, "RedwoodNoiseModel: event");
+  if (host.size() > m->layout_cap) {
+    // The previous layout may still be read by a launch on another stream.
+    if (cudaError_t e = cudaEventSynchronize(m->layout_read)) return cuda_fail(e, "RedwoodNoiseModel: wait");
+    cudaFree(m->layout);
+    m->layout = nullptr;
+    m->layout_cap = 0;
+    if (cudaError_t e = cudaMalloc(&m->layout, host.size() * sizeof(long long)))
+      return cuda_fail(e, "RedwoodNoiseModel: layout allocation");
+    m->layout_cap = host.size();
+  }
+  // Overwrite the device layout only after the last launch that read it.
+  if (cudaError_t e = cudaStreamWaitEvent(s, m->layout_read, 0)) return cuda_fail(e, "RedwoodNoiseModel: wait");
+  if (cudaError_t e = cudaMemcpyAsync(m->layout, host.data(), host.size() * sizeof(long long),
+                                      cudaMemcpyHostToDevice, s))
+    return cuda_fail(e, "RedwoodNoiseModel: layout upload");
+  const TileArgs a = make_args(m, src, dst, 0, 1, 1, 1, count);
+  redwood_images_kernel<<<unsigned(blocks), 256, 0, s>>>(a, m->layout, m->layout + 4 * size_t(count));
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "redwood noise launch");
+  if (cudaError_t e = cudaEventRecord(m->layout_read, s)) return cuda_fail(e, "RedwoodNoiseModel: event");
+  return GBR_OK;
 }
 
 gbr_status gbr_redwood_noise_simulate_device(gbr_redwood_noise* m, const float* depth, int32_t rows,

@@ -339,6 +339,14 @@ class RendererStandalone:
         check(self._lib.gbr_scene_viewport(self._h, scene, out))
         return tuple(int(v) for v in out)
 
+    def sceneViewports(self):
+        """Every scene's (offset, pitch, width, height) as an int64 array
+        [sceneCount, 4]; the layout is fixed at creation, so it is read once."""
+        if getattr(self, "_scene_layout", None) is None:
+            v = np.array([self.sceneViewport(i) for i in range(self.sceneCount())], np.int64)
+            self._scene_layout = v.reshape(-1, 4)
+        return self._scene_layout
+
     # ------------------------------------------------------------- files
     def addFile(self, filename, flags=0, name=None):
         st = self._lib.gbr_add_file(self._h, str(filename).encode(), int(flags),

@@ -85,20 +85,33 @@ class RedwoodNoiseModelGPUImpl:
                                                          int(tile_w), int(tile_h), int(tiles_x),
                                                          int(count), stream))
 
+    def simulate_images(self, src, dst, layout, stream=None):
+        """Images at any places of a plane (device addresses): `layout` holds
+        one (offset, pitch, width, height) per image, in floats."""
+        lay = np.ascontiguousarray(layout, np.int64).reshape(-1, 4)
+        check(self._lib.gbr_redwood_noise_simulate_images(
+            self._h, int(src), int(dst), lay.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            int(lay.shape[0]), stream))
+
     def apply_to_renderer(self, renderer, out=None, stream=None):
-        """Noise every scene of a tile-grid ``RendererStandalone``'s linear-depth
-        plane into `out` (a CUDA float32 tensor of the framebuffer's shape,
-        allocated if None), on `stream` (torch's current stream if None)."""
+        """Noise every scene of a ``RendererStandalone``'s linear-depth plane
+        (tile grid or ragged layout) into `out` (a CUDA float32 tensor of the
+        plane's shape, allocated if None; only the scenes' pixels are
+        written), on `stream` (torch's current stream if None).  Scene i is
+        image i of the batch."""
         import torch
         src = renderer.linearDepthTensor()
         if out is None:
             out = torch.empty_like(src)
         if out.shape != src.shape or out.dtype != torch.float32 or not out.is_contiguous():
             raise ValueError("out must be a contiguous float32 tensor of the plane's shape")
-        (tw, th), (tx, ty) = renderer.tileSize(), renderer.tileCount()
         s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        self.simulate_tiles(src.data_ptr(), out.data_ptr(), src.shape[1], tw, th, tx,
-                            renderer.sceneCount(), s)
+        if src.dim() == 2 and not renderer._config.viewports:
+            (tw, th), (tx, ty) = renderer.tileSize(), renderer.tileCount()
+            self.simulate_tiles(src.data_ptr(), out.data_ptr(), src.shape[1], tw, th, tx,
+                                renderer.sceneCount(), s)
+        else:
+            self.simulate_images(src.data_ptr(), out.data_ptr(), renderer.sceneViewports(), s)
         return out
 
 

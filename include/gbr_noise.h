@@ -50,6 +50,14 @@ gbr_status gbr_redwood_noise_simulate_host(gbr_redwood_noise* m, const float* de
 gbr_status gbr_redwood_noise_simulate_tiles(gbr_redwood_noise* m, const float* src, float* dst,
                                             int64_t pitch, int32_t tile_w, int32_t tile_h,
                                             int32_t tiles_x, int32_t count, void* stream);
+/* Batched form for any plane layout (no reference counterpart): `count`
+ * images, image i at src + layout[4i] with row pitch layout[4i+1] floats,
+ * layout[4i+2] x layout[4i+3] pixels (the renderer's ragged framebuffer:
+ * gbr_scene_viewport of every scene), noised in one launch into the same
+ * places of dst (device).  layout is a host array; image i draws the same
+ * noise as image i of gbr_redwood_noise_simulate_tiles. */
+gbr_status gbr_redwood_noise_simulate_images(gbr_redwood_noise* m, const float* src, float* dst,
+                                             const int64_t* layout, int32_t count, void* stream);
 /* Seed and call counter: every simulate call uses the counter's value and
  * then increments it. */
 gbr_status gbr_redwood_noise_set_state(gbr_redwood_noise* m, uint64_t seed, uint64_t counter);

@@ -99,3 +99,33 @@ def test_renderer_plane_tiles(pkg, noise):
         want = N.redwood_f32(plane[y0:y0 + th, x0:x0 + tw], m._model, 1.0, 77, 0, image=s, table=table)
         assert np.array_equal(got[y0:y0 + th, x0:x0 + tw], want)
     assert m.get_state() == (77, 1)
+
+
+def test_renderer_plane_ragged(pkg, noise):
+    """A ragged (mixed-resolution) framebuffer: every scene noised in one
+    launch from the per-scene layout equals the oracle on that scene, image
+    index = scene, and equals the tile form's noise of the same image."""
+    import torch
+    from habitat_sim_gb300 import procedural
+    wl = procedural.config2(envs=7, scenes=2, tri_range=(2e4, 3e4), texture_size=64)
+    r = procedural.build_renderer(pkg, wl)
+    procedural.set_cameras(r, wl, procedural.camera_poses(wl, 0))
+    r.draw()
+    m = noise.RedwoodNoiseModelGPUImpl(noise.load_model(), 0, 1.0, seed=5)
+    out = m.apply_to_renderer(r)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    table = N.normal_table()
+    for s in range(r.sceneCount()):
+        off, pitch, w, h = r.sceneViewport(s)
+        depth = r.sceneImage(pkg.Plane.LinearDepth, s)
+        want = N.redwood_f32(depth, m._model, 1.0, 5, 0, image=s, table=table)
+        img = np.lib.stride_tricks.as_strided(got.reshape(-1)[off:], shape=(h, w), strides=(4 * pitch, 4))
+        assert np.array_equal(img, want), s
+    assert m.get_state() == (5, 1)
+    # Bad layouts are rejected before any launch.
+    src = r.linearDepthTensor()
+    with pytest.raises(pkg.GbrError, match="bad layout of image 1"):
+        m.simulate_images(src.data_ptr(), out.data_ptr(), [(0, 8, 8, 8), (0, 4, 8, 8)])
+    m.close()
+
