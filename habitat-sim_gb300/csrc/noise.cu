@@ -98,9 +98,10 @@ __device__ __forceinline__ void noise_pixel(const TileArgs& a, int img, int idx,
     // Remap to the model's 640 x 480 sensor (a 1-pixel axis maps to 0).
     const int ux = xmax > 0.0f ? int(__fadd_rn(__fmul_rn(__fdiv_rn(float(x), xmax), 639.0f), 0.5f)) : 0;
     const int uy = ymax > 0.0f ? int(__fadd_rn(__fmul_rn(__fdiv_rn(float(y), ymax), 479.0f), 0.5f)) : 0;
-    const int i2 = int(__fdiv_rn(__fadd_rn(d, 1.0f), 2.0f));
+    // v / 2 and v * 0.5 are the same correctly rounded value.
+    const int i2 = int(__fmul_rn(__fadd_rn(d, 1.0f), 0.5f));
     const int i1 = i2 - 1;
-    const float w = __fdiv_rn(__fsub_rn(d, __fadd_rn(__fmul_rn(float(i1), 2.0f), 1.0f)), 2.0f);
+    const float w = __fmul_rn(__fsub_rn(d, __fadd_rn(__fmul_rn(float(i1), 2.0f), 1.0f)), 0.5f);
     const float* cell = a.model + ((uy / 6) * kModelCols + ux / 8) * kModelDims;
     // Bins clamped to 0..4 (the reference clamps the upper bin only from
     // above: equal for every depth >= 0).
