@@ -470,6 +470,8 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
     mv.box_base = uint32_t(box_pool_.alloc(mv.chunk_count + cluster_count(mv.chunk_count)));
     if (boxes_.size() < box_pool_.end) boxes_.resize(box_pool_.end);
     build_chunk_boxes(m, v.index_offset, v.index_count, mv.box_base);
+    boxes_lo_ = std::min<size_t>(boxes_lo_, mv.box_base);
+    boxes_hi_ = std::max<size_t>(boxes_hi_, mv.box_base + mv.chunk_count + cluster_count(mv.chunk_count));
     mv.live = true;
     views_.push_back(mv);
   }
@@ -869,11 +871,18 @@ gbr_status Renderer::upload_tables() {
   if (!d_meshes_.reserve(std::max<size_t>(1, meshes_.size()) * sizeof(MeshRec), false) ||
       !d_materials_.reserve(materials_.size() * sizeof(MaterialRec), false) ||
       !d_textures_.reserve(textures_.size() * sizeof(TextureRec), false) ||
-      !d_boxes_.reserve(std::max<size_t>(1, boxes_.size()) * sizeof(ChunkBox), false))
+      !d_boxes_.reserve(std::max<size_t>(1, boxes_.size()) * sizeof(ChunkBox), true))
     return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of device memory for tables");
-  if (!boxes_.empty())
-    GBR_CUDA(cudaMemcpy(d_boxes_.ptr, boxes_.data(), boxes_.size() * sizeof(ChunkBox),
-                        cudaMemcpyHostToDevice), "table upload");
+  // Only the boxes written since the last upload (the device copy keeps the
+  // rest, also across growth): a scene loaded into a large resident set
+  // costs its own boxes, not the whole table.
+  if (boxes_hi_ > boxes_lo_) {
+    GBR_CUDA(cudaMemcpy(d_boxes_.as<ChunkBox>() + boxes_lo_, boxes_.data() + boxes_lo_,
+                        (boxes_hi_ - boxes_lo_) * sizeof(ChunkBox), cudaMemcpyHostToDevice),
+             "table upload");
+    boxes_lo_ = SIZE_MAX;
+    boxes_hi_ = 0;
+  }
   if (!meshes_.empty())
     GBR_CUDA(cudaMemcpy(d_meshes_.ptr, meshes_.data(), meshes_.size() * sizeof(MeshRec),
                         cudaMemcpyHostToDevice), "table upload");

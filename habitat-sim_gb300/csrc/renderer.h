@@ -191,6 +191,8 @@ class Renderer {
   std::vector<MaterialRec> materials_;
   std::vector<MeshView> views_;
   std::vector<ChunkBox> boxes_;
+  // Boxes written since the last upload: [boxes_lo_, boxes_hi_) of boxes_.
+  size_t boxes_lo_ = SIZE_MAX, boxes_hi_ = 0;
   std::unordered_map<std::string, std::pair<uint32_t, uint32_t>> names_;
   RangePool vertex_pool_, index_pool_, texel_pool_, box_pool_;
   bool tables_dirty_ = true;

@@ -43,6 +43,26 @@ def test_renderer_scenes_match_oracle(pkg, no_blur):
         assert np.array_equal(r.sceneImage(pkg.Plane.LinearDepth, s), depth[s])
 
 
+def test_ragged_scenes_match_oracle(pkg):
+    """A ragged framebuffer (64/128/256 px scenes, per-scene field of view):
+    every scene darkened in the same launches equals the oracle on it."""
+    from habitat_sim_gb300 import procedural
+    wl = procedural.config2(envs=5, scenes=2, tri_range=(2e4, 3e4), texture_size=64)
+    r = procedural.build_renderer(pkg, wl)
+    projs, views = procedural.camera_poses(wl, 2)
+    r.updateCameras(projs, views)
+    r.draw()
+    n = len(projs)
+    before = [r.sceneImage(pkg.Plane.Color, s) for s in range(n)]
+    depth = [r.sceneImage(pkg.Plane.LinearDepth, s) for s in range(n)]
+    assert len({b.shape for b in before}) > 1          # mixed resolutions
+    r.drawHbao(pkg.HbaoConfiguration())
+    for s in range(n):
+        got = r.sceneImage(pkg.Plane.Color, s)
+        want = H.hbao(before[s], depth[s], projs[s], H.config())
+        assert np.array_equal(got, want), (s, int((got != want).any(-1).sum()))
+
+
 def test_hbao_apply_one_image(pkg):
     import torch
     import scenarios as S
