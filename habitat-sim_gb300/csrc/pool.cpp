@@ -1,0 +1,72 @@
+// Host worker pool (declared in pool.h).
+#include "pool.h"
+
+#include <algorithm>
+
+namespace gbr {
+
+WorkerPool::WorkerPool(unsigned threads) {
+  for (unsigned t = 0; t < threads; ++t) threads_.emplace_back([this] { work(); });
+}
+
+WorkerPool::~WorkerPool() {
+  {
+    std::lock_guard<std::mutex> lk(m_);
+    stop_ = true;
+  }
+  start_.notify_all();
+  for (auto& t : threads_) t.join();
+}
+
+void WorkerPool::drain() {
+  for (;;) {
+    const uint32_t b = next_.fetch_add(chunk_);
+    if (b >= count_) return;
+    (*fn_)(b, std::min(count_, b + chunk_));
+  }
+}
+
+void WorkerPool::work() {
+  uint64_t seen = 0;
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(m_);
+      start_.wait(lk, [&] { return stop_ || generation_ != seen; });
+      if (stop_) return;
+      seen = generation_;
+    }
+    drain();
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      --pending_;
+    }
+    done_.notify_all();
+  }
+}
+
+void WorkerPool::run(uint32_t count, uint32_t chunk, const std::function<void(uint32_t, uint32_t)>& fn) {
+  std::lock_guard<std::mutex> serial(run_m_);
+  {
+    std::lock_guard<std::mutex> lk(m_);
+    fn_ = &fn;
+    count_ = count;
+    chunk_ = std::max(1u, chunk);
+    next_.store(0);
+    pending_ = unsigned(threads_.size());
+    ++generation_;
+  }
+  start_.notify_all();
+  drain();
+  // Every worker takes part in every generation, so none can still be
+  // reading fn_ once they have all reported back.
+  std::unique_lock<std::mutex> lk(m_);
+  done_.wait(lk, [&] { return pending_ == 0; });
+  fn_ = nullptr;
+}
+
+WorkerPool& shared_pool() {
+  static WorkerPool pool(std::min(std::max(1u, std::thread::hardware_concurrency()), 16u) - 1);
+  return pool;
+}
+
+}  // namespace gbr

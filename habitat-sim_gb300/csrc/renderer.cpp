@@ -20,6 +20,7 @@
 #include "hbao.h"
 #include "importer.h"
 #include "mips.h"
+#include "pool.h"
 #include "trace.h"
 
 namespace gbr {
@@ -312,41 +313,61 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
     undo();
     return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of device memory");
   }
-  std::vector<float> pos(nv * 4), col(nv * 4), uv(nv * 2, 0.0f);
-  for (size_t v = 0; v < nv; ++v) {
-    pos[v * 4 + 0] = m.positions[v * 3 + 0];
-    pos[v * 4 + 1] = m.positions[v * 3 + 1];
-    pos[v * 4 + 2] = m.positions[v * 3 + 2];
-    uint32_t oid = m.object_ids ? m.object_ids[v] : 0u;
-    std::memcpy(&pos[v * 4 + 3], &oid, 4);
-    for (int c = 0; c < 4; ++c) col[v * 4 + c] = m.colors ? m.colors[v * 4 + c] : 1.0f;
-    if (m.texcoords) {
-      uv[v * 2] = m.texcoords[v * 2];
-      uv[v * 2 + 1] = m.texcoords[v * 2 + 1];
-    }
-  }
-  GBR_CUDA(cudaMemcpy(d_pos_.as<char>() + vb * 16, pos.data(), nv * 16, cudaMemcpyHostToDevice),
-           "addMesh upload");
-  GBR_CUDA(cudaMemcpy(d_color_.as<char>() + vb * 16, col.data(), nv * 16, cudaMemcpyHostToDevice),
-           "addMesh upload");
-  GBR_CUDA(cudaMemcpy(d_uv_.as<char>() + vb * 8, uv.data(), nv * 8, cudaMemcpyHostToDevice),
-           "addMesh upload");
   const bool normals = max_lights_ > 0 && m.normals;
-  if (normals) {
-    if (!d_normal_.reserve(ve * 16, true)) {
-      undo();
-      return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of device memory");
-    }
-    std::vector<float> nrm(nv * 4, 0.0f);
-    for (size_t v = 0; v < nv; ++v)
-      for (int c = 0; c < 3; ++c) nrm[v * 4 + c] = m.normals[v * 3 + c];
-    GBR_CUDA(cudaMemcpy(d_normal_.as<char>() + vb * 16, nrm.data(), nv * 16, cudaMemcpyHostToDevice),
-             "addMesh upload");
+  if (normals && !d_normal_.reserve(ve * 16, true)) {
+    undo();
+    return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of device memory");
   }
-  if (m.index_count)
-    GBR_CUDA(cudaMemcpy(d_indices_.as<char>() + size_t(ib) * 4, m.indices,
-                        size_t(m.index_count) * 4, cudaMemcpyHostToDevice),
+  // Device layouts written straight into pinned staging (position + object
+  // id, colour, texture coordinate, normal), then copied at full link speed.
+  const size_t o_col = nv * 16, o_uv = o_col + nv * 16, o_nrm = o_uv + nv * 8,
+               o_idx = o_nrm + (normals ? nv * 16 : 0), total = o_idx + size_t(m.index_count) * 4;
+  if (!h_mesh_stage_.reserve(std::max<size_t>(total, 16))) {
+    undo();
+    return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of pinned host memory");
+  }
+  char* stage = static_cast<char*>(h_mesh_stage_.ptr);
+  float* pos = reinterpret_cast<float*>(stage);
+  float* col = reinterpret_cast<float*>(stage + o_col);
+  float* uv = reinterpret_cast<float*>(stage + o_uv);
+  float* nrm = reinterpret_cast<float*>(stage + o_nrm);
+  const std::function<void(uint32_t, uint32_t)> fill = [&](uint32_t v0, uint32_t v1) {
+    for (size_t v = v0; v < v1; ++v) {
+      pos[v * 4 + 0] = m.positions[v * 3 + 0];
+      pos[v * 4 + 1] = m.positions[v * 3 + 1];
+      pos[v * 4 + 2] = m.positions[v * 3 + 2];
+      const uint32_t oid = m.object_ids ? m.object_ids[v] : 0u;
+      std::memcpy(&pos[v * 4 + 3], &oid, 4);
+      for (int c = 0; c < 4; ++c) col[v * 4 + c] = m.colors ? m.colors[v * 4 + c] : 1.0f;
+      uv[v * 2] = m.texcoords ? m.texcoords[v * 2] : 0.0f;
+      uv[v * 2 + 1] = m.texcoords ? m.texcoords[v * 2 + 1] : 0.0f;
+      if (normals) {
+        for (int c = 0; c < 3; ++c) nrm[v * 4 + c] = m.normals[v * 3 + c];
+        nrm[v * 4 + 3] = 0.0f;
+      }
+    }
+  };
+  if (nv >= (1u << 16))
+    shared_pool().run(uint32_t(nv), 8192, fill);
+  else
+    fill(0, uint32_t(nv));
+  if (m.index_count) std::memcpy(stage + o_idx, m.indices, size_t(m.index_count) * 4);
+  // The legacy stream, as cudaMemcpy would: ordered after earlier work on
+  // blocking streams; the staging buffer is free again once it is drained.
+  GBR_CUDA(cudaMemcpyAsync(d_pos_.as<char>() + vb * 16, pos, nv * 16, cudaMemcpyHostToDevice, 0),
+           "addMesh upload");
+  GBR_CUDA(cudaMemcpyAsync(d_color_.as<char>() + vb * 16, col, nv * 16, cudaMemcpyHostToDevice, 0),
+           "addMesh upload");
+  GBR_CUDA(cudaMemcpyAsync(d_uv_.as<char>() + vb * 8, uv, nv * 8, cudaMemcpyHostToDevice, 0),
+           "addMesh upload");
+  if (normals)
+    GBR_CUDA(cudaMemcpyAsync(d_normal_.as<char>() + vb * 16, nrm, nv * 16, cudaMemcpyHostToDevice, 0),
              "addMesh upload");
+  if (m.index_count)
+    GBR_CUDA(cudaMemcpyAsync(d_indices_.as<char>() + size_t(ib) * 4, stage + o_idx, size_t(m.index_count) * 4,
+                             cudaMemcpyHostToDevice, 0),
+             "addMesh upload");
+  GBR_CUDA(cudaStreamSynchronize(0), "addMesh upload");
   MeshRec rec{};
   rec.vertex_base = uint32_t(vb);
   rec.vertex_count = m.vertex_count;
@@ -453,23 +474,10 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
     mv.index_count = v.index_count;
     mv.material = v.material;
     std::memcpy(mv.transform, v.transform, 64);
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (uint32_t k = 0; k < v.index_count; ++k) {
-      const uint32_t vi = host_indices_[size_t(m.index_base) + v.index_offset + k];
-      const float* p = &host_pos_[(size_t(m.vertex_base) + vi) * 3];
-      for (int c = 0; c < 3; ++c) {
-        lo[c] = std::min(lo[c], p[c]);
-        hi[c] = std::max(hi[c], p[c]);
-      }
-    }
-    for (int c = 0; c < 3; ++c) {
-      mv.bbox[c] = lo[c];
-      mv.bbox[3 + c] = hi[c];
-    }
     mv.chunk_count = (v.index_count / 3 + kChunkTris - 1) / kChunkTris;
     mv.box_base = uint32_t(box_pool_.alloc(mv.chunk_count + cluster_count(mv.chunk_count)));
     if (boxes_.size() < box_pool_.end) boxes_.resize(box_pool_.end);
-    build_chunk_boxes(m, v.index_offset, v.index_count, mv.box_base);
+    build_chunk_boxes(m, v.index_offset, v.index_count, mv.box_base, mv.bbox);
     boxes_lo_ = std::min<size_t>(boxes_lo_, mv.box_base);
     boxes_hi_ = std::max<size_t>(boxes_hi_, mv.box_base + mv.chunk_count + cluster_count(mv.chunk_count));
     mv.live = true;
@@ -481,37 +489,65 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
   return GBR_OK;
 }
 
-// Object-space bounding box of every kChunkTris consecutive triangles of a view.
+// Object-space bounding box of every kChunkTris consecutive triangles of a
+// view, of every kClusterChunks consecutive chunks, and of the whole view
+// (every index of the range, also a trailing partial triangle) into bbox
+// {lo xyz, hi xyz}.  Views of many chunks are split over the host pool.
 void Renderer::build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count,
-                                 uint32_t box_base) {
+                                 uint32_t box_base, float bbox[6]) {
   const uint32_t tris = index_count / 3;
-  const uint32_t* idx = &host_indices_[size_t(m.index_base) + index_offset];
-  for (uint32_t t0 = 0; t0 < tris; t0 += kChunkTris) {
+  const uint32_t chunks = (tris + kChunkTris - 1) / kChunkTris;
+  const uint32_t clusters = (chunks + kClusterChunks - 1) / kClusterChunks;
+  const uint32_t* idx = host_indices_.data() + size_t(m.index_base) + index_offset;
+  const float* pos = host_pos_.data() + size_t(m.vertex_base) * 3;
+  auto extend = [](ChunkBox& b, const float* p) {
+    for (int c = 0; c < 3; ++c) {
+      b.lo[c] = std::min(b.lo[c], p[c]);
+      b.hi[c] = std::max(b.hi[c], p[c]);
+    }
+  };
+  auto empty = []() {
     ChunkBox b{};
     for (int k = 0; k < 3; ++k) {
       b.lo[k] = INFINITY;
       b.hi[k] = -INFINITY;
     }
-    const uint32_t t1 = std::min(tris, t0 + kChunkTris);
-    for (uint32_t k = t0 * 3; k < t1 * 3; ++k) {
-      const float* p = &host_pos_[(size_t(m.vertex_base) + idx[k]) * 3];
-      for (int c = 0; c < 3; ++c) {
-        b.lo[c] = std::min(b.lo[c], p[c]);
-        b.hi[c] = std::max(b.hi[c], p[c]);
+    return b;
+  };
+  // One cluster per work unit: its chunk boxes, then their union.
+  const std::function<void(uint32_t, uint32_t)> fn = [&](uint32_t c0, uint32_t c1) {
+    for (uint32_t cl = c0; cl < c1; ++cl) {
+      ChunkBox u = empty();
+      const uint32_t ch1 = std::min(chunks, (cl + 1) * kClusterChunks);
+      for (uint32_t ch = cl * kClusterChunks; ch < ch1; ++ch) {
+        ChunkBox b = empty();
+        const uint32_t k1 = std::min(tris, (ch + 1) * kChunkTris) * 3;
+        for (uint32_t k = ch * kChunkTris * 3; k < k1; ++k) extend(b, pos + size_t(idx[k]) * 3);
+        boxes_[box_base + ch] = b;
+        for (int k = 0; k < 3; ++k) {
+          u.lo[k] = std::min(u.lo[k], b.lo[k]);
+          u.hi[k] = std::max(u.hi[k], b.hi[k]);
+        }
       }
+      boxes_[box_base + chunks + cl] = u;
     }
-    boxes_[box_base + t0 / kChunkTris] = b;
+  };
+  if (tris >= (1u << 16))
+    shared_pool().run(clusters, 4, fn);
+  else
+    fn(0, clusters);
+  ChunkBox all = empty();
+  for (uint32_t cl = 0; cl < clusters; ++cl) {
+    const ChunkBox& u = boxes_[box_base + chunks + cl];
+    for (int k = 0; k < 3; ++k) {
+      all.lo[k] = std::min(all.lo[k], u.lo[k]);
+      all.hi[k] = std::max(all.hi[k], u.hi[k]);
+    }
   }
-  // Cluster boxes: the union of every kClusterChunks consecutive chunk boxes.
-  const uint32_t chunks = (tris + kChunkTris - 1) / kChunkTris;
-  for (uint32_t c0 = 0; c0 < chunks; c0 += kClusterChunks) {
-    ChunkBox b = boxes_[box_base + c0];
-    for (uint32_t c = c0 + 1; c < std::min(chunks, c0 + kClusterChunks); ++c)
-      for (int k = 0; k < 3; ++k) {
-        b.lo[k] = std::min(b.lo[k], boxes_[box_base + c].lo[k]);
-        b.hi[k] = std::max(b.hi[k], boxes_[box_base + c].hi[k]);
-      }
-    boxes_[box_base + chunks + c0 / kClusterChunks] = b;
+  for (uint32_t k = tris * 3; k < index_count; ++k) extend(all, pos + size_t(idx[k]) * 3);
+  for (int c = 0; c < 3; ++c) {
+    bbox[c] = all.lo[c];
+    bbox[3 + c] = all.hi[c];
   }
 }
 

@@ -165,8 +165,8 @@ class Renderer {
   gbr_status upload_step(cudaStream_t stream);
   gbr_status enqueue_step(cudaStream_t stream, uint32_t mode);
   gbr_status ensure_raster_config();
-  void build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count,
-                         uint32_t box_base);
+  void build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count, uint32_t box_base,
+                         float bbox[6]);
   void* plane_ptr(uint32_t plane, size_t* elem) const;
   gbr_status sync_and_check();
   gbr_status quiesce();
@@ -223,6 +223,7 @@ class Renderer {
   // that the host stages draw k + 1 while draw k runs; upload_done_[slot]
   // follows the whole step that last used the slot.
   PinnedBuffer h_stage_[2];
+  PinnedBuffer h_mesh_stage_;  // addMesh uploads
   cudaEvent_t upload_done_[2] = {nullptr, nullptr};
   bool upload_pending_[2] = {false, false};
   int slot_ = 1;  // slot of the last draw (the next draw takes the other)

@@ -734,64 +734,6 @@ gbr_status ReplayRenderer::set_keyframes_json(uint32_t env, const char* json, ui
   return GBR_OK;
 }
 
-WorkerPool::WorkerPool(unsigned threads) {
-  for (unsigned t = 0; t < threads; ++t) threads_.emplace_back([this] { work(); });
-}
-
-WorkerPool::~WorkerPool() {
-  {
-    std::lock_guard<std::mutex> lk(m_);
-    stop_ = true;
-  }
-  start_.notify_all();
-  for (auto& t : threads_) t.join();
-}
-
-void WorkerPool::drain() {
-  for (;;) {
-    const uint32_t b = next_.fetch_add(chunk_);
-    if (b >= count_) return;
-    (*fn_)(b, std::min(count_, b + chunk_));
-  }
-}
-
-void WorkerPool::work() {
-  uint64_t seen = 0;
-  for (;;) {
-    {
-      std::unique_lock<std::mutex> lk(m_);
-      start_.wait(lk, [&] { return stop_ || generation_ != seen; });
-      if (stop_) return;
-      seen = generation_;
-    }
-    drain();
-    {
-      std::lock_guard<std::mutex> lk(m_);
-      --pending_;
-    }
-    done_.notify_all();
-  }
-}
-
-void WorkerPool::run(uint32_t count, uint32_t chunk, const std::function<void(uint32_t, uint32_t)>& fn) {
-  {
-    std::lock_guard<std::mutex> lk(m_);
-    fn_ = &fn;
-    count_ = count;
-    chunk_ = std::max(1u, chunk);
-    next_.store(0);
-    pending_ = unsigned(threads_.size());
-    ++generation_;
-  }
-  start_.notify_all();
-  drain();
-  // Every worker takes part in every generation, so none can still be
-  // reading fn_ once they have all reported back.
-  std::unique_lock<std::mutex> lk(m_);
-  done_.wait(lk, [&] { return pending_ == 0; });
-  fn_ = nullptr;
-}
-
 // setEnvironmentKeyframe (+ setSensorTransformsFromKeyframe) for environments
 // first .. first + count - 1 in one call.  Every document is parsed before any
 // is applied, so a malformed one leaves all environments unchanged; large
@@ -837,8 +779,7 @@ gbr_status ReplayRenderer::set_keyframe_batch(uint32_t first, uint32_t count, co
   // hundred keyframes and more are split over the worker threads.
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
   if (count >= 256 && hw > 1) {
-    if (!pool_) pool_.reset(new WorkerPool(std::min(hw, 16u) - 1));
-    pool_->run(count, 32, parse_range);
+    shared_pool().run(count, 32, parse_range);
   } else {
     parse_range(0, count);
   }

@@ -6,11 +6,6 @@
 // esp::sim::BatchPlayerImplementation (src/esp/sim/BatchPlayerImplementation.cpp).
 #pragma once
 #include <array>
-#include <atomic>
-#include <condition_variable>
-#include <functional>
-#include <mutex>
-#include <thread>
 #include <map>
 #include <memory>
 #include <set>
@@ -20,6 +15,7 @@
 
 #include "../../include/gbr_replay.h"
 #include "json.h"
+#include "pool.h"
 
 namespace gbr {
 
@@ -151,33 +147,6 @@ class Player {
   std::map<int, Record> records_;
 };
 
-// Host worker threads that split an index range [0, count) into chunks
-// taken from a shared counter; the calling thread works too.  Started on
-// first use, stopped with the owner.
-class WorkerPool {
- public:
-  explicit WorkerPool(unsigned threads);
-  ~WorkerPool();
-  WorkerPool(const WorkerPool&) = delete;
-  WorkerPool& operator=(const WorkerPool&) = delete;
-  unsigned size() const { return unsigned(threads_.size()) + 1; }
-  // fn(begin, end) over chunks of `chunk` indices; returns when all are done.
-  void run(uint32_t count, uint32_t chunk, const std::function<void(uint32_t, uint32_t)>& fn);
-
- private:
-  void work();
-  void drain();
-  std::mutex m_;
-  std::condition_variable start_, done_;
-  std::vector<std::thread> threads_;
-  const std::function<void(uint32_t, uint32_t)>* fn_ = nullptr;
-  uint32_t count_ = 0, chunk_ = 1;
-  std::atomic<uint32_t> next_{0};
-  unsigned pending_ = 0;  // workers yet to finish the current generation
-  uint64_t generation_ = 0;
-  bool stop_ = false;
-};
-
 class ReplayRenderer {
  public:
   static ReplayRenderer* create(const gbr_replay_config& cfg, gbr_status& st);
@@ -211,7 +180,6 @@ class ReplayRenderer {
   Renderer* renderer_ = nullptr;
   std::vector<std::unique_ptr<Player>> players_;
   std::vector<std::array<float, 16>> camera_;  // camera-to-world per environment
-  std::unique_ptr<WorkerPool> pool_;           // keyframe parsing of large batches
 };
 
 }  // namespace replay

@@ -8,12 +8,13 @@
 #include <vector>
 
 #include "json.h"
+#include "pool.h"
 #include "replay.h"
 
 using gbr::Json;
 using gbr::JsonParser;
 using gbr::replay::Keyframe;
-using gbr::replay::WorkerPool;
+using gbr::WorkerPool;
 
 static int failures = 0;
 #define CHECK(c)                                                     \
