@@ -21,6 +21,7 @@ loop (src/esp/sim/BatchReplayRenderer.cpp:117-151); this module is that loop
 for a request-driven caller of the same draw path.
 """
 import collections
+import concurrent.futures
 import dataclasses
 import math
 import time
@@ -292,8 +293,10 @@ class RenderServer:
                                   pin_memory=True) for t in self.planes] for _ in range(2)]
         self._proj = {}
         self._step = 0
+        self._copier = concurrent.futures.ThreadPoolExecutor(max_workers=9)
 
     def close(self):
+        self._copier.shutdown()
         self.torch.cuda.synchronize(self.device)
         self.planes = None
         self.r.close()
@@ -398,15 +401,23 @@ class RenderServer:
         batch, buf, ev = handle
         ev.synchronize()
         now = clock() if clock else math.nan
-        color, depth, sem = (t.numpy() for t in buf)
-        for c, reqs in batch.items():
-            o = self.class_offset[c]
+        planes = [t.numpy() for t in buf]
+        # One new array per resolution class and plane, copied out of the
+        # double-buffered pinned staging on worker threads (the copies are
+        # memory-bound); each request keeps views of its class's arrays.
+        jobs = [(c, reqs, k, planes[k][self.class_offset[c]:self.class_offset[c] + len(reqs) * c * c])
+                for c, reqs in batch.items() for k in range(3)]
+        blocks = list(self._copier.map(np.copy, [j[3] for j in jobs]))
+        for (c, reqs, k, _), blk in zip(jobs, blocks):
             for i, req in enumerate(reqs):
-                a, b = o + i * c * c, o + (i + 1) * c * c
-                req.color = color[a:b].reshape(c, c, 4).copy()
-                req.depth = depth[a:b].reshape(c, c).copy()
-                req.semantic = sem[a:b].reshape(c, c).view(np.uint32).copy()
-                req.done = now
+                img = blk[i * c * c:(i + 1) * c * c]
+                if k == 0:
+                    req.color = img.reshape(c, c, 4)
+                elif k == 1:
+                    req.depth = img.reshape(c, c)
+                else:
+                    req.semantic = img.reshape(c, c).view(np.uint32)
+                    req.done = now
         return batch
 
     # -- the request loop
