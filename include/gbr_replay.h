@@ -88,8 +88,11 @@ gbr_status gbr_replay_set_environment_keyframe_unwrapped(gbr_replay* r, uint32_t
  * sensor_prefix) for each (AbstractReplayRenderer.cpp:61-66, 83-92).  All documents
  * are parsed before any is applied: a malformed one returns
  * GBR_ERROR_INVALID_ARGUMENT naming its environment and changes nothing.
- * Large batches are parsed on several host threads.  Same results as the
- * per-environment calls in environment order. */
+ * Errors while applying (a missing asset, a missing sensor transform) stop
+ * at that environment with the per-environment call's status; earlier
+ * environments keep their new keyframes.  Large batches are parsed on
+ * several host threads.  Same results as the per-environment calls in
+ * environment order. */
 gbr_status gbr_replay_set_environment_keyframes(gbr_replay* r, uint32_t first_env, uint32_t count,
                                                 const char* const* json, const uint64_t* length,
                                                 const char* sensor_prefix);
