@@ -1183,7 +1183,7 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
     // survivors to the chunk ring.  Rounds: each warp takes one chunk of the
     // ring and its lanes set up one triangle each; triangles covering more
     // than small_area pixels are queued.  The queue is rasterised by the
-    // whole CTA (flush) once it is half full, before a cull pass and at the
+    // whole CTA (flush) once it is three quarters full, before a cull pass and at the
     // end.  A cull pass runs whenever fewer chunks than warps wait in the
     // chunk ring, after the depth tiles are refreshed from the z-buffer.
     const uint32_t nclusters = p.vis_clusters[wi.scene];
@@ -1207,7 +1207,9 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
       const bool low = wr - rd < uint32_t(T / 32);
       const bool clusters_left = next < nclusters, have_clusters = cwr != crd;
       const bool need_cull = low && (clusters_left || have_clusters);
-      if (nq > 0 && (nq >= uint32_t(T / 2) || need_cull || wr == rd)) {
+      // A round adds at most T entries to fewer than 3T/4: the queue and the
+      // spill area (T each) hold them.
+      if (nq > 0 && (nq >= uint32_t(3 * T / 4) || need_cull || wr == rd)) {
         // ---- flush: every thread takes a contiguous run of the queued
         // triangles' bounding-box pixels.
         uint32_t area = 0;
