@@ -24,6 +24,7 @@ class WorkerPool {
   WorkerPool& operator=(const WorkerPool&) = delete;
   unsigned size() const { return unsigned(threads_.size()) + 1; }
   // fn(begin, end) over chunks of `chunk` indices; returns when all are done.
+  // fn must not throw and must not call run() itself.
   void run(uint32_t count, uint32_t chunk, const std::function<void(uint32_t, uint32_t)>& fn);
 
  private:

@@ -318,56 +318,68 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
     undo();
     return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of device memory");
   }
-  // Device layouts written straight into pinned staging (position + object
-  // id, colour, texture coordinate, normal), then copied at full link speed.
-  const size_t o_col = nv * 16, o_uv = o_col + nv * 16, o_nrm = o_uv + nv * 8,
-               o_idx = o_nrm + (normals ? nv * 16 : 0), total = o_idx + size_t(m.index_count) * 4;
-  if (!h_mesh_stage_.reserve(std::max<size_t>(total, 16))) {
+  // Device layouts (position + object id, colour, texture coordinate,
+  // normal) written straight into pinned staging and copied at full link
+  // speed, in pieces of at most kStageBytes so that a large mesh does not
+  // keep a large pinned buffer.  The copies go on the legacy stream, as
+  // cudaMemcpy's would (ordered after earlier work on blocking streams); the
+  // staging is free again once a piece is drained.
+  constexpr size_t kStageBytes = size_t(32) << 20;
+  const size_t vbytes = normals ? 56 : 40;
+  const size_t piece_v = kStageBytes / vbytes, piece_i = kStageBytes / 4;
+  const size_t need = std::max(std::min(nv, piece_v) * vbytes, std::min<size_t>(m.index_count, piece_i) * 4);
+  if (!h_mesh_stage_.reserve(std::max<size_t>(need, 16))) {
     undo();
     return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of pinned host memory");
   }
   char* stage = static_cast<char*>(h_mesh_stage_.ptr);
-  float* pos = reinterpret_cast<float*>(stage);
-  float* col = reinterpret_cast<float*>(stage + o_col);
-  float* uv = reinterpret_cast<float*>(stage + o_uv);
-  float* nrm = reinterpret_cast<float*>(stage + o_nrm);
-  const std::function<void(uint32_t, uint32_t)> fill = [&](uint32_t v0, uint32_t v1) {
-    for (size_t v = v0; v < v1; ++v) {
-      pos[v * 4 + 0] = m.positions[v * 3 + 0];
-      pos[v * 4 + 1] = m.positions[v * 3 + 1];
-      pos[v * 4 + 2] = m.positions[v * 3 + 2];
-      const uint32_t oid = m.object_ids ? m.object_ids[v] : 0u;
-      std::memcpy(&pos[v * 4 + 3], &oid, 4);
-      for (int c = 0; c < 4; ++c) col[v * 4 + c] = m.colors ? m.colors[v * 4 + c] : 1.0f;
-      uv[v * 2] = m.texcoords ? m.texcoords[v * 2] : 0.0f;
-      uv[v * 2 + 1] = m.texcoords ? m.texcoords[v * 2 + 1] : 0.0f;
-      if (normals) {
-        for (int c = 0; c < 3; ++c) nrm[v * 4 + c] = m.normals[v * 3 + c];
-        nrm[v * 4 + 3] = 0.0f;
+  for (size_t p0 = 0; p0 < nv; p0 += piece_v) {
+    const size_t n = std::min(piece_v, nv - p0);
+    float* pos = reinterpret_cast<float*>(stage);
+    float* col = reinterpret_cast<float*>(stage + n * 16);
+    float* uv = reinterpret_cast<float*>(stage + n * 32);
+    float* nrm = reinterpret_cast<float*>(stage + n * 40);
+    const std::function<void(uint32_t, uint32_t)> fill = [&](uint32_t a, uint32_t b) {
+      for (size_t i = a; i < b; ++i) {
+        const size_t v = p0 + i;
+        pos[i * 4 + 0] = m.positions[v * 3 + 0];
+        pos[i * 4 + 1] = m.positions[v * 3 + 1];
+        pos[i * 4 + 2] = m.positions[v * 3 + 2];
+        const uint32_t oid = m.object_ids ? m.object_ids[v] : 0u;
+        std::memcpy(&pos[i * 4 + 3], &oid, 4);
+        for (int c = 0; c < 4; ++c) col[i * 4 + c] = m.colors ? m.colors[v * 4 + c] : 1.0f;
+        uv[i * 2] = m.texcoords ? m.texcoords[v * 2] : 0.0f;
+        uv[i * 2 + 1] = m.texcoords ? m.texcoords[v * 2 + 1] : 0.0f;
+        if (normals) {
+          for (int c = 0; c < 3; ++c) nrm[i * 4 + c] = m.normals[v * 3 + c];
+          nrm[i * 4 + 3] = 0.0f;
+        }
       }
-    }
-  };
-  if (nv >= (1u << 16))
-    shared_pool().run(uint32_t(nv), 8192, fill);
-  else
-    fill(0, uint32_t(nv));
-  if (m.index_count) std::memcpy(stage + o_idx, m.indices, size_t(m.index_count) * 4);
-  // The legacy stream, as cudaMemcpy would: ordered after earlier work on
-  // blocking streams; the staging buffer is free again once it is drained.
-  GBR_CUDA(cudaMemcpyAsync(d_pos_.as<char>() + vb * 16, pos, nv * 16, cudaMemcpyHostToDevice, 0),
-           "addMesh upload");
-  GBR_CUDA(cudaMemcpyAsync(d_color_.as<char>() + vb * 16, col, nv * 16, cudaMemcpyHostToDevice, 0),
-           "addMesh upload");
-  GBR_CUDA(cudaMemcpyAsync(d_uv_.as<char>() + vb * 8, uv, nv * 8, cudaMemcpyHostToDevice, 0),
-           "addMesh upload");
-  if (normals)
-    GBR_CUDA(cudaMemcpyAsync(d_normal_.as<char>() + vb * 16, nrm, nv * 16, cudaMemcpyHostToDevice, 0),
+    };
+    if (n >= (1u << 16))
+      shared_pool().run(uint32_t(n), 8192, fill);
+    else
+      fill(0, uint32_t(n));
+    const size_t v = vb + p0;
+    GBR_CUDA(cudaMemcpyAsync(d_pos_.as<char>() + v * 16, pos, n * 16, cudaMemcpyHostToDevice, 0),
              "addMesh upload");
-  if (m.index_count)
-    GBR_CUDA(cudaMemcpyAsync(d_indices_.as<char>() + size_t(ib) * 4, stage + o_idx, size_t(m.index_count) * 4,
+    GBR_CUDA(cudaMemcpyAsync(d_color_.as<char>() + v * 16, col, n * 16, cudaMemcpyHostToDevice, 0),
+             "addMesh upload");
+    GBR_CUDA(cudaMemcpyAsync(d_uv_.as<char>() + v * 8, uv, n * 8, cudaMemcpyHostToDevice, 0),
+             "addMesh upload");
+    if (normals)
+      GBR_CUDA(cudaMemcpyAsync(d_normal_.as<char>() + v * 16, nrm, n * 16, cudaMemcpyHostToDevice, 0),
+               "addMesh upload");
+    GBR_CUDA(cudaStreamSynchronize(0), "addMesh upload");
+  }
+  for (size_t i0 = 0; i0 < m.index_count; i0 += piece_i) {
+    const size_t n = std::min<size_t>(piece_i, m.index_count - i0);
+    std::memcpy(stage, m.indices + i0, n * 4);
+    GBR_CUDA(cudaMemcpyAsync(d_indices_.as<char>() + (size_t(ib) + i0) * 4, stage, n * 4,
                              cudaMemcpyHostToDevice, 0),
              "addMesh upload");
-  GBR_CUDA(cudaStreamSynchronize(0), "addMesh upload");
+    GBR_CUDA(cudaStreamSynchronize(0), "addMesh upload");
+  }
   MeshRec rec{};
   rec.vertex_base = uint32_t(vb);
   rec.vertex_count = m.vertex_count;
