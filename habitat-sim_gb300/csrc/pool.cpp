@@ -1,11 +1,13 @@
 // Host worker pool (declared in pool.h).
 #include "pool.h"
 
+#include <unistd.h>
+
 #include <algorithm>
 
 namespace gbr {
 
-WorkerPool::WorkerPool(unsigned threads) {
+WorkerPool::WorkerPool(unsigned threads) : owner_pid_(getpid()) {
   for (unsigned t = 0; t < threads; ++t) threads_.emplace_back([this] { work(); });
 }
 
@@ -45,6 +47,11 @@ void WorkerPool::work() {
 }
 
 void WorkerPool::run(uint32_t count, uint32_t chunk, const std::function<void(uint32_t, uint32_t)>& fn) {
+  if (getpid() != owner_pid_) {
+    // A forked child inherits the pool but not its threads: work alone.
+    for (uint32_t b = 0; b < count; b += std::max(1u, chunk)) fn(b, std::min(count, b + std::max(1u, chunk)));
+    return;
+  }
   std::lock_guard<std::mutex> serial(run_m_);
   {
     std::lock_guard<std::mutex> lk(m_);
@@ -65,8 +72,10 @@ void WorkerPool::run(uint32_t count, uint32_t chunk, const std::function<void(ui
 }
 
 WorkerPool& shared_pool() {
-  static WorkerPool pool(std::min(std::max(1u, std::thread::hardware_concurrency()), 16u) - 1);
-  return pool;
+  // Never destroyed: its threads end with the process, and a forked child
+  // (which has the object but not the threads) never joins them.
+  static WorkerPool* pool = new WorkerPool(std::min(std::max(1u, std::thread::hardware_concurrency()), 16u) - 1);
+  return *pool;
 }
 
 }  // namespace gbr

@@ -40,10 +40,11 @@ class WorkerPool {
   unsigned pending_ = 0;  // workers yet to finish the current generation
   uint64_t generation_ = 0;
   bool stop_ = false;
+  int owner_pid_;  // the process whose threads these are
 };
 
 // The process-wide pool (hardware threads - 1 workers, at most 15), started
-// on first use.
+// on first use and kept for the life of the process.
 WorkerPool& shared_pool();
 
 }  // namespace gbr
