@@ -2,6 +2,9 @@
 // parsing (no GPU): every index of a range is visited exactly once per run,
 // runs back to back reuse the same threads, and keyframes parsed on the pool
 // equal keyframes parsed serially.
+#include <sys/wait.h>
+#include <unistd.h>
+
 #include <atomic>
 #include <cstdio>
 #include <string>
@@ -75,6 +78,30 @@ int main() {
     const auto it = pooled[i].user_transforms.find("sensor_A");
     CHECK(it != pooled[i].user_transforms.end());
     if (it != pooled[i].user_transforms.end()) CHECK(it->second.translation[2] == float(i));
+  }
+  // A forked child has the pool object but not its threads: run() must
+  // still finish, on the calling thread alone.
+  {
+    std::vector<int> seen(5000, 0);
+    const std::function<void(uint32_t, uint32_t)> mark = [&](uint32_t b, uint32_t e) {
+      for (uint32_t i = b; i < e; ++i) ++seen[i];
+    };
+    pool.run(5000, 64, mark);  // the threads exist and have run
+    const pid_t child = fork();
+    if (child == 0) {
+      std::vector<int> again(5000, 0);
+      const std::function<void(uint32_t, uint32_t)> mark2 = [&](uint32_t b, uint32_t e) {
+        for (uint32_t i = b; i < e; ++i) ++again[i];
+      };
+      pool.run(5000, 64, mark2);
+      for (int v : again)
+        if (v != 1) _exit(3);
+      _exit(0);
+    }
+    int status = 0;
+    CHECK(child > 0 && waitpid(child, &status, 0) == child);
+    CHECK(WIFEXITED(status) && WEXITSTATUS(status) == 0);
+    for (int v : seen) CHECK(v == 1);
   }
   if (failures) {
     std::fprintf(stderr, "%d failures\n", failures);
