@@ -62,3 +62,22 @@ def test_reference_arm_other_ranks_exit_without_work():
     p = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--gpus", "2"], cwd=ROOT,
                        env=env, capture_output=True, text=True, timeout=300)
     assert p.returncode == 0 and p.stdout.strip() == ""
+
+
+def test_reference_arm_json_line():
+    """The reference arm on rank 0 (a few envs of config1 through the CPU
+    oracle) prints one JSON line with the contract's keys, its own e2e and a
+    cpu_baseline describing the run."""
+    import json
+    env = dict(os.environ, RANK="0", LOCAL_RANK="0", WORLD_SIZE="1")
+    p = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "1",
+                        "--envs", "8", "--cpu-seconds", "0.5"], cwd=ROOT, env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    line = json.loads(p.stdout.strip().splitlines()[-1])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["value"] > 0 and line["steps"] == 1
+    assert line["cpu_baseline"]["kind"] in ("port", "reference") and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
