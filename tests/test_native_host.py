@@ -19,19 +19,22 @@ def _cuda_include():
     pytest.skip("CUDA headers not found")
 
 
-@pytest.mark.parametrize("name", ["worker_pool_test", "json_test"])
+@pytest.mark.parametrize("name", ["worker_pool_test", "json_test", "c_abi_test"])
 def test_native(name, tmp_path):
-    if shutil.which("g++") is None:
-        pytest.skip("g++ not available")
+    if shutil.which("g++") is None or shutil.which("gcc") is None:
+        pytest.skip("g++/gcc not available")
     graft.load_package()
     from habitat_sim_gb300 import _lib
     lib = _lib._build.build()
     exe = str(tmp_path / name)
     src = os.path.join(ROOT, "tests", "native", name + ".cpp")
-    subprocess.check_call(["g++", "-O1", "-std=c++17", "-pthread", "-I" + CSRC,
-                           "-I" + os.path.join(ROOT, "include"), "-I" + _cuda_include(), src,
-                           "-o", exe, "-L" + os.path.dirname(lib), "-lgbr",
-                           "-Wl,-rpath," + os.path.dirname(lib)])
+    if os.path.exists(src):
+        cmd = ["g++", "-O1", "-std=c++17", "-pthread", "-I" + CSRC, "-I" + _cuda_include()]
+    else:  # the public headers as plain C, without the CUDA headers
+        src = os.path.join(ROOT, "tests", "native", name + ".c")
+        cmd = ["gcc", "-O1", "-std=c99", "-Wall", "-Werror", "-pedantic"]
+    subprocess.check_call(cmd + ["-I" + os.path.join(ROOT, "include"), src, "-o", exe,
+                                 "-L" + os.path.dirname(lib), "-lgbr", "-Wl,-rpath," + os.path.dirname(lib)])
     out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr
     assert "ok" in out.stdout
