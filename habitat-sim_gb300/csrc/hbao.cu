@@ -120,14 +120,35 @@ __device__ __forceinline__ uint32_t modulate(uint32_t c, float ao) {
   return out;
 }
 
+// The grid has one block per 256 pixels of the batch: scene i owns blocks
+// scenes[i].block0 .. scenes[i + 1].block0 - 1.  The block's scene, by a
+// binary search of thread 0.
+__device__ __forceinline__ int scene_of_block(const HbaoScene* scenes, int count) {
+  __shared__ int s_si;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = count;  // scenes[lo].block0 <= blockIdx.x < scenes[hi].block0
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (scenes[mid].block0 <= int(blockIdx.x))
+        lo = mid;
+      else
+        hi = mid;
+    }
+    s_si = lo;
+  }
+  __syncthreads();
+  return s_si;
+}
+
 __global__ void __launch_bounds__(256) hbao_ao_kernel(const HbaoScene* __restrict__ scenes, int count,
                                                       const float* __restrict__ depth, uint32_t* color,
                                                       uint8_t* q1, const HbaoParams p) {
-  for (int si = blockIdx.y; si < count; si += gridDim.y) {
-    const HbaoScene s = scenes[si];
+  {
+    const HbaoScene s = scenes[scene_of_block(scenes, count)];
     const int pixels = s.w * s.h;
     const float inv_w = __fdiv_rn(1.0f, float(s.w)), inv_h = __fdiv_rn(1.0f, float(s.h));
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < pixels; idx += gridDim.x * blockDim.x) {
+    const int idx = (int(blockIdx.x) - s.block0) * 256 + int(threadIdx.x);
+    if (idx < pixels) {
       const int x = idx % s.w, y = idx / s.w;
       const float u = __fdiv_rn(__fadd_rn(float(x), 0.5f), float(s.w));
       const float v = __fdiv_rn(__fadd_rn(float(y), 0.5f), float(s.h));
@@ -182,10 +203,11 @@ __global__ void __launch_bounds__(256) hbao_blur_kernel(const HbaoScene* __restr
                                                         const uint8_t* __restrict__ src, uint8_t* dst,
                                                         uint32_t* color, const HbaoParams p) {
   const float falloff = 1.0f / (2.0f * 1.5f * 1.5f);
-  for (int si = blockIdx.y; si < count; si += gridDim.y) {
-    const HbaoScene s = scenes[si];
+  {
+    const HbaoScene s = scenes[scene_of_block(scenes, count)];
     const int pixels = s.w * s.h;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < pixels; idx += gridDim.x * blockDim.x) {
+    const int idx = (int(blockIdx.x) - s.block0) * 256 + int(threadIdx.x);
+    if (idx < pixels) {
       const int x = idx % s.w, y = idx / s.w;
       const long long at = s.offset + (long long)y * s.pitch + x;
       const float cd = depth_at(s, depth, x, y);
@@ -269,10 +291,10 @@ HbaoScene hbao_scene(const float* m, int w, int h, long long offset, long long p
   return s;
 }
 
-cudaError_t hbao_launch(const HbaoScene* d_scenes, int count, int max_pixels, const float* depth,
+cudaError_t hbao_launch(const HbaoScene* d_scenes, int count, int blocks, const float* depth,
                         uint32_t* color, uint8_t* q1, uint8_t* q2, const HbaoParams& p, cudaStream_t stream) {
-  if (count <= 0 || max_pixels <= 0) return cudaSuccess;
-  const dim3 grid(std::min((max_pixels + 255) / 256, 4096), std::min(count, 65535));
+  if (count <= 0 || blocks <= 0) return cudaSuccess;
+  const dim3 grid(blocks);
   hbao_ao_kernel<<<grid, 256, 0, stream>>>(d_scenes, count, depth, color, q1, p);
   if (!p.no_blur) {
     hbao_blur_kernel<0><<<grid, 256, 0, stream>>>(d_scenes, count, depth, q1, q2, color, p);
@@ -338,7 +360,7 @@ gbr_status gbr_hbao_apply(const gbr_hbao_config* config, const float projection[
   cudaError_t e = cudaMalloc(&d_scene, sizeof s);
   if (!e) e = cudaMalloc(&q, 2 * plane);
   if (!e) e = cudaMemcpyAsync(d_scene, &s, sizeof s, cudaMemcpyHostToDevice, st);
-  if (!e) e = gbr::hbao_launch(d_scene, 1, w * h, depth, color, q, q + plane, p, st);
+  if (!e) e = gbr::hbao_launch(d_scene, 1, (w * h + 255) / 256, depth, color, q, q + plane, p, st);
   if (!e) e = cudaStreamSynchronize(st);
   cudaFree(d_scene);
   cudaFree(q);

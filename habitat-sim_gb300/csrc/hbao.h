@@ -19,7 +19,7 @@ struct HbaoScene {
   float radius_to_screen;
   float far_plane;   // depth given to background pixels (linear depth 0)
   int ortho;
-  int pad;
+  int block0;        // first block of the scene in the launch grid (256 pixels per block)
 };
 
 struct HbaoParams {
@@ -37,7 +37,7 @@ HbaoScene hbao_scene(const float* projection, int w, int h, long long offset, lo
 // Three launches on `stream`: AO (into q1, or straight into colour without
 // blur), blur along x (q1 -> q2), blur along y and the colour multiply.
 // q1 / q2 are 8-bit planes with the colour plane's layout.
-cudaError_t hbao_launch(const HbaoScene* d_scenes, int count, int max_pixels, const float* depth,
+cudaError_t hbao_launch(const HbaoScene* d_scenes, int count, int blocks, const float* depth,
                         uint32_t* color, uint8_t* q1, uint8_t* q2, const HbaoParams& p,
                         cudaStream_t stream);
 

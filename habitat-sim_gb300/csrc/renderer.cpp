@@ -1468,12 +1468,14 @@ gbr_status Renderer::hbao(const gbr_hbao_config& c, cudaStream_t stream) {
   std::string err;
   if (!hbao_params(c, params, err)) return fail(GBR_ERROR_INVALID_ARGUMENT, err);
   std::vector<HbaoScene> recs;
-  int max_pixels = 0;
+  long long blocks = 0;  // one per 256 pixels of each scene
   for (const SceneState& sc : scenes_) {
     if (!sc.enabled || sc.width <= 0 || sc.height <= 0) continue;
     recs.push_back(hbao_scene(sc.proj, sc.width, sc.height, sc.fb_offset, sc.pitch, c.radius));
-    max_pixels = std::max(max_pixels, sc.width * sc.height);
+    recs.back().block0 = int(blocks);
+    blocks += (static_cast<long long>(sc.width) * sc.height + 255) / 256;
   }
+  if (blocks > 0x7fffffffLL) return fail(GBR_ERROR_INVALID_ARGUMENT, "Hbao: too many pixels in one call");
   if (recs.empty()) return GBR_OK;
   cudaSetDevice(device_);
   const size_t fb = size_t(fb_w_) * size_t(fb_h_);
@@ -1488,7 +1490,7 @@ gbr_status Renderer::hbao(const gbr_hbao_config& c, cudaStream_t stream) {
   uint32_t* color = static_cast<uint32_t*>(plane_ptr(GBR_PLANE_COLOR, &elem));
   const float* depth = static_cast<const float*>(plane_ptr(GBR_PLANE_LINEAR_DEPTH, &elem));
   uint8_t* q = static_cast<uint8_t*>(d_hbao_ao_.ptr);
-  GBR_CUDA(hbao_launch(d_hbao_scenes_.as<HbaoScene>(), int(recs.size()), max_pixels, depth, color, q, q + fb,
+  GBR_CUDA(hbao_launch(d_hbao_scenes_.as<HbaoScene>(), int(recs.size()), int(blocks), depth, color, q, q + fb,
                        params, stream),
            "Hbao launch");
   // Readbacks of this draw now follow the effect.
