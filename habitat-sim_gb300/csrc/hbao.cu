@@ -360,7 +360,7 @@ gbr_status gbr_hbao_apply(const gbr_hbao_config* config, const float projection[
   cudaError_t e = cudaMalloc(&d_scene, sizeof s);
   if (!e) e = cudaMalloc(&q, 2 * plane);
   if (!e) e = cudaMemcpyAsync(d_scene, &s, sizeof s, cudaMemcpyHostToDevice, st);
-  if (!e) e = gbr::hbao_launch(d_scene, 1, (w * h + 255) / 256, depth, color, q, q + plane, p, st);
+  if (!e) e = gbr::hbao_launch(d_scene, 1, int((int64_t(w) * h + 255) / 256), depth, color, q, q + plane, p, st);
   if (!e) e = cudaStreamSynchronize(st);
   cudaFree(d_scene);
   cudaFree(q);

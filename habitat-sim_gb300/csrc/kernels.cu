@@ -1624,6 +1624,7 @@ constexpr int kNoAllocRegion = 128;    // region side of one work item
 constexpr int kNoAllocMaxItems =
     (kNoAllocMaxSide / kNoAllocRegion) * (kNoAllocMaxSide / kNoAllocRegion);
 constexpr size_t kNoAllocScratchBytes = 16384;
+constexpr uint32_t kNoAllocMaxTriangles = 0xFFFFFFFFu / 3;
 constexpr int kNoAllocMaxDevices = 64;
 
 struct NoAllocScratch {
@@ -1749,8 +1750,12 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
     return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT,
                          "viewport " + std::to_string(width) + "x" + std::to_string(height) +
                              " is outside 1..4096 x 1..4096, the limit of its fixed scratch");
-  if (triangle_count >= (1u << 31))
-    return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT, "2^31 or more triangles");
+  // The raster kernel addresses index 3 * t + k of the mesh in 32 bits.
+  if (triangle_count > kNoAllocMaxTriangles)
+    return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT,
+                         std::to_string(triangle_count) + " triangles: more than " +
+                             std::to_string(kNoAllocMaxTriangles) +
+                             " (3 x triangles indices must be addressable in 32 bits)");
   if (triangle_count && (!positions || !indices || vertex_count == 0))
     return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT, "positions, indices and vertices are required");
   if ((reinterpret_cast<uintptr_t>(positions) | reinterpret_cast<uintptr_t>(colors)) & 15u)
@@ -1764,23 +1769,36 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
   if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
     return no_alloc_fail(GBR_ERROR_CUDA, "no usable current device");
   void* scratch = nullptr;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
   {
-    // First call on this device: look up the device address of the fixed
-    // scratch (a host-side name of a __device__ array is not a device address).
+    // The device address of the fixed scratch (the host-side name of a
+    // __device__ array is not a device address).  It belongs to the current
+    // context, which a device reset or a caller's own driver-API context
+    // replaces, so it is looked up again on every call made outside a stream
+    // capture; inside a capture the address of the last call on this device
+    // is used, so some call on the device must come before the first capture.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &capture) != cudaSuccess) {
+      cudaGetLastError();
+      capture = cudaStreamCaptureStatusActive;  // unknown: do not call into the runtime's symbol table
+    }
     std::lock_guard<std::mutex> lock(g_no_alloc_mutex);
-    if (!g_no_alloc_ptr[dev]) {
-      e = cudaGetSymbolAddress(&g_no_alloc_ptr[dev], g_no_alloc_scratch);
+    if (capture == cudaStreamCaptureStatusNone) {
+      void* ptr = nullptr;
+      e = cudaGetSymbolAddress(&ptr, g_no_alloc_scratch);
       if (e != cudaSuccess) {
-        g_no_alloc_ptr[dev] = nullptr;
         cudaGetLastError();
         return no_alloc_fail(GBR_ERROR_CUDA, std::string("cudaGetSymbolAddress: ") +
                                                  cudaGetErrorString(e));
       }
+      g_no_alloc_ptr[dev] = ptr;
+    } else if (!g_no_alloc_ptr[dev]) {
+      return no_alloc_fail(GBR_ERROR_INVALID_ARGUMENT,
+                           "the first call on a device must come before any stream capture");
     }
     scratch = g_no_alloc_ptr[dev];
   }
   NoAllocScratch* s = static_cast<NoAllocScratch*>(scratch);
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int cols = (width + kNoAllocRegion - 1) / kNoAllocRegion;
   const int rows = (height + kNoAllocRegion - 1) / kNoAllocRegion;
   NoAllocSetup a{};

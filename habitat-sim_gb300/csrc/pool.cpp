@@ -21,10 +21,12 @@ WorkerPool::~WorkerPool() {
 }
 
 void WorkerPool::drain() {
+  // A 64-bit counter: it cannot wrap below count_ however many threads
+  // overshoot the end, so no chunk runs twice.
   for (;;) {
-    const uint32_t b = next_.fetch_add(chunk_);
+    const uint64_t b = next_.fetch_add(chunk_);
     if (b >= count_) return;
-    (*fn_)(b, std::min(count_, b + chunk_));
+    (*fn_)(uint32_t(b), uint32_t(std::min<uint64_t>(count_, b + chunk_)));
   }
 }
 
@@ -49,7 +51,8 @@ void WorkerPool::work() {
 void WorkerPool::run(uint32_t count, uint32_t chunk, const std::function<void(uint32_t, uint32_t)>& fn) {
   if (getpid() != owner_pid_) {
     // A forked child inherits the pool but not its threads: work alone.
-    for (uint32_t b = 0; b < count; b += std::max(1u, chunk)) fn(b, std::min(count, b + std::max(1u, chunk)));
+    const uint64_t step = std::max(1u, chunk);
+    for (uint64_t b = 0; b < count; b += step) fn(uint32_t(b), uint32_t(std::min<uint64_t>(count, b + step)));
     return;
   }
   std::lock_guard<std::mutex> serial(run_m_);

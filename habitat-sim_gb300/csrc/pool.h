@@ -36,7 +36,7 @@ class WorkerPool {
   std::vector<std::thread> threads_;
   const std::function<void(uint32_t, uint32_t)>* fn_ = nullptr;
   uint32_t count_ = 0, chunk_ = 1;
-  std::atomic<uint32_t> next_{0};
+  std::atomic<uint64_t> next_{0};
   unsigned pending_ = 0;  // workers yet to finish the current generation
   uint64_t generation_ = 0;
   bool stop_ = false;

@@ -346,7 +346,10 @@ gbr_status gbr_last_draw_stats(gbr_renderer* r, gbr_draw_stats* out);
  *  positions   device, float4 per vertex (x, y, z, object-id bits), 16-B aligned
  *  colors      device, float4 RGBA per vertex, 16-B aligned, or NULL
  *  indices     device, 3 uint32 per triangle (an index >= vertex_count makes
- *              the call render only background)
+ *              the call render only background; the call still returns
+ *              GBR_OK, since it does not wait for the GPU)
+ *  triangle_count  at most 1431655765 (3 x triangle_count indices are
+ *              addressed in 32 bits); more is rejected
  *  projection, view   host, column-major 4x4 (as gbr_update_camera)
  *  semantic_id id of every pixel the mesh covers, unless use_vertex_ids,
  *              then the last vertex's id from positions[].w
@@ -358,9 +361,11 @@ gbr_status gbr_last_draw_stats(gbr_renderer* r, gbr_draw_stats* out);
  * (held by every GPU that loads it until the process exits); each call
  * rewrites what must start fresh.  All calls share that array, so calls that
  * may overlap on the GPU (different streams without ordering) race: order
- * them on one stream.  The first call on each device looks up the array's
- * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture.  Asynchronous on `stream`. */
+ * them on one stream.  Each call made outside a stream capture looks up the
+ * array's device address in the current context (cudaGetSymbolAddress); a
+ * call inside a capture reuses the address of the last call on that device,
+ * so make a first call before any capture, and again after a device reset.
+ * Asynchronous on `stream`. */
 gbr_status gbr_render_mesh_no_alloc(const void* positions, const void* colors,
                                     const uint32_t* indices, uint32_t vertex_count,
                                     uint32_t triangle_count, const float projection[16],

@@ -1,6 +1,6 @@
 """Copy the Redwood depth distortion model from a habitat-sim checkout.
 
-    python habitat-sim_gb300/data/copy_redwood_model.py /path/to/habitat-sim
+    python tests/golden/copy_redwood_model.py /path/to/habitat-sim
 
 The model (80 x 400 float32: an 80 x 80 grid over a 640 x 480 sensor, 5
 depth bins per cell) is the published Redwood / CLAMS PrimeSense distortion
@@ -14,12 +14,13 @@ import shutil
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+DATA = os.path.join(os.path.dirname(os.path.dirname(HERE)), "habitat-sim_gb300", "data")
 NAME = "redwood-depth-dist-model.npy"
 
 
 def main(root):
     src = os.path.join(root, "src_python", "habitat_sim", "sensors", "noise_models", "data", NAME)
-    dst = os.path.join(HERE, NAME)
+    dst = os.path.join(DATA, NAME)
     shutil.copyfile(src, dst)
     digest = hashlib.sha256(open(dst, "rb").read()).hexdigest()
     with open(dst + ".sha256", "w") as f:
@@ -28,4 +29,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: copy_redwood_model.py /path/to/habitat-sim")
+    main(sys.argv[1])

@@ -17,8 +17,6 @@ import pytest
 
 import __graft_entry__ as graft
 
-pytestmark = pytest.mark.gpu
-
 W, H = 200, 150   # two 128-pixel regions in each direction, ragged edges
 
 
@@ -50,6 +48,7 @@ def _view(x, y, z, yaw):
     return np.linalg.inv(cam).T.astype(np.float32)   # [col][row]
 
 
+@pytest.mark.gpu
 def test_no_alloc_matches_draw():
     import torch
     if not torch.cuda.is_available():
@@ -111,16 +110,65 @@ def test_no_alloc_matches_draw():
         assert (sid > 0).any()
 
 
-def test_no_alloc_rejects_oversized_viewport():
-    import torch
-    if not torch.cuda.is_available():
-        pytest.skip("no CUDA device")
+def _lib():
     graft.load_package()
-    from habitat_sim_gb300 import _lib
-    lib = _lib.load()
+    from habitat_sim_gb300 import _lib as lib_mod
+    return lib_mod, lib_mod.load()
+
+
+def test_no_alloc_rejects_sizes_beyond_its_limits():
+    """Argument checks come before any CUDA call, so they run without a GPU:
+    viewports beyond the 4096 x 4096 the fixed scratch can tile, and more
+    triangles than 32-bit index addressing reaches (3 x count < 2^32)."""
+    lib_mod, lib = _lib()
     eye = np.eye(4, dtype=np.float32)
-    st = lib.gbr_render_mesh_no_alloc(None, None, None, 0, 0, eye.ctypes.data_as(_lib.c_float_p),
-                                      eye.ctypes.data_as(_lib.c_float_p), 0, 0, 4097, 16,
+    m = eye.ctypes.data_as(lib_mod.c_float_p)
+    st = lib.gbr_render_mesh_no_alloc(None, None, None, 0, 0, m, m, 0, 0, 4097, 16,
                                       None, None, None, None, None)
     assert st == 1
     assert b"4096" in lib.gbr_last_error()
+    fake = 1 << 20   # never dereferenced: the count is rejected first
+    st = lib.gbr_render_mesh_no_alloc(fake, None, fake, 3, 0x55555556, m, m, 0, 0, 16, 16,
+                                      None, None, None, None, None)
+    assert st == 1
+    assert b"1431655765" in lib.gbr_last_error()
+
+
+@pytest.mark.gpu
+def test_no_alloc_bad_index_renders_background_then_recovers():
+    """An index beyond the vertex count makes the call draw nothing (every
+    pixel background) while still returning GBR_OK: the check runs on the
+    GPU and the call does not wait for it.  The next call with good indices
+    renders the mesh again (the flag in the shared scratch is cleared on
+    every call)."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    lib_mod, lib = _lib()
+    from habitat_sim_gb300 import procedural
+    pos, col, ids, idx = _mesh(procedural)
+    pos4 = np.zeros((len(pos), 4), np.float32)
+    pos4[:, :3] = pos
+    pos4[:, 3] = ids.view(np.float32)
+    d_pos = torch.from_numpy(pos4).cuda()
+    bad = idx.copy()
+    bad[7] = len(pos) + 5
+    d_bad = torch.from_numpy(bad.view(np.int32)).cuda()
+    d_idx = torch.from_numpy(idx.view(np.int32)).cuda()
+    proj = np.ascontiguousarray(procedural.projection(80.0, W, H), np.float32)
+    view = np.ascontiguousarray(_view(0.3, 1.25, 2.5, 0.4), np.float32)
+    col_plane = torch.empty((H, W), dtype=torch.int32, device="cuda")
+    lin_plane = torch.empty((H, W), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    out = []
+    for d in (d_bad, d_idx):
+        st = lib.gbr_render_mesh_no_alloc(
+            d_pos.data_ptr(), None, d.data_ptr(), len(pos), len(idx) // 3,
+            proj.ctypes.data_as(lib_mod.c_float_p), view.ctypes.data_as(lib_mod.c_float_p), 0, 1,
+            W, H, col_plane.data_ptr(), None, lin_plane.data_ptr(), None, stream)
+        assert st == 0, lib.gbr_last_error()
+        torch.cuda.synchronize()
+        out.append((col_plane.cpu().numpy().view(np.uint32).copy(), lin_plane.cpu().numpy().copy()))
+    (c_bad, l_bad), (c_ok, l_ok) = out
+    assert (c_bad == 0xFF1F1F1F).all() and (l_bad == 0).all()
+    assert (c_ok != 0xFF1F1F1F).all() and (l_ok > 0).all()   # the camera is inside the room
