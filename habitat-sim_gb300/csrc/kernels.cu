@@ -441,6 +441,7 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int threads, int regi
 struct Setup {
   int32_t X[3], Y[3];
   float zw0, d1, d2, inva;
+  float zmin;  // nearest window depth of the three vertices
   uint32_t bias;
   int x0, y0, x1, y1;
 };
@@ -456,6 +457,12 @@ struct Ctx {
   int small_area;
   float hw, hh;          // half the viewport size
   float gx, gy;          // guard band in NDC: 32768 / W, 32768 / H
+  // Deepest depth of each 8x8 depth tile and 32x32 coarse tile of the region
+  // (null when occlusion culling is off).  Refreshed from the z-buffer from
+  // time to time; depths only decrease, so a stale value is conservative.
+  const uint32_t* tiles;
+  const uint32_t* coarse;
+  int tcols, ccols;
 };
 
 __device__ __forceinline__ void set_viewport(Ctx& c, int W, int H) {
@@ -501,6 +508,7 @@ __device__ __forceinline__ bool setup_sub(const float4* q, const Ctx& c, Setup& 
   st.y1 = min((maxY - 128) >> 8, c.ry0 + c.rh - 1);
   if (st.x0 > st.x1 || st.y0 > st.y1) return false;
   st.inva = __frcp_rn(__ll2float_rn(area));
+  st.zmin = fminf(zw[0], fminf(zw[1], zw[2]));
   st.zw0 = zw[0];
   st.d1 = __fsub_rn(zw[1], zw[0]);
   st.d2 = __fsub_rn(zw[2], zw[0]);
@@ -560,11 +568,44 @@ __device__ __forceinline__ void store_entry(QEntry& e, const Setup& st, uint32_t
   e.y1 = int16_t(st.y1);
 }
 
+// Triangle-level occlusion test: true when every fragment the (sub)triangle
+// could produce loses the depth test against the z-buffer.  A fragment's
+// depth is interpolated from the vertices' window depths with barycentrics
+// in [0, 1], so it is at least their minimum less a few units of rounding;
+// with a margin far above that rounding, if that bound is deeper than the
+// deepest depth of every tile the bounding box touches, no fragment passes
+// (the z-buffer's depths only decrease).  The tile values may be stale,
+// which only makes the test keep more.
+__device__ __forceinline__ bool hidden(const Setup& st, const Ctx& c) {
+  const float zm = __fsub_rn(st.zmin, 4e-6f);
+  if (!c.tiles || !(zm > 0.0f)) return false;
+  const uint32_t zbits = __float_as_uint(zm);
+  int tx0 = (st.x0 - c.rx0) / kTile, tx1 = (st.x1 - c.rx0) / kTile;
+  int ty0 = (st.y0 - c.ry0) / kTile, ty1 = (st.y1 - c.ry0) / kTile;
+  const uint32_t* t = c.tiles;
+  int cols = c.tcols;
+  if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > 16) {  // large footprint: coarse tiles
+    tx0 /= kCoarse;
+    tx1 /= kCoarse;
+    ty0 /= kCoarse;
+    ty1 /= kCoarse;
+    t = c.coarse;
+    cols = c.ccols;
+  }
+  for (int ty = ty0; ty <= ty1; ++ty)
+    for (int tx = tx0; tx <= tx1; ++tx)
+      if (t[ty * cols + tx] >= zbits) return false;
+  return true;
+}
+
 __device__ __forceinline__ void emit(const float4* q, uint32_t ordinal, const Ctx& c) {
   Setup st;
   if (!setup_sub(q, c, st)) return;
   const int area = (st.x1 - st.x0 + 1) * (st.y1 - st.y0 + 1);
   if (area > c.small_area) {
+    // Only triangles bound for the shared queue are tested: their pixels
+    // cost the whole CTA; a small one is cheaper to rasterise than to test.
+    if (hidden(st, c)) return;
     const uint32_t slot = atomicAdd(c.qcount, 1u);
     if (slot < uint32_t(c.qcap)) {
       store_entry(c.queue[slot], st, ordinal);
@@ -599,8 +640,8 @@ __device__ __forceinline__ float4 lerp_clip(const float4& in, const float4& out,
 // call would place the caller's vertices in local memory for every triangle,
 // not only for the few that are clipped.  (The context stays a reference: it
 // is stored once per work item, and copying it for the call costs registers.)
-__device__ __noinline__ void clip_and_emit(float4 v0, float4 v1, float4 v2, uint32_t ordinal,
-                                           const Ctx& c) {
+__device__ __noinline__ void clip_general(float4 v0, float4 v1, float4 v2, uint32_t ordinal,
+                                          const Ctx& c) {
   const float gx = c.gx, gy = c.gy;
   float4 poly[9], next[9];
   int n = 3;
@@ -622,6 +663,50 @@ __device__ __noinline__ void clip_and_emit(float4 v0, float4 v1, float4 v2, uint
   }
   for (int i = 1; i + 1 < n; ++i) {
     const float4 sub[3] = {poly[0], poly[i], poly[i + 1]};
+    emit(sub, ordinal, c);
+  }
+}
+
+__device__ __forceinline__ bool inside_guard(const float4& v, float gx, float gy) {
+  return plane_dist(v, 1, gx, gy) >= 0.0f && plane_dist(v, 2, gx, gy) >= 0.0f &&
+         plane_dist(v, 3, gx, gy) >= 0.0f && plane_dist(v, 4, gx, gy) >= 0.0f;
+}
+
+// Clipping of a triangle that needs it.  The common case -- the near plane
+// cuts it and its clipped polygon lies inside the guard band -- is done in
+// registers: the polygon is the one Sutherland-Hodgman makes for the near
+// plane (same vertices, same order, same intersection arithmetic), which the
+// guard-band planes then leave unchanged, so the fan triangles are those of
+// the general path.  Any other case runs the general path.
+__device__ __noinline__ void clip_and_emit(float4 v0, float4 v1, float4 v2, uint32_t ordinal,
+                                           const Ctx& c) {
+  const float gx = c.gx, gy = c.gy;
+  const float d0 = plane_dist(v0, 0, gx, gy), d1 = plane_dist(v1, 0, gx, gy),
+              d2 = plane_dist(v2, 0, gx, gy);
+  const uint32_t out = (d0 >= 0.0f ? 0u : 1u) | (d1 >= 0.0f ? 0u : 2u) | (d2 >= 0.0f ? 0u : 4u);
+  float4 q0, q1, q2, q3;
+  int n = 4;
+  switch (out) {
+    case 0: q0 = v0; q1 = v1; q2 = v2; n = 3; break;
+    case 1: q0 = lerp_clip(v1, v0, d1, d0); q1 = v1; q2 = v2; q3 = lerp_clip(v2, v0, d2, d0); break;
+    case 2: q0 = v0; q1 = lerp_clip(v0, v1, d0, d1); q2 = lerp_clip(v2, v1, d2, d1); q3 = v2; break;
+    case 4: q0 = v0; q1 = v1; q2 = lerp_clip(v1, v2, d1, d2); q3 = lerp_clip(v0, v2, d0, d2); break;
+    case 3: q0 = lerp_clip(v2, v1, d2, d1); q1 = v2; q2 = lerp_clip(v2, v0, d2, d0); n = 3; break;
+    case 6: q0 = v0; q1 = lerp_clip(v0, v1, d0, d1); q2 = lerp_clip(v0, v2, d0, d2); n = 3; break;
+    case 5: q0 = lerp_clip(v1, v0, d1, d0); q1 = v1; q2 = lerp_clip(v1, v2, d1, d2); n = 3; break;
+    default: return;  // all three behind the near plane
+  }
+  if (!inside_guard(q0, gx, gy) || !inside_guard(q1, gx, gy) || !inside_guard(q2, gx, gy) ||
+      (n == 4 && !inside_guard(q3, gx, gy))) {
+    clip_general(v0, v1, v2, ordinal, c);
+    return;
+  }
+  {
+    const float4 sub[3] = {q0, q1, q2};
+    emit(sub, ordinal, c);
+  }
+  if (n == 4) {
+    const float4 sub[3] = {q0, q2, q3};
     emit(sub, ordinal, c);
   }
 }
@@ -1078,8 +1163,12 @@ __device__ __forceinline__ bool chunk_keep(const float* mvp, const ChunkBox& b, 
     out |= (cz - cw > az) ? 16u : 0u;
     out |= (-cz - cw > az) ? 32u : 0u;
     all_out &= out;
-    if (cw > 1e-6f) {
-      const float iw = 1.0f / cw;
+    if (cw > 1e-6f && cw < 1e30f) {
+      // An approximate reciprocal (relative error ~2^-22; w is bounded so it
+      // cannot underflow): the decisions below compare against margins of
+      // 1-2 pixels and 4e-6 in depth, far above the error it adds at values
+      // near those thresholds.
+      const float iw = __fdividef(1.0f, cw);
       const float sx = (cx * iw * 0.5f + 0.5f) * float(c.W);
       const float sy = (cy * iw * 0.5f + 0.5f) * float(c.H);
       x0 = fminf(x0, sx);
@@ -1193,6 +1282,10 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tcols = (c.rw + kTile - 1) / kTile, trows = (c.rh + kTile - 1) / kTile;
     const int ccols = (tcols + kCoarse - 1) / kCoarse, crows = (trows + kCoarse - 1) / kCoarse;
+    c.tiles = occlusion ? tiles : nullptr;  // filled by the first cull pass, before any round
+    c.coarse = coarse;
+    c.tcols = tcols;
+    c.ccols = ccols;
     if (threadIdx.x == 0) {
       s_rd = s_wr = s_crd = s_cwr = s_next = 0;
     }
@@ -1270,24 +1363,29 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
       if (need_cull) {
         if (occlusion && tiles_stale) {
           // Deepest depth (as ordered bits; empty pixels are all ones) of
-          // each tile; pixels outside the region count as 0.
-          for (int t = warp; t < tcols * trows; t += T / 32) {
-            const int tx = (t % tcols) * kTile + (lane & 7), ty = (t / tcols) * kTile + (lane >> 3);
-            uint32_t m = 0;
-            if (tx < c.rw) {
-              if (ty < c.rh) m = uint32_t(keys[ty * c.rw + tx] >> 32);
-              if (ty + 4 < c.rh) m = max(m, uint32_t(keys[(ty + 4) * c.rw + tx] >> 32));
+          // each tile and coarse tile; pixels outside the region count as 0.
+          // One warp per coarse tile: lane x reads column x of its 32 rows
+          // (a warp reads 32 consecutive keys, free of bank conflicts), every
+          // 8 rows groups of 8 lanes give the 4 tiles of that band, and the
+          // whole warp gives the coarse tile.
+          for (int u = warp; u < ccols * crows; u += T / 32) {
+            const int x = (u % ccols) * (kTile * kCoarse) + lane, y0 = (u / ccols) * (kTile * kCoarse);
+            uint32_t band = 0, all = 0;
+            for (int r = 0; r < kTile * kCoarse && y0 + r < c.rh; ++r) {
+              if (x < c.rw) band = max(band, uint32_t(keys[(y0 + r) * c.rw + x] >> 32));
+              if ((r & (kTile - 1)) == kTile - 1 || y0 + r == c.rh - 1) {
+                uint32_t b = band;
+                b = max(b, __shfl_xor_sync(0xffffffffu, b, 1));
+                b = max(b, __shfl_xor_sync(0xffffffffu, b, 2));
+                b = max(b, __shfl_xor_sync(0xffffffffu, b, 4));
+                const int tx = (u % ccols) * kCoarse + (lane >> 3), ty = (y0 + r) / kTile;
+                if ((lane & 7) == 0 && tx < tcols) tiles[ty * tcols + tx] = b;
+                all = max(all, band);
+                band = 0;
+              }
             }
-            m = __reduce_max_sync(0xffffffffu, m);
-            if (lane == 0) tiles[t] = m;
-          }
-          __syncthreads();
-          for (int t = threadIdx.x; t < ccols * crows; t += T) {
-            const int cx0 = (t % ccols) * kCoarse, cy0 = (t / ccols) * kCoarse;
-            uint32_t m = 0;
-            for (int y = cy0; y < min(cy0 + kCoarse, trows); ++y)
-              for (int x = cx0; x < min(cx0 + kCoarse, tcols); ++x) m = max(m, tiles[y * tcols + x]);
-            coarse[t] = m;
+            all = __reduce_max_sync(0xffffffffu, all);
+            if (lane == 0) coarse[u] = all;
           }
           __syncthreads();
           tiles_stale = false;
@@ -1368,10 +1466,28 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
       }
       if (wr == rd) break;  // every chunk culled or drawn
 
-      // ---- round: one chunk per warp
-      const uint32_t n = min(wr - rd, uint32_t(T / 32));
-      if (uint32_t(warp) < n) {
-        const uint2 ch = chunks[(rd + warp) & (ring_capacity(T) - 1)];
+      // ---- round: each warp takes chunks from the ring, one at a time, until
+      // the ring is empty or the queue holds three quarters of its capacity
+      // (a chunk adds at most 32 triangles, or a few more when clipped; the
+      // spill area and, beyond it, rasterisation by the lane itself take the
+      // excess).  Chunks are claimed by compare-and-swap, so the read position
+      // never passes the ring's write position.
+      for (;;) {
+        uint32_t slot = wr;
+        if (lane == 0 && *reinterpret_cast<volatile uint32_t*>(&s_qcount) < uint32_t(3 * T / 4)) {
+          uint32_t cur = *reinterpret_cast<volatile uint32_t*>(&s_rd);
+          while (cur < wr) {
+            const uint32_t prev = atomicCAS(&s_rd, cur, cur + 1u);
+            if (prev == cur) {
+              slot = cur;
+              break;
+            }
+            cur = prev;
+          }
+        }
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot >= wr) break;
+        const uint2 ch = chunks[slot & (ring_capacity(T) - 1)];
         const VisibleRec* rec = vis + ch.x;
         const uint32_t t = ch.y * kChunkTris + lane;
         if (t < __ldg(&rec->tri_count)) {
@@ -1397,7 +1513,6 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
           triangle(cv, __ldg(&rec->ordinal) + t, c);
         }
       }
-      if (threadIdx.x == 0) s_rd = rd + n;
       tiles_stale = true;
       __syncthreads();
     }
