@@ -138,6 +138,9 @@ PROTOTYPES = {
     "gbr_set_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
     "gbr_last_draw_stats": (_ST, [_P, ctypes.POINTER(DrawStats)]),
     "gbr_set_kernel_timing": (_ST, [_P, _I32]),
+    "gbr_set_device_memory_limit": (_ST, [_P, _U64]),
+    "gbr_device_memory": (_ST, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
+    "gbr_debug_corrupt_parent": (_ST, [_P, _U32, _U64, _I32]),
     "gbr_render_mesh_no_alloc": (_ST, [_P, _P, _P, _U32, _U32, c_float_p, c_float_p, _U32, _I32,
                                        _I32, _I32, _P, _P, _P, _P, _P]),
     # include/gbr_replay.h

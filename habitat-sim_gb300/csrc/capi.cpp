@@ -427,6 +427,21 @@ gbr_status gbr_set_kernel_timing(gbr_renderer* r, int32_t enabled) {
   return R(r)->set_kernel_timing(enabled != 0);
 }
 
+gbr_status gbr_set_device_memory_limit(gbr_renderer* r, uint64_t bytes) {
+  GBR_HANDLE(r);
+  return R(r)->set_memory_limit(bytes);
+}
+
+gbr_status gbr_device_memory(gbr_renderer* r, uint64_t* held, uint64_t* limit) {
+  GBR_HANDLE(r);
+  return R(r)->device_memory(held, limit);
+}
+
+gbr_status gbr_debug_corrupt_parent(gbr_renderer* r, uint32_t scene, uint64_t node, int32_t parent) {
+  GBR_HANDLE(r);
+  return guarded([&] { return R(r)->debug_corrupt_parent(scene, node, parent); });
+}
+
 gbr_status gbr_scenes_into_async(gbr_renderer* r, uint32_t plane, uint32_t first, uint32_t count,
                                  void* dst) {
   GBR_HANDLE(r);

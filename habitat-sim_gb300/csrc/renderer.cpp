@@ -52,12 +52,18 @@ const char* last_error_cstr() { return g_last_error.c_str(); }
 // ------------------------------------------------------------- buffers
 DeviceBuffer::~DeviceBuffer() {
   if (ptr) cudaFree(ptr);
+  if (budget) budget->held -= bytes;
 }
 
 bool DeviceBuffer::reserve(size_t n, bool keep, cudaStream_t stream) {
   if (n <= bytes) return true;
   size_t cap = std::max(n, bytes + bytes / 2);
   cap = (cap + 255) & ~size_t(255);
+  if (budget && budget->limit) {
+    // Within the limit: the usual growth, else exactly what is asked, else fail.
+    if (budget->held - bytes + cap > budget->limit) cap = (n + 255) & ~size_t(255);
+    if (budget->held - bytes + cap > budget->limit) return false;
+  }
   void* p = nullptr;
   if (cudaMalloc(&p, cap) != cudaSuccess) {
     cudaGetLastError();
@@ -70,6 +76,7 @@ bool DeviceBuffer::reserve(size_t n, bool keep, cudaStream_t stream) {
     }
   }
   if (ptr) cudaFree(ptr);
+  if (budget) budget->held = budget->held - bytes + cap;
   ptr = p;
   bytes = cap;
   return true;
@@ -176,6 +183,7 @@ Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
     return nullptr;
   }
   std::unique_ptr<Renderer> r(new Renderer());
+  r->attach_budget();
   r->cfg_ = cfg;
   r->max_lights_ = cfg.max_light_count;
   if (r->cfg_.planes == 0) r->cfg_.planes = GBR_PLANE_ALL;
@@ -268,6 +276,45 @@ Renderer* Renderer::create(const gbr_config& cfg, std::string& err) {
   gbr_material_data wm{{1, 1, 1, 1}, 0, 0, {1, 0, 0, 0, 1, 0, 0, 0, 1}};
   r->add_material(wm, &id);
   return r.release();
+}
+
+void Renderer::attach_budget() {
+  DeviceBuffer* all[] = {&d_pos_, &d_color_, &d_uv_, &d_indices_, &d_texels_, &d_normal_, &d_lights_,
+                         &d_model_, &d_spill_, &d_gather_, &d_hbao_scenes_, &d_hbao_ao_, &d_meshes_,
+                         &d_materials_, &d_textures_, &d_boxes_, &d_scenes_, &d_parents_, &d_local_,
+                         &d_draws_, &d_cameras_, &d_visible_, &d_order_, &d_vis_count_, &d_vis_tris_,
+                         &d_vis_clusters_, &d_status_, &d_items_, &d_items_lpt_, &d_counter_};
+  for (DeviceBuffer* b : all) b->budget = &budget_;
+  for (auto& set : d_planes_)
+    for (DeviceBuffer& b : set) b.budget = &budget_;
+}
+
+gbr_status Renderer::set_memory_limit(uint64_t bytes) {
+  budget_.limit = bytes;
+  return GBR_OK;
+}
+
+gbr_status Renderer::device_memory(uint64_t* held, uint64_t* limit) const {
+  if (held) *held = budget_.held;
+  if (limit) *limit = budget_.limit;
+  return GBR_OK;
+}
+
+// Fault injection: the parent of `node` replaced in device memory only,
+// after the host validated and uploaded the scene (the host copy stays
+// right, and is uploaded again once the device reports the bad record).
+gbr_status Renderer::debug_corrupt_parent(uint32_t scene, uint64_t node, int32_t parent) {
+  if (gbr_status st = check_scene(scene, "debugCorruptParent")) return st;
+  if (node >= scenes_[scene].parents.size())
+    return fail(GBR_ERROR_INVALID_ARGUMENT, "debugCorruptParent: node out of range");
+  if (structure_dirty_)
+    if (gbr_status st = rebuild(last_stream_)) return st;
+  cudaSetDevice(device_);
+  GBR_CUDA(cudaStreamSynchronize(last_stream_), "debugCorruptParent: synchronise");
+  const size_t at = size_t(scenes_[scene].node_base) + size_t(node);
+  GBR_CUDA(cudaMemcpy(d_parents_.as<int32_t>() + at, &parent, 4, cudaMemcpyHostToDevice),
+           "debugCorruptParent: write");
+  return GBR_OK;
 }
 
 Renderer::~Renderer() {
@@ -1413,9 +1460,15 @@ gbr_status Renderer::sync_and_check() {
     uint32_t status = 0;
     GBR_CUDA(cudaMemcpy(&status, d_status_.ptr, 4, cudaMemcpyDeviceToHost), "status read");
     if (status) {
+      // The host's scene records are authoritative: upload them again at the
+      // next draw, so that a record damaged on the device does not persist.
       cudaMemset(d_status_.ptr, 0, 4);
+      structure_dirty_ = true;
       return fail(GBR_ERROR_DEVICE, "draw: the device reported bad scene data (status " +
-                                        std::to_string(status) + ")");
+                                        std::to_string(status) +
+                                        ((status & kStatusBadNode) ? ": a node's parent is out of range" : "") +
+                                        ((status & kStatusHierarchyTooDeep) ? ": a hierarchy deeper than 64 or a cycle" : "") +
+                                        "); the scene records are uploaded again at the next draw");
     }
   }
   return GBR_OK;

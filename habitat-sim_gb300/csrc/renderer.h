@@ -18,10 +18,17 @@
 
 namespace gbr {
 
-// A growable device allocation.
+// Device bytes a renderer's buffers may hold (0: no limit) and hold now.
+struct DeviceBudget {
+  uint64_t limit = 0;
+  uint64_t held = 0;
+};
+
+// A growable device allocation, charged to a budget when it has one.
 struct DeviceBuffer {
   void* ptr = nullptr;
   size_t bytes = 0;
+  DeviceBudget* budget = nullptr;
   ~DeviceBuffer();
   bool reserve(size_t n, bool keep, cudaStream_t stream = nullptr);
   template <class T>
@@ -147,6 +154,9 @@ class Renderer {
   gbr_status set_tuning(const gbr_tuning& t);
   gbr_status last_stats(gbr_draw_stats* out);
   gbr_status set_kernel_timing(bool on);
+  gbr_status set_memory_limit(uint64_t bytes);
+  gbr_status device_memory(uint64_t* held, uint64_t* limit) const;
+  gbr_status debug_corrupt_parent(uint32_t scene, uint64_t node, int32_t parent);
 
   uint32_t scene_count() const { return uint32_t(scenes_.size()); }
   const gbr_config& config() const { return cfg_; }
@@ -200,7 +210,10 @@ class Renderer {
   std::vector<SceneState> scenes_;
   bool structure_dirty_ = true;
 
-  // device
+  // device (every buffer below is charged to budget_, declared first so that
+  // it outlives them)
+  DeviceBudget budget_;
+  void attach_budget();
   DeviceBuffer d_pos_, d_color_, d_uv_, d_indices_, d_texels_, d_normal_;
   DeviceBuffer d_lights_, d_model_;  // lit renderers: world lights, per-draw model data
   DeviceBuffer d_spill_;  // raster queue spill area, per CTA

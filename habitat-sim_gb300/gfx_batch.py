@@ -561,6 +561,22 @@ class RendererStandalone:
         draws; read back through lastDrawStats() (prepare_ms, raster_ms)."""
         check(self._lib.gbr_set_kernel_timing(self._h, 1 if enabled else 0))
 
+    def setDeviceMemoryLimit(self, limit_bytes):
+        """Cap the device memory this renderer's buffers may hold (0: none);
+        an allocation beyond it fails with GBR_ERROR_OUT_OF_MEMORY."""
+        check(self._lib.gbr_set_device_memory_limit(self._h, int(limit_bytes)))
+
+    def deviceMemory(self):
+        """(bytes held by the renderer's device buffers, limit or 0)."""
+        held, limit = ctypes.c_uint64(), ctypes.c_uint64()
+        check(self._lib.gbr_device_memory(self._h, ctypes.byref(held), ctypes.byref(limit)))
+        return held.value, limit.value
+
+    def debugCorruptParent(self, scene, node, parent):
+        """Fault injection for tests: the node's parent replaced in device
+        memory only; the next draw reports GBR_ERROR_DEVICE."""
+        check(self._lib.gbr_debug_corrupt_parent(self._h, int(scene), int(node), int(parent)))
+
     def tuning(self):
         t = _lib.Tuning()
         check(self._lib.gbr_get_tuning(self._h, ctypes.byref(t)))

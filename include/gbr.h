@@ -334,6 +334,24 @@ typedef struct gbr_draw_stats {
 gbr_status gbr_set_kernel_timing(gbr_renderer* r, int32_t enabled);
 gbr_status gbr_last_draw_stats(gbr_renderer* r, gbr_draw_stats* out);
 
+/* Device-memory limit of one renderer (no counterpart in the reference):
+ * an add, draw or readback whose device allocation would take the
+ * renderer's buffers above `bytes` fails with GBR_ERROR_OUT_OF_MEMORY and
+ * leaves the renderer usable; 0 (the default) is no limit.  Lowering the
+ * limit below what the renderer holds frees nothing. */
+gbr_status gbr_set_device_memory_limit(gbr_renderer* r, uint64_t bytes);
+/* Device bytes the renderer's buffers hold now, and the limit. */
+gbr_status gbr_device_memory(gbr_renderer* r, uint64_t* held, uint64_t* limit);
+
+/* Fault injection for tests (no counterpart in the reference): replaces, in
+ * device memory only, the parent index of `node` of `scene` after the host
+ * has validated and uploaded the scene's records.  The next draw's prepare
+ * kernel finds the bad record and sets the device status word, and the next
+ * readback or gbr_last_draw_stats returns GBR_ERROR_DEVICE; the host's
+ * records are then uploaded again at the following draw.  An out-of-range
+ * parent reports a bad node, a parent cycle a hierarchy deeper than 64. */
+gbr_status gbr_debug_corrupt_parent(gbr_renderer* r, uint32_t scene, uint64_t node, int32_t parent);
+
 /* Renders one triangle mesh into caller-owned device planes without
  * allocating any memory.  No counterpart in the reference: it is for callers
  * that must not call cudaMalloc -- code running inside another framework's
