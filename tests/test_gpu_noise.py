@@ -64,6 +64,21 @@ def test_reference_gpu_cpu_comparison(noise):
         assert np.abs(g - c).mean() <= tol
 
 
+def test_reference_code_comparison(noise):
+    """The same statistical test against habitat-sim's own CPU code: the
+    means of 100 GPU simulations of the ramp against the means of its
+    _simulate, run from the reference's source when the fixture was made
+    (tests/golden/make_redwood_means.py)."""
+    import os
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "redwood",
+                               "reference_means.npz"))
+    depth = np.linspace(0, 20, num=256 * 256, dtype=np.float32).reshape(256, 256)
+    for mult, tol, want in [(0.0, 1e-5, ref["mult0"]), (1.0, 1e-2, ref["mult1"])]:
+        gpu = noise.RedwoodDepthNoiseModel(noise_multiplier=mult, gpu_device_id=0, seed=31)
+        g = np.mean(np.stack([gpu(depth) for _ in range(100)]), 0)
+        assert np.abs(g - want).mean() <= tol
+
+
 def test_device_and_host_paths_agree(noise):
     import torch
     depth = depth_cases()[1]

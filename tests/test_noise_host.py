@@ -95,3 +95,27 @@ def test_noise_without_gpu_fails_cleanly(pkg, model):
     from habitat_sim_gb300 import noise
     with pytest.raises(pkg.GbrError):
         noise.RedwoodDepthNoiseModel(noise_multiplier=1.0)
+
+
+def _reference_means():
+    """Means of habitat-sim's own _simulate (run from its source by
+    tests/golden/make_redwood_means.py) over the reference test's ramp."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "redwood",
+                        "reference_means.npz")
+    return np.load(path)
+
+
+@pytest.mark.parametrize("mult,tolerance", [(0.0, 1e-5), (1.0, 1e-2)])
+def test_restatements_match_reference_code(model, mult, tolerance):
+    """Both restatements against the reference's own CPU code: the means of
+    100 simulations of the 0-20 m ramp within the tolerances of the
+    reference's GPU-versus-CPU test (tests/test_noise_models.py:24-51)."""
+    ref = _reference_means()
+    want = ref["mult0"] if mult == 0.0 else ref["mult1"]
+    depth = np.linspace(0, 20, num=256 * 256, dtype=np.float32).reshape(256, 256)
+    rng = np.random.default_rng(7)
+    cpu = np.mean([N.redwood_reference_cpu(depth, model, mult, rng) for _ in range(100)], 0)
+    assert np.abs(cpu - want).mean() <= tolerance
+    table = N.normal_table()
+    ker = np.mean([N.redwood_f32(depth, model, mult, 5, c, table=table) for c in range(100)], 0)
+    assert np.abs(ker - want).mean() <= tolerance
