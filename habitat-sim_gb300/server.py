@@ -23,7 +23,9 @@ for a request-driven caller of the same draw path.
 import collections
 import concurrent.futures
 import dataclasses
+import gc
 import math
+import os
 import time
 
 import numpy as np
@@ -44,7 +46,8 @@ class SceneAsset:
     texcoords: np.ndarray   # [V, 2] float32
     object_ids: np.ndarray  # [V] uint32
     indices: np.ndarray     # [3T] uint32
-    texture: np.ndarray     # [h, w, 4] uint8
+    texture: np.ndarray     # [layers, h, w, 4] uint8
+    parts: list             # per object: (first index, index count, texture layer)
 
     @property
     def triangles(self):
@@ -52,18 +55,42 @@ class SceneAsset:
 
     def device_bytes(self):
         """Bytes the renderer keeps on the device for this scene: 40 per
-        vertex (position, colour, texcoord), 4 per index, 4 per texel, 32 per
-        box (one per 32-triangle chunk and one per 32 chunks)."""
-        chunks = (self.triangles + 31) // 32
-        boxes = chunks + (chunks + 31) // 32
+        vertex (position, colour, texcoord), 4 per index, 4 per texel, and
+        per object (one mesh view) 32 per box: one per 32-triangle chunk and
+        one per 32 chunks."""
+        boxes = 0
+        for (_, count, _) in self.parts:
+            chunks = (count // 3 + 31) // 32
+            boxes += chunks + (chunks + 31) // 32
         return len(self.positions) * 40 + len(self.indices) * 4 + self.texture.size + boxes * 32
 
 
-def serving_scene(seed, triangles, texture_size=64):
+class TexelPool:
+    """Uniform-noise RGBA8 texels (alpha 255) in host memory.  Every catalog
+    scene's texture layers are a window of the pool at an offset drawn from
+    the scene's seed: the host holds one pool, the device a distinct copy of
+    every resident scene's layers."""
+
+    def __init__(self, nbytes, seed):
+        rng = np.random.default_rng([seed, 2718])
+        self.data = np.frombuffer(rng.bytes(nbytes), np.uint8).copy()
+        self.data.reshape(-1, 4)[:, 3] = 255
+
+    def window(self, key, layers, side):
+        n = layers * side * side * 4
+        if n > len(self.data):
+            raise ValueError(f"{layers} layers of {side}^2 texels exceed the texel pool")
+        rng = np.random.default_rng([key, 161803])
+        off = int(rng.integers(0, (len(self.data) - n) // 4 + 1)) * 4
+        return self.data[off:off + n].reshape(layers, side, side, 4)
+
+
+def serving_scene(seed, triangles, texture=None):
     """One catalog scene of about ``triangles`` triangles: a 12 x 3 x 12 m
     room shell (80 % of the budget) and 20 boxes (20 %), random RGB per
     vertex, object id 1 for the shell and 2..21 for the boxes, planar
-    texcoords into one noise texture."""
+    texcoords.  ``texture`` is the scene's [layers, h, w, 4] texel array
+    (default: one 64 x 64 noise layer); object k samples layer k % layers."""
     rng = np.random.default_rng([seed, 104729])
     n = max(2, int(round(math.sqrt(0.8 * triangles / 12.0))))
     m = max(1, int(round(math.sqrt(0.2 * triangles / (20 * 12.0)))))
@@ -75,39 +102,77 @@ def serving_scene(seed, triangles, texture_size=64):
         lo = np.array([c[0] - size[0] / 2, 0.0, c[1] - size[2] / 2])
         parts.append(procedural.box_faces(lo, lo + size, m, inward=False))
         ids.append(np.full(len(parts[-1][0]), 2 + b, np.uint32))
-    pos, idx, base = [], [], 0
-    for p, t in parts:
+    if texture is None:
+        texture = rng.integers(0, 256, size=(1, 64, 64, 4), dtype=np.uint8)
+        texture[..., 3] = 255
+    layers = texture.shape[0]
+    pos, idx, views, base, first = [], [], [], 0, 0
+    for k, (p, t) in enumerate(parts):
         pos.append(p)
         idx.append(t + base)
+        views.append((first, t.size, k % layers))
         base += len(p)
+        first += t.size
     pos = np.concatenate(pos).astype(np.float32)
     col = np.ones((len(pos), 4), np.float32)
     col[:, :3] = rng.integers(0, 256, size=(len(pos), 3)).astype(np.float32) / np.float32(255.0)
     uv = np.stack([pos[:, 0] + pos[:, 1], pos[:, 2] + pos[:, 1]], 1).astype(np.float32) / 2.0
-    tex = rng.integers(0, 256, size=(texture_size, texture_size, 4), dtype=np.uint8)
-    tex[..., 3] = 255
     return SceneAsset(pos, col, uv, np.concatenate(ids),
-                      np.concatenate(idx).astype(np.uint32).reshape(-1), tex)
+                      np.concatenate(idx).astype(np.uint32).reshape(-1), texture, views)
+
+
+def add_asset(r, asset, name, texture_filter=1):
+    """Add one catalog scene's resources to renderer ``r`` (the GPU renderer
+    or the oracle): its texture array, its mesh, one material per texture
+    layer it uses, and a hierarchy template ``name`` with one mesh view per
+    object.  Returns (mesh, texture)."""
+    tex = r.addTexture(asset.texture, filter=texture_filter)
+    mesh = r.addMesh(asset.positions, asset.colors, asset.texcoords, asset.object_ids, asset.indices)
+    mats, views = {}, []
+    for (first, count, layer) in asset.parts:
+        if layer not in mats:
+            mats[layer] = r.addMaterial((1, 1, 1, 1), tex, layer)
+        views.append((mesh, first, count, mats[layer], None))
+    r.addNodeHierarchyTemplate(name, views)
+    return mesh, tex
 
 
 class SceneCatalog:
     """``count`` scenes with triangle counts log-uniform in ``tri_range``,
-    generated on first use from (seed, scene) and kept in host memory."""
+    generated on first use from (seed, scene) and kept in host memory.
+    With ``texture_side``, scene s gets max(1, round(triangles /
+    tris_per_layer)) texture layers of texture_side^2 RGBA8 noise, windows
+    of one shared host pool of ``pool_bytes`` (the default sizes make a
+    256-scene catalog of 10k-1M triangles about 40 GB on the device);
+    otherwise one 64 x 64 layer per scene."""
 
-    def __init__(self, count, seed=0, tri_range=(1e4, 1e6)):
+    def __init__(self, count, seed=0, tri_range=(1e4, 1e6), texture_side=None,
+                 tris_per_layer=24000, pool_bytes=1 << 30):
         rng = np.random.default_rng([seed, 31337])
         self.seed = seed
         self.targets = np.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1]), count))
+        self.texture_side = texture_side
+        self.tris_per_layer = tris_per_layer
+        self.pool_bytes = pool_bytes
+        self._pool = None
         self._assets = {}
 
     def __len__(self):
         return len(self.targets)
 
+    def layers(self, scene):
+        return max(1, int(round(self.targets[scene] / self.tris_per_layer))) if self.texture_side else 1
+
     def asset(self, scene):
         a = self._assets.get(scene)
         if a is None:
-            a = self._assets[scene] = serving_scene(self.seed * 100003 + scene,
-                                                    int(self.targets[scene]))
+            key = self.seed * 100003 + scene
+            tex = None
+            if self.texture_side:
+                if self._pool is None:
+                    self._pool = TexelPool(self.pool_bytes, self.seed)
+                tex = self._pool.window(key, self.layers(scene), self.texture_side)
+            a = self._assets[scene] = serving_scene(key, int(self.targets[scene]), tex)
         return a
 
 
@@ -130,22 +195,39 @@ class Request:
         return self.done - self.arrival
 
 
+def _rot(axis, a):
+    """Rotation matrices [..., 3, 3] by angles ``a`` about x (0), y (1), z (2)."""
+    c, s = np.cos(a), np.sin(a)
+    m = np.zeros(np.shape(a) + (3, 3))
+    i, j = [(1, 2), (2, 0), (0, 1)][axis]
+    k = 3 - i - j
+    m[..., k, k] = 1.0
+    m[..., i, i] = c
+    m[..., i, j] = -s
+    m[..., j, i] = s
+    m[..., j, j] = c
+    return m
+
+
+def pose_views(x, y, z, yaw, pitch, roll):
+    """World -> camera matrices ([n][col][row] float32) of cameras at
+    (x, y, z) rotated by yaw (about +y), then pitch (about +x), then roll
+    (about -z); arguments are arrays of n values."""
+    r = _rot(1, np.asarray(yaw, np.float64)) @ _rot(0, np.asarray(pitch, np.float64)) @ \
+        _rot(2, np.asarray(roll, np.float64))
+    t = np.stack([x, y, z], -1).astype(np.float64)
+    inv = np.zeros(r.shape[:-2] + (4, 4))
+    rt = np.swapaxes(r, -1, -2)
+    inv[..., :3, :3] = rt
+    inv[..., :3, 3] = -(rt @ t[..., None])[..., 0]
+    inv[..., 3, 3] = 1.0
+    return np.swapaxes(inv, -1, -2).astype(np.float32)
+
+
 def pose_view(x, y, z, yaw, pitch, roll):
-    """World -> camera matrix ([col][row]) of a camera at (x, y, z) rotated
-    by yaw (about +y), then pitch (about +x), then roll (about -z)."""
-    def rot(axis, a):
-        c, s = math.cos(a), math.sin(a)
-        m = np.eye(3)
-        i, j = [(1, 2), (2, 0), (0, 1)][axis]
-        m[i, i] = c
-        m[i, j] = -s
-        m[j, i] = s
-        m[j, j] = c
-        return m
-    cam = np.eye(4)
-    cam[:3, :3] = rot(1, yaw) @ rot(0, pitch) @ rot(2, roll)
-    cam[:3, 3] = [x, y, z]
-    return np.linalg.inv(cam).T.astype(np.float32)
+    """pose_views for one camera."""
+    return pose_views(np.array([x]), np.array([y]), np.array([z]), np.array([yaw]),
+                      np.array([pitch]), np.array([roll]))[0]
 
 
 def random_requests(catalog, count, rate, seed=0, classes=CLASSES, p=CLASS_P, zipf=None):
@@ -162,14 +244,14 @@ def random_requests(catalog, count, rate, seed=0, classes=CLASSES, p=CLASS_P, zi
     else:
         scenes = rng.integers(0, len(catalog), count)
     res = rng.choice(classes, size=count, p=p)
-    out = []
-    for i in range(count):
-        x, z = rng.uniform(ROOM_LO[[0, 2]] + 0.5, ROOM_HI[[0, 2]] - 0.5)
-        y = rng.uniform(0.5, 2.5)
-        view = pose_view(x, y, z, rng.uniform(0, 2 * math.pi), math.radians(rng.uniform(-30, 30)),
-                         math.radians(rng.uniform(-10, 10)))
-        out.append(Request(int(scenes[i]), int(res[i]), view, 90.0, float(arrivals[i]), i))
-    return out
+    xz = rng.uniform(ROOM_LO[[0, 2]] + 0.5, ROOM_HI[[0, 2]] - 0.5, size=(count, 2))
+    y = rng.uniform(0.5, 2.5, count)
+    yaw = rng.uniform(0, 2 * math.pi, count)
+    pitch = np.radians(rng.uniform(-30, 30, count))
+    roll = np.radians(rng.uniform(-10, 10, count))
+    views = pose_views(xz[:, 0], y, xz[:, 1], yaw, pitch, roll)
+    return [Request(int(scenes[i]), int(res[i]), views[i], 90.0, float(arrivals[i]), i)
+            for i in range(count)]
 
 
 # ------------------------------------------------------------ host policies
@@ -223,10 +305,20 @@ class Residency:
         return slot
 
 
-def take_batch(queues, slots):
+def take_batch(queues, slots, max_batch=None):
     """Continuous batching: up to ``slots[c]`` oldest requests of each
-    resolution class ``c`` (FIFO per class)."""
+    resolution class ``c`` (FIFO per class); with ``max_batch``, at most that
+    many requests in all, the earliest arrivals first."""
     batch = {}
+    if max_batch is not None:
+        for _ in range(max_batch):
+            heads = [(q[0].arrival, c) for c, q in queues.items()
+                     if q and len(batch.get(c, ())) < slots.get(c, 0)]
+            if not heads:
+                break
+            c = min(heads)[1]
+            batch.setdefault(c, []).append(queues[c].popleft())
+        return batch
     for c, q in queues.items():
         k = min(len(q), slots.get(c, 0))
         if k:
@@ -293,7 +385,8 @@ class RenderServer:
                                   pin_memory=True) for t in self.planes] for _ in range(2)]
         self._proj = {}
         self._step = 0
-        self._copier = concurrent.futures.ThreadPoolExecutor(max_workers=9)
+        self._copier = concurrent.futures.ThreadPoolExecutor(
+            max_workers=max(1, min(8, (os.cpu_count() or 2) - 1)))
 
     def close(self):
         self._copier.shutdown()
@@ -309,11 +402,8 @@ class RenderServer:
             self._evict(victim)
         r = self.r
         live0 = r.memoryUsage()[0]
-        tex = r.addTexture(a.texture, filter=0)
-        mesh = r.addMesh(a.positions, a.colors, a.texcoords, a.object_ids, a.indices)
-        mat = r.addMaterial((1, 1, 1, 1), tex, 0)
         name = f"serving/{scene}"
-        r.addNodeHierarchyTemplate(name, [(mesh, 0, len(a.indices), mat, None)])
+        mesh, tex = add_asset(r, a, name)
         nbytes = r.memoryUsage()[0] - live0
         slot = self.residency.add(scene, nbytes)
         r.addNodeHierarchy(self.content_base + slot, name)
@@ -396,11 +486,18 @@ class RenderServer:
         ev.record(self.stream)
         return (batch, buf, ev), deferred
 
-    def finish(self, handle, clock=None):
-        """Wait for a launched step and hand each request its images."""
+    def finish(self, handle, clock=None, keep_images=True):
+        """Wait for a launched step and hand each request its images (with
+        ``keep_images`` false, only its completion time: the images reached
+        pinned host memory, where they stay until the step after next)."""
         batch, buf, ev = handle
         ev.synchronize()
         now = clock() if clock else math.nan
+        if not keep_images:
+            for reqs in batch.values():
+                for req in reqs:
+                    req.done = now
+            return batch
         planes = [t.numpy() for t in buf]
         # One new array per resolution class and plane, copied out of the
         # double-buffered pinned staging on worker threads (the copies are
@@ -421,16 +518,30 @@ class RenderServer:
         return batch
 
     # -- the request loop
-    def serve(self, requests, realtime=True):
+    def serve(self, requests, realtime=True, keep_images=True, max_batch=None):
         """Serve ``requests`` (sorted by arrival).  With ``realtime`` a request
         is admitted once the wall clock passes its arrival time; otherwise
         all are pending from the start (a closed-loop saturation run).
-        Returns statistics; each request gets its images and ``done``."""
+        ``max_batch`` caps the requests of one step (1: the plain path, one
+        request per draw).  Returns statistics; each request gets ``done``
+        and, with ``keep_images``, its images."""
         queues = {c: collections.deque() for c in self.slots}
         pending = collections.deque(sorted(requests, key=lambda q: q.arrival))
         for req in pending:
             if req.resolution not in self.slots:
                 raise ValueError(f"no render slots for resolution {req.resolution}")
+        # The cyclic garbage collector is paused while serving: a full
+        # collection walks every live request (images included) and stalls the
+        # loop for tens of milliseconds, which would show in the tail latency.
+        gc_was_enabled = gc.isenabled()
+        gc.disable()
+        try:
+            return self._serve(queues, pending, requests, realtime, keep_images, max_batch)
+        finally:
+            if gc_was_enabled:
+                gc.enable()
+
+    def _serve(self, queues, pending, requests, realtime, keep_images, max_batch):
         t0 = time.perf_counter()
         clock = lambda: time.perf_counter() - t0
         if not realtime:
@@ -444,7 +555,7 @@ class RenderServer:
             while pending and pending[0].arrival <= now:
                 req = pending.popleft()
                 queues[req.resolution].append(req)
-            batch = take_batch(queues, self.slots)
+            batch = take_batch(queues, self.slots, max_batch)
             if batch:
                 handle, deferred = self.launch(batch)
                 for req in reversed(deferred):
@@ -453,7 +564,7 @@ class RenderServer:
                 steps += 1
                 batched += sum(len(v) for v in handle[0].values())
             if inflight and (len(inflight) >= 2 or not batch):
-                self.finish(inflight.popleft(), clock)
+                self.finish(inflight.popleft(), clock, keep_images)
             elif not batch and pending:
                 time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.002)))
         elapsed = clock()

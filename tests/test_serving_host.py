@@ -90,7 +90,38 @@ def test_catalog_scene_sizes(server):
         assert 0.6 * cat.targets[s] < a.triangles < 1.6 * cat.targets[s]
         assert a.indices.max() < len(a.positions)
         assert set(np.unique(a.object_ids)) == set(range(1, 22))
-        chunks = (a.triangles + 31) // 32
-        boxes = chunks + (chunks + 31) // 32
+        # One mesh view per object (the shell, 20 boxes), covering the indices in order.
+        assert len(a.parts) == 21
+        assert sum(n for (_, n, _) in a.parts) == len(a.indices)
+        assert [f for (f, _, _) in a.parts] == list(np.cumsum([0] + [n for (_, n, _) in a.parts])[:-1])
+        boxes = 0
+        for (_, n, _) in a.parts:
+            chunks = (n // 3 + 31) // 32
+            boxes += chunks + (chunks + 31) // 32
         assert a.device_bytes() == len(a.positions) * 40 + a.triangles * 12 + 64 * 64 * 4 + boxes * 32
     assert cat.asset(2) is cat.asset(2)
+
+
+def test_textured_catalog_layers_and_sizes(server):
+    """The serving benchmark's textured catalog: a scene of T triangles gets
+    max(1, round(T / tris_per_layer)) noise layers, windows of one host pool
+    (alpha 255), and object k samples layer k % layers."""
+    cat = server.SceneCatalog(6, seed=2, tri_range=(1e4, 1e5), texture_side=64, tris_per_layer=12000,
+                              pool_bytes=1 << 22)
+    for s in range(6):
+        a = cat.asset(s)
+        L = max(1, int(round(cat.targets[s] / 12000)))
+        assert a.texture.shape == (L, 64, 64, 4) and (a.texture[..., 3] == 255).all()
+        assert [layer for (_, _, layer) in a.parts] == [k % L for k in range(21)]
+        assert a.device_bytes() > a.texture.size
+    assert not np.array_equal(cat.asset(0).texture[0], cat.asset(1).texture[0])
+
+
+def test_take_batch_caps_the_step():
+    """max_batch takes the earliest arrivals across classes, within the slots."""
+    import collections
+    from habitat_sim_gb300 import server as srv
+    reqs = [srv.Request(0, c, None, arrival=t) for (c, t) in ((64, 0.3), (128, 0.1), (64, 0.2))]
+    queues = {64: collections.deque([reqs[2], reqs[0]]), 128: collections.deque([reqs[1]])}
+    b = srv.take_batch(queues, {64: 4, 128: 4}, max_batch=2)
+    assert b == {128: [reqs[1]], 64: [reqs[2]]} and list(queues[64]) == [reqs[0]]
