@@ -22,9 +22,16 @@ Printed (rank 0, one JSON line):
   cpu_baseline the CPU oracle (the renderer restated in C++) on a bounded
                sample of the same envs, all host threads;
   parity       sampled envs of the timed workload against the oracle;
-  serving      request serving over 256 scenes (continuous batching, LRU
-               device budget): saturation requests/s, p50/p99 latency under
-               Poisson arrivals, an eviction run with a small budget.
+  configs      the same measurements (batched, plain, e2e, roofline, parity
+               sample, CPU oracle) for the other workloads: config0 (16 envs,
+               one room), config2 (4096 envs, 64 scenes of 20k-2M triangles,
+               mixed resolutions), config3 (256 envs of 5M-triangle scans,
+               the 100-step camera walk);
+  serving      request serving over 256 textured scenes (about 40 GB on the
+               device; continuous batching, 150 GB budget with LRU
+               eviction): saturation requests/s, p50/p99 latency under
+               Poisson arrivals swept towards saturation, the plain
+               one-request path, an eviction run with a small budget.
 
 ``--impl reference`` times the CPU restatement alone on this workload (the
 reference renderer itself is GL-only and cannot run here)."""
@@ -59,14 +66,22 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--envs", type=int, default=None)
-    p.add_argument("--workload", default="config1", choices=["config1", "config2", "config3"],
-                   help="config1 (the metric's workload) by default; config2/config3 for reference")
+    p.add_argument("--workload", default="config1", choices=["config0", "config1", "config2", "config3"],
+                   help="the main line's workload: config1 (the metric's) by default")
+    p.add_argument("--configs", type=lambda t: [] if t in ("", "none") else t.split(","),
+                   default=["config0", "config2", "config3"],
+                   help="workloads measured as sub-blocks of the line (comma list, or none)")
+    p.add_argument("--parity-envs", type=int, default=64)
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--no-replay", action="store_true")
     p.add_argument("--no-postprocess", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--serving-scenes", type=int, default=256)
-    p.add_argument("--serving-requests", type=int, default=20000)
+    p.add_argument("--serving-requests", type=int, default=100000)
+    p.add_argument("--serving-plain-requests", type=int, default=3000)
+    p.add_argument("--serving-texture-side", type=int, default=2048)
+    p.add_argument("--serving-fractions", type=lambda t: [float(x) for x in t.split(",")],
+                   default=[0.1, 0.25, 0.5, 0.75, 0.9])
     return p.parse_args()
 
 
@@ -156,6 +171,9 @@ class ClockSampler:
 
 # ------------------------------------------------------------- workload
 WORKLOADS = {
+    "config0": ("config0 plain small: 16 envs sharing one procedural room (8 x 8 x 3 m box of 64 x 64 "
+                "quad grids, 49,152 triangles, + 20 boxes), per-vertex random RGB, per-object ids, "
+                "128x128 pinhole hfov 90 at 1.25 m, uniform position and yaw"),
     "config1": WORKLOAD,
     "config2": ("config2 uneven batching: 4096 envs over 64 procedural scenes of 20k-2M triangles "
                 "(log-uniform), per-env resolution 64/128/256 px (p 0.3/0.5/0.2), hfov U(60,110)"),
@@ -163,6 +181,33 @@ WORKLOADS = {
                 "(noisy 1.31 cm tessellation, value-noise colour, 64 Voronoi ids), 256x256, "
                 "random-walk cameras"),
 }
+PLANES = "rgba8 + f32 linear depth + u32 semantic id"
+
+
+def workload_config(name, wl):
+    """The ``config`` object of a JSON line: the same for both arms."""
+    return {"workload": WORKLOADS[name], "envs": wl.envs,
+            "resolution": sorted({w for (w, _) in wl.viewports}), "planes": PLANES}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
 
 
 def load_workload(name, envs=None):
@@ -201,56 +246,287 @@ def cpu_frames_per_s(procedural, wl, seconds, threads):
     return best[0] / best[1], best[0], best[1]
 
 
+def parity_envs(name, wl, count):
+    """Envs checked against the oracle: spread over the scenes (config2: the
+    envs of the largest scenes in every resolution class, and a spread of
+    the rest)."""
+    if name != "config2":
+        step = max(1, wl.envs // count)
+        return sorted({min(wl.envs - 1, i * step + i % 3) for i in range(count)})
+    tri = wl.triangles_per_env()
+    classes = sorted({w for (w, _) in wl.viewports})
+    out = []
+    for k, c in enumerate(classes):
+        envs = [e for e in range(wl.envs) if wl.viewports[e][0] == c]
+        envs.sort(key=lambda e: -int(tri[e]))
+        take = count // len(classes) + (1 if k < count % len(classes) else 0)
+        big = take // 2
+        rest = envs[big:]
+        out += envs[:big] + rest[::max(1, len(rest) // max(1, take - big))][:take - big]
+    return sorted(set(out))
+
+
+def check_parity(procedural, wl, r, host, envs, poses):
+    """Sampled envs of one step (read back into `host`) against the oracle:
+    pixels whose colour or id differ, largest linear-depth error where they agree."""
+    from oracle.model import OracleRenderer
+    host_color, host_lin, host_sem = host
+    cpu = procedural.build_oracle(OracleRenderer, wl, envs=envs)
+    procedural.set_cameras(cpu, wl, poses, envs)
+    cpu.draw(threads=os.cpu_count() or 1)
+    mism, max_err, px = 0, 0.0, 0
+    for slot, e in enumerate(envs):
+        off, pitch, w, h = r.sceneViewport(e)
+        if wl.uniform:
+            y0, x0 = off // pitch, off % pitch
+            g_col = host_color[y0:y0 + h, x0:x0 + w]
+            g_lin = host_lin[y0:y0 + h, x0:x0 + w]
+            g_sem = host_sem[y0:y0 + h, x0:x0 + w]
+        else:   # ragged: one row, scene after scene
+            g_col = host_color[0, off:off + w * h].reshape(h, w, 4)
+            g_lin = host_lin[0, off:off + w * h].reshape(h, w)
+            g_sem = host_sem[0, off:off + w * h].reshape(h, w)
+        c_col = cpu.scene_image(cpu.color, slot).view(np.uint8).reshape(h, w, 4)
+        c_lin = cpu.scene_image(cpu.linear_depth, slot)
+        c_sem = cpu.scene_image(cpu.semantic, slot)
+        same = (g_col == c_col).all(-1) & (g_sem == c_sem)
+        mism += int((~same).sum())
+        px += same.size
+        if same.any():
+            max_err = max(max_err, float(np.abs(g_lin[same].astype(np.float64) - c_lin[same]).max()))
+    return {"envs_checked": len(envs), "pixels": px, "mismatched_pixels": mism,
+            "max_linear_depth_err_m": max_err, "depth_tolerance_m": 1e-4}
+
+
+def measure(pkg, procedural, name, wl, steps, warmup, plain_steps, e2e_steps, parity_count, world=1,
+            rank=0, local_rank=0, autotune=True, keep=False):
+    """One workload: batched steps (CUDA graph, device-resident inputs, L2
+    flushed before every step, CUDA events on the launching stream), the
+    plain per-scene path, end to end through the C ABI with host buffers,
+    the raster kernel's roofline, and a parity sample of the last e2e step.
+    Returns (result dict, renderer if `keep` else None)."""
+    import torch
+    planes = pkg.Plane.Color | pkg.Plane.LinearDepth | pkg.Plane.Semantic
+    r = procedural.build_renderer(pkg, wl, mode=pkg.DrawMode.Batched, planes=planes, double_buffer=True)
+    r.setKernelTiming(True)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    n = warmup + max(steps, e2e_steps + 1)
+    poses = [procedural.camera_poses(wl, i) for i in range(n)]
+    tune_report = {"cached": None, "trials": []}
+    if autotune:
+        from habitat_sim_gb300 import autotune as at
+        _, tune_report = at.tune(
+            r, [procedural.camera_poses(wl, 1000 + i) for i in range(3)], int(wl.triangles_per_env().sum()),
+            cache=os.path.join(ROOT, "habitat-sim_gb300", "_build", "autotune.json"))
+
+    def batched_step(i, events=None):
+        flush.zero_()
+        r.updateCameras(*poses[i % n])
+        if events:
+            events[0].record(stream)
+        r.draw(stream=stream, mode=pkg.DrawMode.Batched, graph=True)
+        if events:
+            events[1].record(stream)
+
+    for i in range(warmup):
+        batched_step(i)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    barrier_sync(world)
+    step_ms, raster_ms, prepare_ms = [], [], []
+    tri = None
+    for k in range(steps):
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        batched_step(warmup + k, ev)
+        st = r.lastDrawStats()          # synchronises the stream
+        step_ms.append(ev[0].elapsed_time(ev[1]))
+        raster_ms.append(st["raster_ms"])
+        prepare_ms.append(st["prepare_ms"])
+        tri = st["triangles"]
+    barrier_sync(world)
+    clocks = sampler.stop()
+    total_ms = max_over_ranks(sum(step_ms), world)
+    value = job_frames_per_s(wl.envs, steps, world, total_ms)
+
+    # Plain per-scene path: one prepare + one raster launch per env, no graph.
+    plain_ms = []
+    for k in range(plain_steps + 1 if plain_steps else 0):
+        r.updateCameras(*poses[k % n])
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r.draw(stream=stream, mode=pkg.DrawMode.PerScene)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if k > 0:
+            plain_ms.append(e0.elapsed_time(e1))
+    plain_fps = wl.envs * len(plain_ms) / (sum(plain_ms) / 1e3) if plain_ms else None
+    t = r.tuning()
+    plain_ctas = [-(-w // t["plain_region_width"]) * -(-h // t["plain_region_height"]) for (w, h) in wl.viewports]
+
+    # End to end through the C ABI with host buffers: every step takes its
+    # poses from host arrays (uploaded in the step's camera block) and reads
+    # its three planes back into pinned host memory; the readback of step k
+    # runs on the renderer's copy stream from one set of planes while step
+    # k + 1 draws into the other (double buffering).
+    fbw, fbh = r.framebufferSize()
+
+    def host_set():
+        return (torch.empty((fbh, fbw, 4), dtype=torch.uint8, pin_memory=True).numpy(),
+                torch.empty((fbh, fbw), dtype=torch.float32, pin_memory=True).numpy(),
+                torch.empty((fbh, fbw), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32))
+    hosts = [host_set(), host_set()]
+    rect = ((0, 0), (fbw, fbh))
+    readback = (pkg.Plane.Color, pkg.Plane.LinearDepth, pkg.Plane.Semantic)
+
+    def e2e_step(k):
+        r.updateCameras(*poses[k % n])
+        r.draw(stream=stream, mode=pkg.DrawMode.Batched, graph=True)
+        for plane, buf in zip(readback, hosts[k % 2]):
+            r.imageIntoAsync(plane, rect, buf)
+
+    e2e_s = None
+    if e2e_steps:
+        e2e_step(0)
+        r.readbackWait()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(1, e2e_steps + 1):
+            e2e_step(k)
+        r.readbackWait()
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = wl.envs * 96   # the camera block (P*V, view row, binding) per env
+    d2h = sum(b.nbytes for b in hosts[0])
+    parity = None
+    if rank == 0 and e2e_steps and parity_count:
+        parity = check_parity(procedural, wl, r, hosts[e2e_steps % 2], parity_envs(name, wl, parity_count),
+                              poses[e2e_steps % n])
+
+    fb_bytes, geo_bytes = algorithmic_bytes(wl)
+    launch_bytes = fb_bytes + geo_bytes
+    raster_avg = statistics.mean(raster_ms)
+    achieved = launch_bytes / (raster_avg / 1e3) / 1e9
+    peak, peak_src = 6800.0, "fallback"
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"raster_kernel_{name}.txt")
+    if os.path.exists(tpath):
+        for line in open(tpath):
+            if line.startswith("dram_bytes_per_launch:"):
+                traffic = float(line.split(":")[1])
+    res = {
+        "value": value, "unit": "frames/s", "steps": steps, "warmup": warmup,
+        "ms_per_step": statistics.mean(step_ms), "p50_ms": float(np.percentile(step_ms, 50)),
+        "p99_ms": float(np.percentile(step_ms, 99)),
+        "plain": None if not plain_ms else {
+            "value": plain_fps, "unit": "frames/s", "ms_per_step": statistics.mean(plain_ms),
+            "p50_ms": float(np.percentile(plain_ms, 50)), "p99_ms": float(np.percentile(plain_ms, 99)),
+            "ctas_per_env": {"min": min(plain_ctas), "max": max(plain_ctas),
+                             "mean": float(np.mean(plain_ctas))},
+            "form": "per-scene prepare + raster launches (2 per env, one env after another), no graph; "
+                    "each env's raster launch is ctas_per_env CTAs of %d threads (%d x %d px regions)"
+                    % (t["threads"], t["plain_region_width"], t["plain_region_height"])},
+        "batched_over_plain": value / plain_fps if plain_fps else None,
+        "e2e": None if e2e_s is None else {
+            "value": wl.envs / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s,
+            "timing": ("host clock over the steps: updateCameras + draw + 3 imageIntoAsync readbacks per "
+                       "step, readback of step k overlapping the draw of step k+1, then readbackWait")},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                     "kernel": "raster_kernel", "bytes_per_launch": launch_bytes,
+                     "bytes_breakdown": {"framebuffer": fb_bytes, "geometry_textures": geo_bytes},
+                     "avg_launch_ms": raster_avg, "prepare_avg_ms": statistics.mean(prepare_ms),
+                     "visible_draw_triangles_per_launch": tri,
+                     "visible_draw_triangles_per_s": tri / (raster_avg / 1e3) if tri else None},
+        "triangles_per_step_before_culling": int(wl.triangles_per_env().sum()),
+        "tuning": t,
+        "autotune": None if not autotune else {"cached": tune_report["cached"],
+                                               "candidates": len(tune_report.get("trials", []))},
+        "clocks": clocks,
+        "parity": parity,
+        "gpu_launches": 2 * steps,
+    }
+    del flush
+    if keep:
+        return res, r
+    r.close()
+    return res, None
+
+
 def serving_leg(pkg, args):
-    """Request serving over a catalog of procedural scenes (triangles
-    log-uniform in 10k-1M, resolution 64/128/256 with p 0.3/0.5/0.2, 6-DoF
-    poses): continuous batching into 96 + 64 + 16 render slots per step, one
-    graph launch per step, slot rectangles copied back to pinned host memory
-    overlapped with the next step.  A closed-loop run (every request pending
-    at the start) gives the saturation rate; Poisson arrivals at 50 % and
-    80 % of it give latency percentiles (arrival to images in host memory);
-    a run with the device budget at a quarter of the catalog's bytes, Zipf(1)
-    scene popularity and 500 requests/s exercises LRU eviction."""
+    """Request serving on the serving workload: a catalog of 256 procedural
+    scenes (a 12 x 3 x 12 m room shell + 20 boxes, triangles log-uniform in
+    10k-1M, one 2048 x 2048 RGBA8 uniform-noise texture layer per 24k
+    triangles sampled bilinear, one mesh view and material per object: about
+    40 GB of geometry and textures on the device), requests (scene uniform,
+    6-DoF pose, 64/128/256 px with p 0.3/0.5/0.2), a 150 GB device budget with
+    LRU eviction.  Continuous batching into 96 + 64 + 16 render slots per
+    step, one graph launch per step, slot rectangles copied back to pinned
+    host memory overlapped with the next step.  Runs: every scene loaded
+    (timed); a closed-loop run of all requests (saturation); Poisson arrivals
+    at fractions of saturation (the sweep; latency from arrival to the three
+    images in pinned host memory); the plain path (one request per draw) on a
+    closed-loop sample; a run with the budget at a quarter of the catalog's
+    bytes, Zipf(1) popularity and 200 requests/s, where eviction works."""
     from habitat_sim_gb300 import server
     slots = {64: 96, 128: 64, 256: 16}
-    cat = server.SceneCatalog(args.serving_scenes, seed=4, tri_range=(1e4, 1e6))
+    n = args.serving_requests
     t0 = time.perf_counter()
+    cat = server.SceneCatalog(args.serving_scenes, seed=4, tri_range=(1e4, 1e6),
+                              texture_side=args.serving_texture_side)
     assets = [cat.asset(s) for s in range(len(cat))]
     gen_s = time.perf_counter() - t0
     total_bytes = sum(a.device_bytes() for a in assets)
+    tex_bytes = sum(a.texture.size for a in assets)
     tris = [a.triangles for a in assets]
-    n = args.serving_requests
-    out = {"workload": ("serving: %d procedural scenes (room shell + 20 boxes, %d-%d triangles, "
-                        "mean %d, log-uniform), requests (scene, 6-DoF pose, 64/128/256 px "
-                        "with p 0.3/0.5/0.2)" % (len(cat), min(tris), max(tris),
-                                                  int(np.mean(tris)))),
-           "slots": slots, "catalog_bytes": total_bytes, "catalog_generation_s": gen_s,
+    out = {"workload": ("serving: %d procedural scenes (room shell + 20 boxes, %d-%d triangles, mean %d, "
+                        "log-uniform; %d x %d RGBA8 noise texture layers, one per 24k triangles, bilinear), "
+                        "requests (scene uniform, 6-DoF pose, 64/128/256 px with p 0.3/0.5/0.2)"
+                        % (len(cat), min(tris), max(tris), int(np.mean(tris)), args.serving_texture_side,
+                           args.serving_texture_side)),
+           "slots": slots, "catalog_bytes": total_bytes, "catalog_texture_bytes": tex_bytes,
+           "catalog_geometry_bytes": total_bytes - tex_bytes, "catalog_generation_s": gen_s,
+           "budget_bytes": 150 * 10**9, "requests_per_run": n,
            "planes": "rgba8 + f32 linear depth + u32 semantic id per request",
-           "latency": "arrival to all three images in host memory"}
-    srv = server.RenderServer(pkg, cat, slots=slots, max_resident=len(cat),
-                              budget_bytes=150 * 10**9)
-    warm = server.random_requests(cat, max(len(cat), 2000), rate=0, seed=100)
-    for s, q in enumerate(warm[:len(cat)]):
+           "latency": "arrival to all three images in pinned host memory"}
+    srv = server.RenderServer(pkg, cat, slots=slots, max_resident=len(cat), budget_bytes=150 * 10**9,
+                              max_loads_per_step=len(cat))
+    warm = server.random_requests(cat, len(cat), rate=0, seed=100)
+    for s, q in enumerate(warm):
         q.scene = s                       # every scene resident before timing
     t0 = time.perf_counter()
-    srv.serve(warm, realtime=False)
+    srv.serve(warm, realtime=False, keep_images=False)
     out["warm_load_s"] = time.perf_counter() - t0
+    out["resident_bytes"] = int(srv.residency.bytes)
+    out["device_bytes_held"] = int(srv.r.deviceMemory()[0])
 
-    def keep(st):
-        return {k: st[k] for k in ("requests", "requests_per_s", "p50_ms", "p99_ms", "mean_ms",
-                                   "mean_batch", "steps", "loads", "evictions", "elapsed_s")}
-    sat = srv.serve(server.random_requests(cat, n, rate=0, seed=101), realtime=False)
-    out["saturation"] = keep(sat)
+    def keep(st, closed=False):
+        # A closed-loop run has every request pending at the start: its
+        # latencies are queueing time, so only its throughput is reported.
+        keys = ("requests", "requests_per_s", "mean_batch", "steps", "loads", "evictions", "elapsed_s")
+        return {k: st[k] for k in keys + (() if closed else ("p50_ms", "p99_ms", "mean_ms"))}
+    sat = srv.serve(server.random_requests(cat, n, rate=0, seed=101), realtime=False, keep_images=False)
+    out["saturation"] = dict(keep(sat, closed=True), form="closed loop: all requests pending at the start")
     rate = sat["requests_per_s"]
-    out["open_loop"] = []
-    for k, frac in enumerate((0.5, 0.8)):
-        st = srv.serve(server.random_requests(cat, n // 2, rate=frac * rate, seed=102 + k))
-        out["open_loop"].append(dict(offered_per_s=frac * rate, **keep(st)))
+    out["sweep"] = []
+    for k, frac in enumerate(args.serving_fractions):
+        st = srv.serve(server.random_requests(cat, n, rate=frac * rate, seed=102 + k), keep_images=False)
+        out["sweep"].append(dict(fraction=frac, offered_per_s=frac * rate, **keep(st)))
+    plain = srv.serve(server.random_requests(cat, args.serving_plain_requests, rate=0, seed=120),
+                      realtime=False, keep_images=False, max_batch=1)
+    out["plain"] = dict(keep(plain, closed=True), form="one request per step (one draw per request), closed loop")
+    out["saturation_over_plain"] = rate / plain["requests_per_s"]
     srv.close()
     budget = total_bytes // 4
     srv = server.RenderServer(pkg, cat, slots=slots, max_resident=len(cat), budget_bytes=budget)
-    st = srv.serve(server.random_requests(cat, 2500, rate=500.0, seed=110, zipf=1.0))
-    out["small_budget"] = dict(budget_bytes=budget, offered_per_s=500.0, popularity="zipf 1.0",
+    st = srv.serve(server.random_requests(cat, 1000, rate=200.0, seed=110, zipf=1.0), keep_images=False)
+    out["small_budget"] = dict(budget_bytes=budget, offered_per_s=200.0, popularity="zipf 1.0",
                                **keep(st))
     srv.close()
     return out
@@ -387,10 +663,10 @@ def run_reference_impl(args):
         "ms_per_step": statistics.mean(ms), "p50_ms": float(np.percentile(ms, 50)),
         "p99_ms": float(np.percentile(ms, 99)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload], "envs_per_step": per_step_envs,
-                   "sample": f"first {per_step_envs} of {wl.envs} envs per step"},
-        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
-                         "sample": f"{per_step_envs} envs per step, {args.steps} steps"},
+        "config": workload_config(args.workload, wl),
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "cpu_model": cpu_model(),
+                         "kind": "port",
+                         "sample": f"first {per_step_envs} of {wl.envs} envs per step, {args.steps} steps"},
         "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": ("the reference renderer is OpenGL-only (no GL, EGL or software rasteriser on "
@@ -398,6 +674,12 @@ def run_reference_impl(args):
     }
     print(json.dumps(line))
     return 0
+
+
+# Per-config sub-blocks of the default run: (steps, warmup, plain steps, e2e
+# steps, envs checked against the oracle).  config3's 100 steps are its
+# stated 100-step camera walk.
+SUB_CONFIGS = {"config0": (20, 3, 3, 10, 16), "config2": (10, 3, 1, 5, 16), "config3": (100, 3, 1, 5, 8)}
 
 
 def main():
@@ -412,218 +694,69 @@ def main():
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     pkg, procedural, wl = load_workload(args.workload, args.envs)
-    planes = pkg.Plane.Color | pkg.Plane.LinearDepth | pkg.Plane.Semantic
-    r = procedural.build_renderer(pkg, wl, mode=pkg.DrawMode.Batched, planes=planes,
-                                  double_buffer=True)
-    r.setKernelTiming(True)
+    main_res, r = measure(pkg, procedural, args.workload, wl, args.steps, args.warmup, args.plain_steps,
+                          args.e2e_steps, args.parity_envs, world, rank, local_rank,
+                          autotune=not args.no_autotune, keep=True)
     stream = torch.cuda.current_stream()
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    steps = args.warmup + args.steps
-    poses = [procedural.camera_poses(wl, i) for i in range(steps)]
-    # Launch shape chosen by the autotuner (cached per GPU and workload), or
-    # the library's default shape with --no-autotune.
-    tune_report = {"cached": None, "trials": []}
-    if not args.no_autotune:
-        from habitat_sim_gb300 import autotune
-        _, tune_report = autotune.tune(
-            r, [procedural.camera_poses(wl, 1000 + i) for i in range(3)],
-            int(wl.triangles_per_env().sum()),
-            cache=os.path.join(ROOT, "habitat-sim_gb300", "_build", "autotune.json"))
-
-    def batched_step(i, events=None):
-        flush.zero_()
-        r.updateCameras(*poses[i % steps])
-        if events:
-            events[0].record(stream)
-        r.draw(stream=stream, mode=pkg.DrawMode.Batched, graph=True)
-        if events:
-            events[1].record(stream)
-
-    for i in range(args.warmup):
-        batched_step(i)
-    torch.cuda.synchronize()
-
-    # ---- timed batched steps
-    sampler = ClockSampler(local_rank)
-    sampler.start()
-    time.sleep(0.3)
-    barrier_sync(world)
-    step_ms, raster_ms, prepare_ms = [], [], []
-    tri = None
-    for k in range(args.steps):
-        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-        batched_step(args.warmup + k, ev)
-        st = r.lastDrawStats()          # synchronises the stream
-        step_ms.append(ev[0].elapsed_time(ev[1]))
-        raster_ms.append(st["raster_ms"])
-        prepare_ms.append(st["prepare_ms"])
-        tri = st["triangles"]
-    barrier_sync(world)
-    clocks = sampler.stop()
-    total_ms = max_over_ranks(sum(step_ms), world)
-    value = job_frames_per_s(wl.envs, args.steps, world, total_ms)
-
-    # ---- plain per-scene path
-    plain_ms = []
-    for k in range(args.plain_steps + 1 if args.plain_steps else 0):
-        r.updateCameras(*poses[k % steps])
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        r.draw(stream=stream, mode=pkg.DrawMode.PerScene)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        if k > 0:
-            plain_ms.append(e0.elapsed_time(e1))
-    plain_fps = wl.envs * len(plain_ms) / (sum(plain_ms) / 1e3) if plain_ms else None
-
-    # ---- end to end through the C ABI with host buffers: every step takes
-    # its poses from host arrays (uploaded in the step's camera block) and
-    # reads its three planes back into pinned host memory; the readback of
-    # step k runs on the renderer's copy stream from one set of planes while
-    # step k + 1 draws into the other (double buffering).
-    fbw, fbh = r.framebufferSize()
-
-    def host_set():
-        return (torch.empty((fbh, fbw, 4), dtype=torch.uint8, pin_memory=True).numpy(),
-                torch.empty((fbh, fbw), dtype=torch.float32, pin_memory=True).numpy(),
-                torch.empty((fbh, fbw), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32))
-    hosts = [host_set(), host_set()]
-    rect = ((0, 0), (fbw, fbh))
-    readback = (pkg.Plane.Color, pkg.Plane.LinearDepth, pkg.Plane.Semantic)
-
-    def e2e_step(k):
-        r.updateCameras(*poses[k % steps])
-        r.draw(stream=stream, mode=pkg.DrawMode.Batched, graph=True)
-        for plane, buf in zip(readback, hosts[k % 2]):
-            r.imageIntoAsync(plane, rect, buf)
-
-    e2e_s = []
-    n_e2e = args.e2e_steps
-    if n_e2e:
-        e2e_step(0)
-        r.readbackWait()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for k in range(1, n_e2e + 1):
-            e2e_step(k)
-        r.readbackWait()
-        e2e_s = [(time.perf_counter() - t0) / n_e2e] * n_e2e
-    e2e_fps = wl.envs * len(e2e_s) / sum(e2e_s) if e2e_s else None
-    host_color, host_lin, host_sem = hosts[n_e2e % 2]
-    h2d = wl.envs * 96   # the camera block (P*V, view row, binding) per env
-    d2h = host_color.nbytes + host_lin.nbytes + host_sem.nbytes
-
-    # ---- parity of sampled envs against the oracle (last e2e step's poses)
-    parity = None
-    if rank == 0 and e2e_s:
-        from oracle.model import OracleRenderer
-        sample = [0, 1, 2, 3, wl.envs // 2 + 1, wl.envs - 1]
-        cpu = procedural.build_oracle(OracleRenderer, wl, envs=sample)
-        procedural.set_cameras(cpu, wl, poses[args.e2e_steps % steps], sample)
-        cpu.draw(threads=os.cpu_count() or 1)
-        mism, max_err, px = 0, 0.0, 0
-        for slot, e in enumerate(sample):
-            off, pitch, w, h = r.sceneViewport(e)
-            if wl.uniform:
-                y0, x0 = off // pitch, off % pitch
-                g_col = host_color[y0:y0 + h, x0:x0 + w]
-                g_lin = host_lin[y0:y0 + h, x0:x0 + w]
-                g_sem = host_sem[y0:y0 + h, x0:x0 + w]
-            else:   # ragged: one row, scene after scene
-                g_col = host_color[0, off:off + w * h].reshape(h, w, 4)
-                g_lin = host_lin[0, off:off + w * h].reshape(h, w)
-                g_sem = host_sem[0, off:off + w * h].reshape(h, w)
-            c_col = cpu.scene_image(cpu.color, slot).view(np.uint8).reshape(h, w, 4)
-            c_lin = cpu.scene_image(cpu.linear_depth, slot)
-            c_sem = cpu.scene_image(cpu.semantic, slot)
-            same = (g_col == c_col).all(-1) & (g_sem == c_sem)
-            mism += int((~same).sum())
-            px += same.size
-            if same.any():
-                max_err = max(max_err, float(np.abs(g_lin[same].astype(np.float64) -
-                                                    c_lin[same]).max()))
-        parity = {"envs_checked": len(sample), "pixels": px, "mismatched_pixels": mism,
-                  "max_linear_depth_err_m": max_err, "depth_tolerance_m": 1e-4}
-
-    # ---- roofline of the raster kernel
-    fb_bytes, geo_bytes = algorithmic_bytes(wl)
-    launch_bytes = fb_bytes + geo_bytes
-    raster_avg_ms = statistics.mean(raster_ms)
-    achieved = launch_bytes / (raster_avg_ms / 1e3) / 1e9
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    peak, peak_src = 6800.0, "fallback"
-    if os.path.exists(peaks_path):
-        peak = float(json.load(open(peaks_path))["hbm_gbs"])
-        peak_src = "measured"
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"raster_kernel_{args.workload}.txt")
-    if os.path.exists(tpath):
-        for line in open(tpath):
-            if line.startswith("dram_bytes_per_launch:"):
-                traffic = float(line.split(":")[1])
-
     post = None if args.no_postprocess else postprocess_leg(pkg, r, wl, stream)
-    serving = None if args.no_serving else serving_leg(pkg, args)
+    tuning = r.tuning()
+    r.close()
     replay = None
     if not args.no_replay and wl.uniform:
-        replay = replay_leg(pkg, procedural, wl, r.tuning())
+        replay = replay_leg(pkg, procedural, wl, tuning)
+    configs = {}
+    if world == 1:
+        for name in args.configs:
+            if name == args.workload:
+                continue
+            steps, warmup, plain, e2e, par = SUB_CONFIGS[name]
+            sub_wl = getattr(procedural, name)()
+            res, _ = measure(pkg, procedural, name, sub_wl, steps, warmup, plain, e2e, par,
+                             autotune=not args.no_autotune)
+            res["config"] = workload_config(name, sub_wl)
+            if not args.no_cpu_baseline:
+                threads = os.cpu_count() or 1
+                fps, n_cpu, dt = cpu_frames_per_s(procedural, sub_wl, 4.0, threads)
+                res["cpu_baseline"] = {"value": fps, "unit": "frames/s", "cores": threads,
+                                       "cpu_model": cpu_model(), "kind": "port",
+                                       "sample": f"first {n_cpu} of {sub_wl.envs} envs, one step, {dt:.2f} s"}
+            configs[name] = res
+            del sub_wl
+    serving = None if args.no_serving else serving_leg(pkg, args)
 
     cpu_baseline = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         fps, n, dt = cpu_frames_per_s(procedural, wl, args.cpu_seconds, threads)
-        cpu_baseline = {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
-                        "sample": f"first {n} of {wl.envs} envs, one step, {dt:.2f} s"}
+        cpu_baseline = {"value": fps, "unit": "frames/s", "cores": threads, "cpu_model": cpu_model(),
+                        "kind": "port", "sample": f"first {n} of {wl.envs} envs, one step, {dt:.2f} s"}
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": statistics.mean(step_ms),
-            "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
+            "metric": METRIC, "value": main_res["value"], "unit": "frames/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": main_res["ms_per_step"],
+            "p50_ms": main_res["p50_ms"], "p99_ms": main_res["p99_ms"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOADS[args.workload], "envs": wl.envs,
-                       "resolution": sorted({w for (w, _) in wl.viewports}),
-                       "planes": "rgba8 + f32 linear depth + u32 semantic id",
-                       "form": "batched: prepare + persistent raster per step, CUDA graph",
-                       "l2": "flushed with a 256 MiB write before every step (outside timing)",
-                       "triangles_per_step_after_draw_culling": tri,
-                       "triangles_per_step_before_culling": int(wl.triangles_per_env().sum()),
-                       "tuning": r.tuning(),
-                       "autotune": None if args.no_autotune else {
-                           "cached": tune_report["cached"],
-                           "candidates": len(tune_report.get("trials", []))}},
-            "plain": None if not plain_ms else {
-                "value": plain_fps, "unit": "frames/s", "ms_per_step": statistics.mean(plain_ms),
-                "p50_ms": float(np.percentile(plain_ms, 50)),
-                "p99_ms": float(np.percentile(plain_ms, 99)),
-                "form": "per-scene prepare + raster launches (2 per env), no graph"},
-            "batched_over_plain": value / plain_fps if plain_fps else None,
-            "e2e": None if not e2e_s else {
-                "value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * statistics.mean(e2e_s),
-                "timing": ("host clock over the steps: updateCameras + draw + 3 imageIntoAsync "
-                           "readbacks per step, readback of step k overlapping the draw of "
-                           "step k+1, then readbackWait")},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "peak_source": peak_src, "kernel": "raster_kernel",
-                         "bytes_per_launch": launch_bytes,
-                         "bytes_breakdown": {"framebuffer": fb_bytes, "geometry_textures": geo_bytes},
-                         "avg_launch_ms": raster_avg_ms,
-                         "prepare_avg_ms": statistics.mean(prepare_ms)},
-            "gpu_launches": 2 * args.steps,
-            "clocks": clocks,
-            "parity": parity,
+            "config": workload_config(args.workload, wl),
+            "details": {"form": "batched: prepare + persistent raster per step, CUDA graph",
+                        "l2": "flushed with a 256 MiB write before every step (outside timing)",
+                        "triangles_per_step_before_culling": main_res["triangles_per_step_before_culling"],
+                        "tuning": main_res["tuning"], "autotune": main_res["autotune"]},
+            "plain": main_res["plain"],
+            "batched_over_plain": main_res["batched_over_plain"],
+            "e2e": main_res["e2e"],
+            "roofline": main_res["roofline"],
+            "gpu_launches": main_res["gpu_launches"],
+            "clocks": main_res["clocks"],
+            "parity": main_res["parity"],
             "cpu_baseline": cpu_baseline,
+            "configs": configs,
             "serving": serving,
             "replay": replay,
             "postprocess": post,
         }
         print(json.dumps(line))
-    r.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0

@@ -160,12 +160,37 @@ def test_config3_scan_subset(pkg, procedural):
     _parity(pkg, procedural, wl, steps=(0, 1, 7))
 
 
-def test_config3_full_density_scene(pkg, procedural):
-    """One 5M-triangle scan room at full density: 16 walking envs in one
-    batched step equal the per-scene path and the same step with occlusion
-    culling off; two envs equal the oracle."""
+def test_config2_full_scale_sample(pkg, procedural):
+    """The full uneven-batching workload (4096 envs, 64 scenes of 20k-2M
+    triangles, mixed 64/128/256 px, hfov U(60, 110)): 16 envs spanning the
+    three resolution classes -- the envs of the largest scenes first -- equal
+    the oracle, rendered in one batched step with the other envs of their
+    ragged framebuffer."""
     from oracle.model import OracleRenderer
-    wl = procedural.config3(envs=16, scenes=1)
+    wl = procedural.config2()
+    tri = wl.triangles_per_env()
+    sample = []
+    for c, k in ((64, 5), (128, 6), (256, 5)):
+        envs = sorted((e for e in range(wl.envs) if wl.viewports[e][0] == c), key=lambda e: -int(tri[e]))
+        sample += envs[:k - 2] + envs[-2:]
+    sample = sorted(sample)
+    assert max(int(tri[e]) for e in sample) == int(tri.max()) > 1e6   # the largest scene is in
+    gpu = procedural.build_renderer(pkg, wl, mode=1, envs=sample)
+    cpu = procedural.build_oracle(OracleRenderer, wl, envs=sample)
+    poses = procedural.camera_poses(wl, 5)
+    procedural.set_cameras(gpu, wl, poses, sample)
+    procedural.set_cameras(cpu, wl, poses, sample)
+    cpu.draw(threads=8)
+    gpu.draw(mode=1, graph=True)
+    assert_parity([compare_scene(gpu, cpu, pkg, k) for k in range(len(sample))])
+
+
+def test_config3_full_density_scene(pkg, procedural):
+    """Two 5M-triangle scan rooms at full density: 16 walking envs in one
+    batched step equal the per-scene path and the same step with occlusion
+    culling off; eight envs (four per room) equal the oracle."""
+    from oracle.model import OracleRenderer
+    wl = procedural.config3(envs=16, scenes=2)
     gpu = procedural.build_renderer(pkg, wl, mode=1)
     poses = procedural.camera_poses(wl, 3)
     procedural.set_cameras(gpu, wl, poses)
@@ -179,7 +204,7 @@ def test_config3_full_density_scene(pkg, procedural):
     gpu.draw(mode=1)
     assert all(np.array_equal(a.view(np.uint8), gpu.sceneImage(p, s).view(np.uint8))
                for a, (s, p) in zip(ref, [(s, p) for s in range(16) for p in planes]))
-    sample = [0, 9]
+    sample = [0, 1, 4, 7, 9, 10, 13, 14]
     cpu = procedural.build_oracle(OracleRenderer, wl, envs=sample)
     procedural.set_cameras(cpu, wl, poses, sample)
     cpu.draw(threads=8)
