@@ -554,6 +554,13 @@ def postprocess_leg(pkg, r, wl, stream, reps=10):
 
     noise_ms = timed(lambda: m.apply_to_renderer(r, dst, stream.cuda_stream))
     hbao_ms = timed(lambda: r.drawHbao(stream=stream))
+    variants = {}
+    for name, cfg in (("cache_aware", pkg.HbaoConfiguration().setAlgorithm(pkg.HbaoType.CacheAware)),
+                      ("special_blur", pkg.HbaoConfiguration().setUseSpecialBlur(True)),
+                      ("cache_aware_special_blur",
+                       pkg.HbaoConfiguration().setAlgorithm(pkg.HbaoType.CacheAware).setUseSpecialBlur(True))):
+        ms = timed(lambda: r.drawHbao(cfg, stream=stream))
+        variants[name] = {"ms": ms, "Gpx_per_s": px / ms / 1e6}
     m.close()
     return {"pixels": px,
             "redwood_noise": {"ms": noise_ms, "Gpx_per_s": px / noise_ms / 1e6,
@@ -563,7 +570,8 @@ def postprocess_leg(pkg, r, wl, stream, reps=10):
                      "GB_per_s": 24 * px / hbao_ms / 1e6, "bytes_per_pixel": 24, "launches": 3,
                      "note": "bytes: depth read by each of the 3 passes, 8-bit AO written and "
                              "read twice, colour read and written; the AO pass's 36 neighbour "
-                             "depth reads per pixel are served by L1/L2"}}
+                             "depth reads per pixel are served by L1/L2",
+                     "variants": variants}}
 
 
 def replay_leg(pkg, procedural, wl, tuning, steps=5, warmup=2):

@@ -66,7 +66,8 @@ class DrawStats(ctypes.Structure):
 class HbaoConfig(ctypes.Structure):
     _fields_ = [("intensity", ctypes.c_float), ("bias", ctypes.c_float),
                 ("radius", ctypes.c_float), ("blur_sharpness", ctypes.c_float),
-                ("no_blur", ctypes.c_int32), ("special_blur", ctypes.c_int32)]
+                ("no_blur", ctypes.c_int32), ("special_blur", ctypes.c_int32),
+                ("algorithm", ctypes.c_int32)]
 
 
 class ReplayConfig(ctypes.Structure):

@@ -24,6 +24,8 @@
 // driver; this fixes it.
 #include "hbao.h"
 
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -140,9 +142,50 @@ __device__ __forceinline__ int scene_of_block(const HbaoScene* scenes, int count
   return s_si;
 }
 
+__device__ __forceinline__ float3 reconstruct_normal(const HbaoScene& s, const float* __restrict__ depth, int x, int y,
+                                                     float u, float v, float inv_w, float inv_h, float3 P,
+                                                     float& inv_len) {
+  const float3 pr = view_pos(s, __fadd_rn(u, inv_w), v, depth_at(s, depth, x + 1, y));
+  const float3 pl = view_pos(s, __fadd_rn(u, -inv_w), v, depth_at(s, depth, x - 1, y));
+  const float3 pt = view_pos(s, u, __fadd_rn(v, inv_h), depth_at(s, depth, x, y + 1));
+  const float3 pb = view_pos(s, u, __fadd_rn(v, -inv_h), depth_at(s, depth, x, y - 1));
+  const float3 c = cross3(min_diff(P, pr, pl), min_diff(P, pt, pb));
+  inv_len = __fdiv_rn(1.0f, __fsqrt_rn(dot3(c, c)));
+  return c;
+}
+
+// Depth of the cache-aware sample: texel (tqx, tqy) of deinterleaved layer
+// (ox, oy), i.e. full-resolution pixel (4 tqx + ox, 4 tqy + oy); texels of
+// the quarter-resolution layer that fall beyond the image read as the far plane.
+__device__ __forceinline__ float layer_depth(const HbaoScene& s, const float* __restrict__ depth, int tqx, int tqy,
+                                             int ox, int oy) {
+  tqx = min(max(tqx, 0), s.qw - 1);
+  tqy = min(max(tqy, 0), s.qh - 1);
+  const int fx = 4 * tqx + ox, fy = 4 * tqy + oy;
+  if (fx >= s.w || fy >= s.h) return s.far_plane;
+  const float z = __ldg(depth + s.offset + (long long)fy * s.pitch + fx);
+  return z == 0.0f ? s.far_plane : z;
+}
+
+__device__ __forceinline__ uint32_t pack_half2(float a, float b) {
+  return uint32_t(__half_as_ushort(__float2half_rn(a))) | (uint32_t(__half_as_ushort(__float2half_rn(b))) << 16);
+}
+__device__ __forceinline__ float half_lo(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v & 0xFFFFu))); }
+__device__ __forceinline__ float half_hi(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v >> 16))); }
+
+// AO per pixel.  Classic: the pixel's own view position and reconstructed
+// normal, samples at full resolution, the 16-bit jitter of texel
+// (x & 3, y & 3).  CacheAware: the pixel belongs to deinterleaved layer
+// (x & 3, y & 3) at quarter-resolution texel (x >> 2, y >> 2); its uv is that
+// texel's centre in the layer, its normal the reconstructed one through an
+// RGBA8 store, its samples are texels of the same layer at quarter-resolution
+// steps (radius / 4), its jitter the layer's unquantized one; the result
+// lands at the pixel, which is the reinterleave.  Special: (AO, view depth)
+// stored as two halves.
+template <bool CacheAware, bool Special>
 __global__ void __launch_bounds__(256) hbao_ao_kernel(const HbaoScene* __restrict__ scenes, int count,
                                                       const float* __restrict__ depth, uint32_t* color,
-                                                      uint8_t* q1, const HbaoParams p) {
+                                                      void* q1, const HbaoParams p) {
   {
     const HbaoScene s = scenes[scene_of_block(scenes, count)];
     const int pixels = s.w * s.h;
@@ -150,19 +193,38 @@ __global__ void __launch_bounds__(256) hbao_ao_kernel(const HbaoScene* __restric
     const int idx = (int(blockIdx.x) - s.block0) * 256 + int(threadIdx.x);
     if (idx < pixels) {
       const int x = idx % s.w, y = idx / s.w;
-      const float u = __fdiv_rn(__fadd_rn(float(x), 0.5f), float(s.w));
-      const float v = __fdiv_rn(__fadd_rn(float(y), 0.5f), float(s.h));
-      const float3 P = view_pos(s, u, v, depth_at(s, depth, x, y));
-      const float3 pr = view_pos(s, __fadd_rn(u, inv_w), v, depth_at(s, depth, x + 1, y));
-      const float3 pl = view_pos(s, __fadd_rn(u, -inv_w), v, depth_at(s, depth, x - 1, y));
-      const float3 pt = view_pos(s, u, __fadd_rn(v, inv_h), depth_at(s, depth, x, y + 1));
-      const float3 pb = view_pos(s, u, __fadd_rn(v, -inv_h), depth_at(s, depth, x, y - 1));
-      const float3 c = cross3(min_diff(P, pr, pl), min_diff(P, pt, pb));
-      const float inv_len = __fdiv_rn(1.0f, __fsqrt_rn(dot3(c, c)));
-      const float3 N = f3(-__fmul_rn(c.x, inv_len), -__fmul_rn(c.y, inv_len), -__fmul_rn(c.z, inv_len));
-      const float radius = __fdiv_rn(s.radius_to_screen, s.ortho ? 1.0f : P.z);
+      float u = __fdiv_rn(__fadd_rn(float(x), 0.5f), float(s.w));
+      float v = __fdiv_rn(__fadd_rn(float(y), 0.5f), float(s.h));
+      float3 P = view_pos(s, u, v, depth_at(s, depth, x, y));
+      float inv_len;
+      const float3 c = reconstruct_normal(s, depth, x, y, u, v, inv_w, inv_h, P, inv_len);
+      float3 N;
+      float radius;
+      const float* j;
+      float su_scale = inv_w, sv_scale = inv_h;
+      const int ox = x & 3, oy = y & 3, qx = x >> 2, qy = y >> 2;
+      if (!CacheAware) {
+        N = f3(-__fmul_rn(c.x, inv_len), -__fmul_rn(c.y, inv_len), -__fmul_rn(c.z, inv_len));
+        radius = __fdiv_rn(s.radius_to_screen, s.ortho ? 1.0f : P.z);
+        j = p.jitter + 4 * ((y & 3) * 4 + (x & 3));
+      } else {
+        const float e[3] = {c.x, c.y, c.z};
+        float n[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float enc = float(unorm8(__fadd_rn(__fmul_rn(__fmul_rn(e[k], inv_len), 0.5f), 0.5f)));
+          n[k] = -__fsub_rn(__fmul_rn(__fdiv_rn(enc, 255.0f), 2.0f), 1.0f);
+        }
+        N = f3(n[0], n[1], n[2]);
+        u = __fmul_rn(__fadd_rn(__fmul_rn(float(qx), 4.0f), __fadd_rn(float(ox), 0.5f)), __fdiv_rn(s.inv_qw, 4.0f));
+        v = __fmul_rn(__fadd_rn(__fmul_rn(float(qy), 4.0f), __fadd_rn(float(oy), 0.5f)), __fdiv_rn(s.inv_qh, 4.0f));
+        P = view_pos(s, u, v, P.z);
+        radius = __fdiv_rn(__fdiv_rn(s.radius_to_screen, s.ortho ? 1.0f : P.z), 4.0f);
+        j = p.jitter_f + 4 * (oy * 4 + ox);
+        su_scale = s.inv_qw;
+        sv_scale = s.inv_qh;
+      }
       const float step = __fdiv_rn(radius, 5.0f);
-      const float* j = p.jitter + 4 * ((y & 3) * 4 + (x & 3));
       float ao = 0.0f;
 #pragma unroll
       for (int d = 0; d < 8; ++d) {
@@ -173,10 +235,12 @@ __global__ void __launch_bounds__(256) hbao_ao_kernel(const HbaoScene* __restric
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const float kx = rintf(__fmul_rn(ray, dx)), ky = rintf(__fmul_rn(ray, dy));
-          const float su = __fadd_rn(__fmul_rn(kx, inv_w), u), sv = __fadd_rn(__fmul_rn(ky, inv_h), v);
+          const float su = __fadd_rn(__fmul_rn(kx, su_scale), u), sv = __fadd_rn(__fmul_rn(ky, sv_scale), v);
           // Offsets beyond the image only select the clamped edge texel.
-          const int ox = int(fminf(fmaxf(kx, -65536.0f), 65536.0f)), oy = int(fminf(fmaxf(ky, -65536.0f), 65536.0f));
-          const float3 S = view_pos(s, su, sv, depth_at(s, depth, x + ox, y + oy));
+          const int ix = int(fminf(fmaxf(kx, -65536.0f), 65536.0f)), iy = int(fminf(fmaxf(ky, -65536.0f), 65536.0f));
+          const float zs = CacheAware ? layer_depth(s, depth, qx + ix, qy + iy, ox, oy)
+                                      : depth_at(s, depth, x + ix, y + iy);
+          const float3 S = view_pos(s, su, sv, zs);
           ray = __fadd_rn(ray, step);
           const float3 V = sub(S, P);
           const float vv = dot3(V, V);
@@ -188,21 +252,29 @@ __global__ void __launch_bounds__(256) hbao_ao_kernel(const HbaoScene* __restric
       ao = __fmul_rn(ao, __fdiv_rn(p.ao_mult, 32.0f));
       const float occl = poly_pow(clamp01(__fsub_rn(1.0f, __fmul_rn(ao, 2.0f))), p.pow_exp);
       const long long at = s.offset + (long long)y * s.pitch + x;
-      if (p.no_blur)
-        color[at] = modulate(color[at], occl);
-      else
-        q1[at] = unorm8(occl);
+      if (p.no_blur) {
+        // The cache-aware result reaches the colour through its 8-bit layers.
+        color[at] = modulate(color[at], CacheAware ? __fdiv_rn(float(unorm8(occl)), 255.0f) : occl);
+      } else if (Special) {
+        static_cast<uint32_t*>(q1)[at] = pack_half2(occl, P.z);
+      } else {
+        static_cast<uint8_t*>(q1)[at] = unorm8(occl);
+      }
     }
   }
 }
 
-// One 7-tap pass along x (axis 0) or y (axis 1).
-template <int Axis>
+// One 7-tap pass along x (axis 0) or y (axis 1).  Bilateral: 8-bit AO, the
+// depths from the linear-depth plane.  Special: (AO, depth) halves, the
+// first pass storing (blurred AO, centre depth) as halves again.
+template <int Axis, bool Special>
 __global__ void __launch_bounds__(256) hbao_blur_kernel(const HbaoScene* __restrict__ scenes, int count,
                                                         const float* __restrict__ depth,
-                                                        const uint8_t* __restrict__ src, uint8_t* dst,
+                                                        const void* __restrict__ src_v, void* dst_v,
                                                         uint32_t* color, const HbaoParams p) {
   const float falloff = 1.0f / (2.0f * 1.5f * 1.5f);
+  const uint8_t* src8 = static_cast<const uint8_t*>(src_v);
+  const uint32_t* src32 = static_cast<const uint32_t*>(src_v);
   {
     const HbaoScene s = scenes[scene_of_block(scenes, count)];
     const int pixels = s.w * s.h;
@@ -210,8 +282,16 @@ __global__ void __launch_bounds__(256) hbao_blur_kernel(const HbaoScene* __restr
     if (idx < pixels) {
       const int x = idx % s.w, y = idx / s.w;
       const long long at = s.offset + (long long)y * s.pitch + x;
-      const float cd = depth_at(s, depth, x, y);
-      float ct = __fdiv_rn(float(src[at]), 255.0f), wt = 1.0f;
+      float cd, ct;
+      if (Special) {
+        const uint32_t c0 = src32[at];
+        ct = half_lo(c0);
+        cd = half_hi(c0);
+      } else {
+        cd = depth_at(s, depth, x, y);
+        ct = __fdiv_rn(float(src8[at]), 255.0f);
+      }
+      float wt = 1.0f;
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
 #pragma unroll
@@ -219,8 +299,17 @@ __global__ void __launch_bounds__(256) hbao_blur_kernel(const HbaoScene* __restr
           const int o = side == 0 ? r : -r;
           const int tx = Axis == 0 ? min(max(x + o, 0), s.w - 1) : x;
           const int ty = Axis == 1 ? min(max(y + o, 0), s.h - 1) : y;
-          const float c = __fdiv_rn(float(src[s.offset + (long long)ty * s.pitch + tx]), 255.0f);
-          const float dd = __fmul_rn(__fsub_rn(depth_at(s, depth, tx, ty), cd), p.sharpness);
+          const long long t_at = s.offset + (long long)ty * s.pitch + tx;
+          float c, dz;
+          if (Special) {
+            const uint32_t t = src32[t_at];
+            c = half_lo(t);
+            dz = half_hi(t);
+          } else {
+            c = __fdiv_rn(float(src8[t_at]), 255.0f);
+            dz = depth_at(s, depth, tx, ty);
+          }
+          const float dd = __fmul_rn(__fsub_rn(dz, cd), p.sharpness);
           const float rf = float(r);
           const float w = poly_exp2(__fsub_rn(__fmul_rn(__fmul_rn(-rf, rf), falloff), __fmul_rn(dd, dd)));
           wt = __fadd_rn(wt, w);
@@ -228,19 +317,52 @@ __global__ void __launch_bounds__(256) hbao_blur_kernel(const HbaoScene* __restr
         }
       }
       const float out = __fdiv_rn(ct, wt);
-      if (Axis == 0)
-        dst[at] = unorm8(out);
-      else
+      if (Axis == 0) {
+        if (Special)
+          static_cast<uint32_t*>(dst_v)[at] = pack_half2(out, cd);
+        else
+          static_cast<uint8_t*>(dst_v)[at] = unorm8(out);
+      } else {
         color[at] = modulate(color[at], out);
+      }
     }
+  }
+}
+
+template <bool CacheAware, bool Special>
+void hbao_launch_t(const HbaoScene* d_scenes, int count, const dim3& grid, const float* depth, uint32_t* color,
+                   void* q1, void* q2, const HbaoParams& p, cudaStream_t stream) {
+  hbao_ao_kernel<CacheAware, Special><<<grid, 256, 0, stream>>>(d_scenes, count, depth, color, q1, p);
+  if (!p.no_blur) {
+    hbao_blur_kernel<0, Special><<<grid, 256, 0, stream>>>(d_scenes, count, depth, q1, q2, color, p);
+    hbao_blur_kernel<1, Special><<<grid, 256, 0, stream>>>(d_scenes, count, depth, q2, nullptr, color, p);
   }
 }
 
 }  // namespace
 
+// The jitter table before its 16-bit storage: the values the cache-aware
+// algorithm passes per layer as a uniform (Hbao.cpp:603-617, 1000).
+void hbao_jitter_unquantized(float out[64]) {
+  std::mt19937 rmt;  // default seed, as the reference
+  for (int i = 0; i < 16; ++i) {
+    const float r1 = float(rmt()) / 4294967296.0f;
+    const float r2 = float(rmt()) / 4294967296.0f;
+    const float angle = 6.28318530718f * r1 / 8.0f;
+    out[4 * i + 0] = float(std::cos(double(angle)));
+    out[4 * i + 1] = float(std::sin(double(angle)));
+    out[4 * i + 2] = r2;
+    out[4 * i + 3] = 0.0f;
+  }
+}
+
 bool hbao_params(const gbr_hbao_config& c, HbaoParams& p, std::string& err) {
-  if (c.special_blur) {
-    err = "Hbao: the special blur variant is not available";
+  if (c.special_blur && c.no_blur) {
+    err = "Hbao: no_blur and special_blur exclude each other (HbaoConfiguration::setNoBlur / setUseSpecialBlur)";
+    return false;
+  }
+  if (c.algorithm != GBR_HBAO_CLASSIC && c.algorithm != GBR_HBAO_CACHE_AWARE) {
+    err = "Hbao: unknown algorithm";
     return false;
   }
   if (!std::isfinite(c.radius) || !(c.radius > 0.0f) || !std::isfinite(c.intensity) ||
@@ -257,7 +379,10 @@ bool hbao_params(const gbr_hbao_config& c, HbaoParams& p, std::string& err) {
   p.ao_mult = 1.0f / (1.0f - p.bias);
   p.sharpness = c.blur_sharpness / 1.0f;
   p.no_blur = c.no_blur ? 1 : 0;
+  p.special = c.special_blur ? 1 : 0;
+  p.cache_aware = c.algorithm == GBR_HBAO_CACHE_AWARE ? 1 : 0;
   gbr_hbao_jitter_table(p.jitter);
+  hbao_jitter_unquantized(p.jitter_f);
   for (int d = 0; d < 8; ++d) {
     const float a = 2.0f * 3.14159265f / 8.0f * float(d);
     p.dirs[2 * d] = float(std::cos(double(a)));
@@ -272,6 +397,10 @@ HbaoScene hbao_scene(const float* m, int w, int h, long long offset, long long p
   s.pitch = pitch;
   s.w = w;
   s.h = h;
+  s.qw = (w + 3) / 4;
+  s.qh = (h + 3) / 4;
+  s.inv_qw = 1.0f / float(s.qw);
+  s.inv_qh = 1.0f / float(s.qh);
   const float p00 = m[0], p11 = m[5], p20 = m[8], p21 = m[9], p22 = m[10], p30 = m[12], p31 = m[13],
               p32 = m[14];
   s.ortho = m[15] != 0.0f ? 1 : 0;
@@ -292,13 +421,19 @@ HbaoScene hbao_scene(const float* m, int w, int h, long long offset, long long p
 }
 
 cudaError_t hbao_launch(const HbaoScene* d_scenes, int count, int blocks, const float* depth,
-                        uint32_t* color, uint8_t* q1, uint8_t* q2, const HbaoParams& p, cudaStream_t stream) {
+                        uint32_t* color, void* q1, void* q2, const HbaoParams& p, cudaStream_t stream) {
   if (count <= 0 || blocks <= 0) return cudaSuccess;
   const dim3 grid(blocks);
-  hbao_ao_kernel<<<grid, 256, 0, stream>>>(d_scenes, count, depth, color, q1, p);
-  if (!p.no_blur) {
-    hbao_blur_kernel<0><<<grid, 256, 0, stream>>>(d_scenes, count, depth, q1, q2, color, p);
-    hbao_blur_kernel<1><<<grid, 256, 0, stream>>>(d_scenes, count, depth, q2, nullptr, color, p);
+  if (p.cache_aware) {
+    if (p.special)
+      hbao_launch_t<true, true>(d_scenes, count, grid, depth, color, q1, q2, p, stream);
+    else
+      hbao_launch_t<true, false>(d_scenes, count, grid, depth, color, q1, q2, p, stream);
+  } else {
+    if (p.special)
+      hbao_launch_t<false, true>(d_scenes, count, grid, depth, color, q1, q2, p, stream);
+    else
+      hbao_launch_t<false, false>(d_scenes, count, grid, depth, color, q1, q2, p, stream);
   }
   return cudaGetLastError();
 }
@@ -356,7 +491,7 @@ gbr_status gbr_hbao_apply(const gbr_hbao_config* config, const float projection[
   const cudaStream_t st = static_cast<cudaStream_t>(stream);
   gbr::HbaoScene* d_scene = nullptr;
   uint8_t* q = nullptr;
-  const size_t plane = size_t(pitch) * size_t(h);
+  const size_t plane = size_t(pitch) * size_t(h) * size_t(gbr::hbao_plane_bytes(p));
   cudaError_t e = cudaMalloc(&d_scene, sizeof s);
   if (!e) e = cudaMalloc(&q, 2 * plane);
   if (!e) e = cudaMemcpyAsync(d_scene, &s, sizeof s, cudaMemcpyHostToDevice, st);

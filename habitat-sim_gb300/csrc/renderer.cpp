@@ -1531,7 +1531,7 @@ gbr_status Renderer::hbao(const gbr_hbao_config& c, cudaStream_t stream) {
   if (blocks > 0x7fffffffLL) return fail(GBR_ERROR_INVALID_ARGUMENT, "Hbao: too many pixels in one call");
   if (recs.empty()) return GBR_OK;
   cudaSetDevice(device_);
-  const size_t fb = size_t(fb_w_) * size_t(fb_h_);
+  const size_t fb = size_t(fb_w_) * size_t(fb_h_) * size_t(hbao_plane_bytes(params));
   if (!d_hbao_scenes_.reserve(recs.size() * sizeof(HbaoScene), false) || !d_hbao_ao_.reserve(2 * fb, false))
     return fail(GBR_ERROR_OUT_OF_MEMORY, "Hbao: device allocation failed");
   if (upload_pending_[slot_])  // after the last draw, whatever stream it ran on

@@ -135,9 +135,16 @@ class RendererStandaloneConfiguration:
         return self
 
 
+class HbaoType(enum.IntEnum):
+    """``HbaoType`` (src/esp/gfx_batch/Hbao.h:135)."""
+    Classic = 0
+    CacheAware = 1
+
+
 class HbaoConfiguration:
     """``HbaoConfiguration`` (src/esp/gfx_batch/Hbao.h:30-141): intensity,
-    bias, radius (metres), blur sharpness, NoBlur; the classic algorithm."""
+    bias, radius (metres), blur sharpness, NoBlur, UseAoSpecialBlur; and the
+    algorithm ``drawEffect`` takes (``HbaoType``)."""
 
     def __init__(self):
         self.intensity = 0.732
@@ -146,6 +153,11 @@ class HbaoConfiguration:
         self.blur_sharpness = 10.0
         self.no_blur = False
         self.special_blur = False
+        self.algorithm = HbaoType.Classic
+
+    def setAlgorithm(self, algorithm):
+        self.algorithm = HbaoType(algorithm)
+        return self
 
     def setNoBlur(self, state):
         self.no_blur = bool(state)
@@ -196,6 +208,7 @@ class HbaoConfiguration:
         c.intensity, c.bias, c.radius = self.intensity, self.bias, self.radius
         c.blur_sharpness = self.blur_sharpness
         c.no_blur, c.special_blur = int(self.no_blur), int(self.special_blur)
+        c.algorithm = int(self.algorithm)
         return c
 
 
@@ -715,11 +728,14 @@ class RendererStandalone:
     def colorTensor(self):
         return self.deviceTensor(Plane.Color)
 
-    def drawHbao(self, configuration=None, stream=None):
-        """``Hbao::drawEffect`` (classic) on every enabled scene of the last
-        draw: colour darkened in place from linear depth and each scene's
-        projection; asynchronous on `stream`."""
+    def drawHbao(self, configuration=None, stream=None, algorithm=None):
+        """``Hbao::drawEffect`` on every enabled scene of the last draw:
+        colour darkened in place from linear depth and each scene's
+        projection; ``algorithm`` (``HbaoType``) overrides the
+        configuration's; asynchronous on `stream`."""
         c = (configuration or HbaoConfiguration())._c()
+        if algorithm is not None:
+            c.algorithm = int(HbaoType(algorithm))
         check(self._lib.gbr_hbao_draw(self._h, ctypes.byref(c), _stream_handle(stream)))
 
     def depthTensor(self):

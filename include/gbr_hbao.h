@@ -1,14 +1,17 @@
 /* gbr_hbao.h -- C ABI of horizon-based ambient occlusion on the GPU.
  *
- * A drop-in for habitat-sim's esp::gfx_batch::Hbao, classic algorithm
- * (src/esp/gfx_batch/Hbao.h:30-190, Hbao.cpp:595-935, shaders
- * src/shaders/gfx_batch/hbao/{hbao,bilateralblur}.frag): per pixel, the view
- * position from linear depth, a normal from the nearest neighbours, 8
- * jittered directions x 4 steps of occlusion within a world-space radius,
- * stored as 8-bit AO, a depth-aware 7-tap blur along x then y, and the
- * colour multiplied by the result.  The GL version draws on the classic
- * renderer's render target; here it runs as three kernels over every scene
- * of a batch renderer (or on one caller image).  Conventions as gbr.h.
+ * A drop-in for habitat-sim's esp::gfx_batch::Hbao (src/esp/gfx_batch/
+ * Hbao.h:30-190, Hbao.cpp:595-1038, shaders src/shaders/gfx_batch/hbao/):
+ * per pixel, the view position from linear depth, a normal from the nearest
+ * neighbours, 8 jittered directions x 4 steps of occlusion within a
+ * world-space radius, stored as 8-bit AO, a depth-aware 7-tap blur along x
+ * then y, and the colour multiplied by the result.  HbaoType::CacheAware
+ * computes the same on 16 deinterleaved quarter-resolution layers of the
+ * depth (normals through an RGBA8 store, per-layer jitter); the special blur
+ * (HbaoFlag::UseAoSpecialBlur) keeps AO and view depth as two halves and
+ * blurs with that depth.  The GL version draws on the classic renderer's
+ * render target; here it runs as three kernels over every scene of a batch
+ * renderer (or on one caller image).  Conventions as gbr.h.
  */
 #ifndef GBR_HBAO_H
 #define GBR_HBAO_H
@@ -19,20 +22,25 @@
 extern "C" {
 #endif
 
-/* HbaoConfiguration (Hbao.h:30-141). */
+/* HbaoType (Hbao.h:135). */
+#define GBR_HBAO_CLASSIC 0
+#define GBR_HBAO_CACHE_AWARE 1
+
+/* HbaoConfiguration (Hbao.h:30-141) and the algorithm of drawEffect. */
 typedef struct gbr_hbao_config {
   float intensity;      /* power exponent, default 0.732                    */
   float bias;           /* N.V bias, default 0.05                           */
   float radius;         /* metres, default 1.84                             */
   float blur_sharpness; /* default 10                                       */
   int32_t no_blur;      /* HbaoFlag::NoBlur: raw AO multiplied in           */
-  int32_t special_blur; /* HbaoFlag::UseAoSpecialBlur: must be 0            */
+  int32_t special_blur; /* HbaoFlag::UseAoSpecialBlur (not with no_blur)    */
+  int32_t algorithm;    /* GBR_HBAO_CLASSIC (default) or GBR_HBAO_CACHE_AWARE */
 } gbr_hbao_config;
 
 void gbr_hbao_config_init(gbr_hbao_config* config);
 
-/* Hbao::drawEffect(projection, HbaoType::Classic, depth, output)
- * (Hbao.cpp:874-935) on every enabled scene of the renderer's last draw:
+/* Hbao::drawEffect(projection, algorithm, depth, output)
+ * (Hbao.cpp:874-1038) on every enabled scene of the renderer's last draw:
  * each scene's colour plane is darkened in place using its linear depth and
  * the projection of its last updateCamera.  Needs the colour and
  * linear-depth planes; asynchronous on stream (ordered after the draw). */

@@ -1,8 +1,9 @@
 """Ambient occlusion without a GPU: the jitter table (the library's host
 function against the oracle's Mersenne-twister rebuild), the polynomial
 exp2/log2 the effect is defined with, the oracle's behaviour on scenes with
-known answers (an open plane is not occluded, a corner is), and the C ABI's
-argument checks (include/gbr_hbao.h)."""
+known answers (an open plane is not occluded, a corner is) for the classic
+and cache-aware algorithms with either blur, and the C ABI's argument checks
+(include/gbr_hbao.h)."""
 import ctypes
 
 import numpy as np
@@ -87,10 +88,42 @@ def test_hbao_c_abi_checks(lib, pkg):
     fp = p.ctypes.data_as(_lib.c_float_p)
     assert lib.gbr_hbao_apply(None, fp, 1, 1, 8, 8, 8, None) == 1
     assert lib.gbr_hbao_apply(ctypes.byref(c), fp, 1, 1, 8, 8, 4, None) == 1      # pitch < width
-    c.special_blur = 1
+    c.special_blur = c.no_blur = 1              # the two flags exclude each other
     assert lib.gbr_hbao_apply(ctypes.byref(c), fp, 1, 1, 8, 8, 8, None) == 1
-    assert b"special blur" in lib.gbr_last_error()
-    c.special_blur = 0
+    assert b"exclude each other" in lib.gbr_last_error()
+    c.special_blur = c.no_blur = 0
+    c.algorithm = 7
+    assert lib.gbr_hbao_apply(ctypes.byref(c), fp, 1, 1, 8, 8, 8, None) == 1
+    assert b"algorithm" in lib.gbr_last_error()
+    c.algorithm = 0
     c.radius = -1.0
     assert lib.gbr_hbao_apply(ctypes.byref(c), fp, 1, 1, 8, 8, 8, None) == 1
     assert lib.gbr_hbao_draw(None, ctypes.byref(c), None) == 1
+
+
+def test_unquantized_jitter_rounds_to_the_table():
+    f = H.jitter_table(quantized=False)
+    q = H.jitter_table()
+    assert np.abs(f[:, :3] - q[:, :3]).max() <= 0.5 / 32767 + 1e-7
+    assert not np.array_equal(f, q)
+
+
+@pytest.mark.parametrize("cache_aware", [False, True], ids=["classic", "cache_aware"])
+@pytest.mark.parametrize("blur", ["bilateral", "special", "none"])
+def test_variants_on_known_scenes(cache_aware, blur):
+    """Every algorithm and blur: an open plane stays lit, a corner darkens."""
+    proj = S.perspective(90.0, 1.0, 0.01, 10.0)
+    h, w = 48, 52     # a width that is not a multiple of 4 (quarter-resolution edge)
+    cfg = H.config(no_blur=blur == "none", special_blur=blur == "special", cache_aware=cache_aware)
+    color = np.full((h, w, 4), 200, np.uint8)
+    flat = H.hbao(color, np.full((h, w), 3.0, np.float32), proj, cfg)
+    assert (flat[..., :3] >= 196).all() and (flat[..., 3] == 200).all()
+    depth = np.full((h, w), 3.0, np.float32)
+    xs = np.arange(w)
+    depth[:, xs >= w // 2] = (3.0 - 0.12 * (xs[xs >= w // 2] - w // 2)).astype(np.float32)
+    out = H.hbao(color, depth, proj, cfg)
+    assert out[:, w // 2 - 2:w // 2 + 2, 0].mean() < flat[:, w // 2, 0].mean() - 5
+    classic = H.hbao(color, depth, proj, H.config(no_blur=blur == "none"))
+    if cache_aware or blur == "special":
+        assert not np.array_equal(out, classic)
+        assert np.abs(out.astype(int) - classic.astype(int)).mean() < 8   # the same effect
