@@ -446,8 +446,11 @@ def measure(pkg, procedural, name, wl, steps, warmup, plain_steps, e2e_steps, pa
                      "visible_draw_triangles_per_s": tri / (raster_avg / 1e3) if tri else None},
         "triangles_per_step_before_culling": int(wl.triangles_per_env().sum()),
         "tuning": t,
-        "autotune": None if not autotune else {"cached": tune_report["cached"],
-                                               "candidates": len(tune_report.get("trials", []))},
+        "autotune": None if not autotune else {
+            "cached": tune_report["cached"], "candidates": len(tune_report.get("trials", [])),
+            "trials": [{k: tr.get(k) for k in ("threads", "region_width", "region_height", "small_area",
+                                                "ctas_per_sm", "queue_fill_percent", "raster_ms", "error")
+                        if tr.get(k) is not None} for tr in tune_report.get("trials", [])]},
         "clocks": clocks,
         "parity": parity,
         "gpu_launches": 2 * steps,

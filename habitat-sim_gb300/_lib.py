@@ -53,7 +53,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("region_width", ctypes.c_int32),
                 ("region_height", ctypes.c_int32), ("small_area", ctypes.c_int32),
                 ("ctas_per_sm", ctypes.c_int32), ("plain_region_width", ctypes.c_int32),
-                ("plain_region_height", ctypes.c_int32), ("occlusion_culling", ctypes.c_int32)]
+                ("plain_region_height", ctypes.c_int32), ("occlusion_culling", ctypes.c_int32),
+                ("queue_fill_percent", ctypes.c_int32)]
 
 
 class DrawStats(ctypes.Structure):

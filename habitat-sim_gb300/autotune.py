@@ -4,7 +4,8 @@ Picks, for a renderer whose scenes are already populated, the CTA size
 (threads), the batched form's region size (the screen tile one CTA owns),
 the small-triangle threshold (bounding boxes up to this many pixels are
 rasterised by one lane, larger ones by the whole CTA from the shared-memory
-bin) and the per-scene form's region size.  Each candidate is timed with CUDA
+bin), the bin capacity in use (how full the bin gets before the CTA
+rasterises it) and the per-scene form's region size.  Each candidate is timed with CUDA
 events around the raster launch over a few draws of the caller's own poses;
 the best is applied and cached in a JSON file keyed by GPU name and a
 signature of the workload (scene count, resolutions, triangles), so a later
@@ -17,12 +18,18 @@ import statistics
 
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "gbr_autotune.json")
 
+# Launch shapes of the batched form: threads per CTA (8, 16 or 32 warps per
+# region), CTAs per SM, the region (screen tile) one CTA owns -- from 128 x 128
+# down to 32 x 32 -- and the small-triangle threshold.
 BATCHED_SPACE = ([dict(threads=1024, region_width=rw, region_height=rh, small_area=sa, ctas_per_sm=1)
                   for (rw, rh) in ((128, 128), (128, 64)) for sa in (1, 4)] +
-                 [dict(threads=512, region_width=128, region_height=64, small_area=sa, ctas_per_sm=2)
-                  for sa in (1, 4)] +
-                 [dict(threads=256, region_width=64, region_height=64, small_area=sa, ctas_per_sm=4)
-                  for sa in (1, 4)])
+                 [dict(threads=512, region_width=rw, region_height=rh, small_area=sa, ctas_per_sm=2)
+                  for (rw, rh) in ((128, 64), (64, 64)) for sa in (1, 4)] +
+                 [dict(threads=256, region_width=rw, region_height=rh, small_area=sa, ctas_per_sm=4)
+                  for (rw, rh) in ((64, 64), (32, 32)) for sa in (1, 4)])
+# Bin capacity in use: the share of the shared triangle queue that triggers
+# its rasterisation, tried on the best shape.
+QUEUE_FILL = (50, 75, 100)
 PLAIN_SPACE = [dict(plain_region_width=w, plain_region_height=h) for (w, h) in
                ((16, 32), (32, 32), (16, 16))]
 
@@ -105,8 +112,18 @@ def tune(renderer, poses, triangles, cache=DEFAULT_CACHE, draws=2, plain=True, f
             continue
         trials.append(dict(cand, raster_ms=_time_batched(renderer, poses, draws)))
     best = min((t for t in trials if "raster_ms" in t), key=lambda t: t["raster_ms"])
-    renderer.setTuning(**{k: best[k] for k in ("threads", "region_width", "region_height",
-                                                 "small_area", "ctas_per_sm")})
+    shape = {k: best[k] for k in ("threads", "region_width", "region_height", "small_area", "ctas_per_sm")}
+    renderer.setTuning(**shape, queue_fill_percent=75)
+    best = dict(best, queue_fill_percent=75)
+    for fill in QUEUE_FILL:
+        if fill == 75:
+            continue
+        renderer.setTuning(queue_fill_percent=fill)
+        t = dict(shape, queue_fill_percent=fill, raster_ms=_time_batched(renderer, poses, draws))
+        trials.append(t)
+        if t["raster_ms"] < best["raster_ms"]:
+            best = t
+    renderer.setTuning(**shape, queue_fill_percent=best["queue_fill_percent"])
     plain_trials = []
     if plain:
         for cand in PLAIN_SPACE:

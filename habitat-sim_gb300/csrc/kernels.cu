@@ -1272,7 +1272,7 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
     // survivors to the chunk ring.  Rounds: each warp takes one chunk of the
     // ring and its lanes set up one triangle each; triangles covering more
     // than small_area pixels are queued.  The queue is rasterised by the
-    // whole CTA (flush) once it is three quarters full, before a cull pass and at the
+    // whole CTA (flush) once it holds flush_at entries, before a cull pass and at the
     // end.  A cull pass runs whenever fewer chunks than warps wait in the
     // chunk ring, after the depth tiles are refreshed from the z-buffer.
     const uint32_t nclusters = p.vis_clusters[wi.scene];
@@ -1300,9 +1300,9 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
       const bool low = wr - rd < uint32_t(T / 32);
       const bool clusters_left = next < nclusters, have_clusters = cwr != crd;
       const bool need_cull = low && (clusters_left || have_clusters);
-      // A round adds at most T entries to fewer than 3T/4: the queue and the
+      // A round adds at most T entries to fewer than flush_at <= T: the queue and the
       // spill area (T each) hold them.
-      if (nq > 0 && (nq >= uint32_t(3 * T / 4) || need_cull || wr == rd)) {
+      if (nq > 0 && (nq >= p.flush_at || need_cull || wr == rd)) {
         // ---- flush: every thread takes a contiguous run of the queued
         // triangles' bounding-box pixels.
         uint32_t area = 0;
@@ -1467,14 +1467,14 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
       if (wr == rd) break;  // every chunk culled or drawn
 
       // ---- round: each warp takes chunks from the ring, one at a time, until
-      // the ring is empty or the queue holds three quarters of its capacity
+      // the ring is empty or the queue holds flush_at entries
       // (a chunk adds at most 32 triangles, or a few more when clipped; the
       // spill area and, beyond it, rasterisation by the lane itself take the
       // excess).  Chunks are claimed by compare-and-swap, so the read position
       // never passes the ring's write position.
       for (;;) {
         uint32_t slot = wr;
-        if (lane == 0 && *reinterpret_cast<volatile uint32_t*>(&s_qcount) < uint32_t(3 * T / 4)) {
+        if (lane == 0 && *reinterpret_cast<volatile uint32_t*>(&s_qcount) < p.flush_at) {
           uint32_t cur = *reinterpret_cast<volatile uint32_t*>(&s_rd);
           while (cur < wr) {
             const uint32_t prev = atomicCAS(&s_rd, cur, cur + 1u);
@@ -1977,6 +1977,7 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
   p.region_px = kNoAllocRegion * kNoAllocRegion;
   p.prefix_cap = 1;
   p.small_area = 1;
+  p.flush_at = 3 * kThreads / 4;
   const uint32_t grid = std::min<uint32_t>(a.items, uint32_t(sms) * uint32_t(occ));
   e = launch_raster(p, kThreads, grid, smem, st);
   if (e != cudaSuccess)

@@ -74,6 +74,7 @@ struct RasterParams {
   int32_t prefix_cap;  // visible draws whose ordinals are cached in shared memory
   int32_t small_area;  // boxes up to this many pixels are rasterised by one lane
   int32_t occlusion;   // skip chunks hidden behind the depths written so far
+  uint32_t flush_at;   // the queue is rasterised once it holds this many triangles (1..threads)
   // Lighting (max_lights > 0): lights per scene, per-draw model data, normals.
   const WorldLight* lights;
   const ModelRec* model;

@@ -1327,6 +1327,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
   rp.spill = d_spill_.ptr;
   rp.small_area = tuning_.small_area;
   rp.occlusion = tuning_.occlusion_culling;
+  rp.flush_at = uint32_t(std::max(1, tuning_.threads * tuning_.queue_fill_percent / 100));
   rp.max_lights = max_lights_;
   rp.ambient_factor = cfg_.ambient_factor;
   rp.any_lod = 0;
@@ -1739,7 +1740,8 @@ gbr_status Renderer::set_tuning(const gbr_tuning& t) {
       t.region_width * t.region_height > 32768 || t.small_area < 1 || t.ctas_per_sm < 1 ||
       t.plain_region_width < 4 || t.plain_region_height < 1 || t.plain_region_width > 1024 ||
       t.plain_region_height > 1024 || t.plain_region_width * t.plain_region_height > 32768 ||
-      t.occlusion_culling < 0 || t.occlusion_culling > 1)
+      t.occlusion_culling < 0 || t.occlusion_culling > 1 || t.queue_fill_percent < 25 ||
+      t.queue_fill_percent > 100)
     return fail(GBR_ERROR_INVALID_ARGUMENT, "setTuning: out of range");
   tuning_ = t;
   raster_configured_ = false;

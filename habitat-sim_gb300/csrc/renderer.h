@@ -252,7 +252,7 @@ class Renderer {
   bool items_staged_ = false;            // a new item order waits in the staging buffer
   uint64_t vis_needed_ = 0;              // visible records the current bindings need
 
-  gbr_tuning tuning_{1024, 128, 128, 1, 1, 16, 32, 1};
+  gbr_tuning tuning_{1024, 128, 128, 1, 1, 16, 32, 1, 75};
   size_t smem_bytes_ = 0, smem_plain_ = 0;
   int prefix_cap_ = 0;
   bool raster_configured_ = false;

@@ -318,6 +318,10 @@ typedef struct gbr_tuning {
   int32_t occlusion_culling;   /* 1: skip 32-triangle chunks hidden behind
                                   the depths already written (exact: the
                                   output does not change); 0: off           */
+  int32_t queue_fill_percent;  /* bin capacity in use: the CTA rasterises
+                                  its shared triangle queue once it holds
+                                  this share of its `threads` entries,
+                                  25..100 (default 75)                      */
 } gbr_tuning;
 gbr_status gbr_get_tuning(gbr_renderer* r, gbr_tuning* out);
 gbr_status gbr_set_tuning(gbr_renderer* r, const gbr_tuning* tuning);
