@@ -1256,7 +1256,21 @@ gbr_status Renderer::upload_step(cudaStream_t stream) {
 // for upload_step().
 void Renderer::order_items() {
   const size_t n = batched_items_.size();
+  // Geometry of each scene: the mesh of its largest draw.  Items of equal
+  // cost are grouped by it, so that the CTAs in flight at any time read the
+  // same vertices and indices and share them in L2 (scenes that draw the
+  // same large mesh would otherwise interleave and thrash it).
+  std::vector<uint32_t> geom(scenes_.size(), 0xffffffffu);
+  for (size_t s = 0; s < scenes_.size(); ++s) {
+    uint32_t best = 0;
+    for (const HostDraw& d : scenes_[s].draws)
+      if (d.index_count > best) {
+        best = d.index_count;
+        geom[s] = d.mesh;
+      }
+  }
   std::vector<uint64_t> cost(n);
+  std::vector<uint32_t> key(n);
   std::vector<uint8_t> on(n);
   for (size_t k = 0; k < n; ++k) {
     const WorkItem& it = batched_items_[k];
@@ -1264,12 +1278,14 @@ void Renderer::order_items() {
     const uint64_t tris = scenes_[sc.source].tris;
     on[k] = sc.enabled;
     cost[k] = (tris + 1) * uint64_t(it.w) * it.h / (uint64_t(sc.width) * sc.height) + tris / 4;
+    key[k] = geom[sc.source];
   }
   std::vector<uint32_t> perm(n);
   std::iota(perm.begin(), perm.end(), 0u);
   std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
     if (on[a] != on[b]) return on[a] > on[b];
-    return cost[a] > cost[b];
+    if (cost[a] != cost[b]) return cost[a] > cost[b];
+    return key[a] < key[b];
   });
   WorkItem* istage = reinterpret_cast<WorkItem*>(static_cast<char*>(h_stage_[slot_].ptr) +
                                                  camera_block_bytes() +
