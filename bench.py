@@ -394,16 +394,20 @@ def measure(pkg, procedural, name, wl, steps, warmup, plain_steps, e2e_steps, pa
         for plane, buf in zip(readback, hosts[k % 2]):
             r.imageIntoAsync(plane, rect, buf)
 
-    e2e_s = None
+    e2e_s, e2e_calls = None, []
     if e2e_steps:
         e2e_step(0)
         r.readbackWait()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        marks = [t0]
         for k in range(1, e2e_steps + 1):
             e2e_step(k)
+            marks.append(time.perf_counter())
         r.readbackWait()
-        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        marks.append(time.perf_counter())
+        e2e_s = (marks[-1] - t0) / e2e_steps
+        e2e_calls = [1e3 * (b - a) for a, b in zip(marks, marks[1:])]
     gc.enable()
     h2d = wl.envs * 96   # the camera block (P*V, view row, binding) per env
     d2h = sum(b.nbytes for b in hosts[0])
@@ -442,8 +446,10 @@ def measure(pkg, procedural, name, wl, steps, warmup, plain_steps, e2e_steps, pa
         "e2e": None if e2e_s is None else {
             "value": wl.envs / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s,
+            "call_ms": [round(x, 3) for x in e2e_calls],
             "timing": ("host clock over the steps: updateCameras + draw + 3 imageIntoAsync readbacks per "
-                       "step, readback of step k overlapping the draw of step k+1, then readbackWait")},
+                       "step, readback of step k overlapping the draw of step k+1, then readbackWait; call_ms: "
+                       "host time of each step's calls, the last entry readbackWait")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                      "kernel": "raster_kernel", "bytes_per_launch": launch_bytes,

@@ -766,17 +766,24 @@ __device__ __forceinline__ float clampc(float f) {
   return f;
 }
 
-// Channel c of an RGBA8 texel as a float: unorm[v] = v / 255 (correctly
-// rounded), a table in shared memory filled at kernel start.
-__device__ __forceinline__ float chan(uint32_t t, int c, const float* unorm) {
-  return unorm[(t >> (8 * c)) & 255u];
+// Channel c of an RGBA8 texel as a float, v / 255 correctly rounded.  1/255
+// is held as the unevaluated sum of two floats, hi = fl(1/255) and
+// lo = fl(1/255 - hi); fl(v hi + fl(v lo)), the sum taken by one fused
+// multiply-add, is the correctly rounded v / 255 for every v in [0, 255]
+// (multiplication by a constant in double-word form: Brisebarre and Muller,
+// "Correctly rounded multiplication by arbitrary precision constants", IEEE
+// Trans. Computers 57(2), 2008; checked here for all 256 v in exact rational
+// arithmetic).  v becomes a float exactly in the mantissa of 2^23.
+__device__ __forceinline__ float chan(uint32_t t, int c) {
+  const float v = __fsub_rn(__uint_as_float(0x4b000000u | ((t >> (8 * c)) & 255u)), 8388608.0f);
+  return __fmaf_rn(v, 0x1.010102p-8f, __fmul_rn(v, -0x1.fdfdfep-33f));
 }
 
 // One level of a texture (level k is max(1, w >> k) x max(1, h >> k); the
 // levels follow one another, each holding every layer), filtered nearest (0)
 // or bilinear (1) at texel centres with the texture's wrap modes.
 __device__ __forceinline__ void sample_level(const TextureRec& t, const uint32_t* texels, int L, int level, int filter,
-                             float s, float u, const float* unorm, float out[4]) {
+                             float s, float u, float out[4]) {
   const int tw = max(1, t.width >> level), th = max(1, t.height >> level);
   size_t off = t.offset;
   for (int k = 0; k < level; ++k) off += size_t(max(1, t.width >> k)) * size_t(max(1, t.height >> k)) * t.layers;
@@ -787,7 +794,7 @@ __device__ __forceinline__ void sample_level(const TextureRec& t, const uint32_t
     const int y = wrap(int(floorf(clampc(__fmul_rn(u, fh)))), th, t.wrap_t);
     const uint32_t v = __ldg(base + size_t(y) * tw + x);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) out[c] = chan(v, c, unorm);
+    for (int c = 0; c < 4; ++c) out[c] = chan(v, c);
     return;
   }
   const float fx = clampc(__fsub_rn(__fmul_rn(s, fw), 0.5f));
@@ -802,8 +809,7 @@ __device__ __forceinline__ void sample_level(const TextureRec& t, const uint32_t
   const uint32_t v11 = __ldg(base + size_t(y1) * tw + x1);
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    const float t00 = chan(v00, c, unorm), t10 = chan(v10, c, unorm), t01 = chan(v01, c, unorm),
-                t11 = chan(v11, c, unorm);
+    const float t00 = chan(v00, c), t10 = chan(v10, c), t01 = chan(v01, c), t11 = chan(v11, c);
     const float lo = fma_(a, __fsub_rn(t10, t00), t00);
     const float hi = fma_(a, __fsub_rn(t11, t01), t01);
     out[c] = fma_(b, __fsub_rn(hi, lo), lo);
@@ -817,8 +823,8 @@ __device__ __forceinline__ int clamp_layer(const TextureRec& t, int layer) {
 // Level-0 sampling with the magnification filter (textures whose
 // minification is the same and that have no mip levels).
 __device__ __forceinline__ void sample(const TextureRec& t, const uint32_t* texels, int layer, float s, float u,
-                                       const float* unorm, float out[4]) {
-  sample_level(t, texels, clamp_layer(t, layer), 0, t.filter, s, u, unorm, out);
+                                       float out[4]) {
+  sample_level(t, texels, clamp_layer(t, layer), 0, t.filter, s, u, out);
 }
 
 // log2 by the atanh series of the mantissa normalised to [sqrt(1/2), sqrt(2))
@@ -846,29 +852,29 @@ __device__ __forceinline__ float series_log2(float x) {
 // level, the nearest level ceil(lambda + 1/2) - 1, or the two levels around
 // lambda blended by its fraction, each with the minification filter.
 __device__ __forceinline__ void sample_lod(const TextureRec& t, const uint32_t* texels, int layer, float s, float u,
-                           float lambda, const float* unorm, float out[4]) {
+                           float lambda, float out[4]) {
   const int L = clamp_layer(t, layer);
   const float c = (t.filter == 1 && t.min_filter == 0 && t.mip_filter != 0) ? 0.5f : 0.0f;
   if (!(lambda > c)) {
-    sample_level(t, texels, L, 0, t.filter, s, u, unorm, out);
+    sample_level(t, texels, L, 0, t.filter, s, u, out);
     return;
   }
   const int q = t.levels - 1;
   if (t.mip_filter == 0) {
-    sample_level(t, texels, L, 0, t.min_filter, s, u, unorm, out);
+    sample_level(t, texels, L, 0, t.min_filter, s, u, out);
   } else if (t.mip_filter == 1) {
     int d = lambda <= 0.5f ? 0 : int(ceilf(__fadd_rn(lambda, 0.5f))) - 1;
     if (d > q) d = q;
-    sample_level(t, texels, L, d, t.min_filter, s, u, unorm, out);
+    sample_level(t, texels, L, d, t.min_filter, s, u, out);
   } else if (lambda >= float(q)) {
-    sample_level(t, texels, L, q, t.min_filter, s, u, unorm, out);
+    sample_level(t, texels, L, q, t.min_filter, s, u, out);
   } else {
     const float fl = floorf(lambda);
     const int d1 = int(fl);
     const float f = __fsub_rn(lambda, fl);
     float hi[4];
-    sample_level(t, texels, L, d1, t.min_filter, s, u, unorm, out);
-    sample_level(t, texels, L, d1 + 1, t.min_filter, s, u, unorm, hi);
+    sample_level(t, texels, L, d1, t.min_filter, s, u, out);
+    sample_level(t, texels, L, d1 + 1, t.min_filter, s, u, hi);
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[k] = fma_(f, __fsub_rn(hi[k], out[k]), out[k]);
   }
@@ -976,7 +982,7 @@ __device__ __noinline__ uint32_t lit_color(const float4* __restrict__ vertex_nor
 // that the derivative code does not add to the common path's registers.
 template <int Mode>
 __device__ __forceinline__ bool shade(const RasterParams& p, int W, int H, const VisibleRec* rec, uint32_t t,
-                                      int px, int py, const float* unorm, const WorldLight* lights, uint32_t nl,
+                                      int px, int py, const WorldLight* lights, uint32_t nl,
                                       const ModelRec* model, uint32_t& color, float& lin, uint32_t& sid) {
   // The record in 16-byte loads: mvp, zrow, (vertex_base, first_index,
   // tri_count, material), (semantic_id, ordinal, flags, chunk).
@@ -1063,7 +1069,7 @@ __device__ __forceinline__ bool shade(const RasterParams& p, int W, int H, const
     tt = fma_(mat.m[4], w, tt);
     const TextureRec& tr = p.textures[tex];
     if (Mode == 0 || (tr.mip_filter == 0 && tr.min_filter == tr.filter)) {
-      sample(tr, p.texels, mat.layer, ts, tt, unorm, tc);
+      sample(tr, p.texels, mat.layer, ts, tt, tc);
     } else if (Mode == 1) {
       return false;
     } else {
@@ -1095,7 +1101,7 @@ __device__ __forceinline__ bool shade(const RasterParams& p, int W, int H, const
       const float ry = __fsqrt_rn(__fadd_rn(__fmul_rn(duy, duy), __fmul_rn(dvy, dvy)));
       const float rho = fmaxf(rx, ry);
       const float lambda = rho > 0.0f ? (rho < 3.0e38f ? series_log2(rho) : 128.0f) : -1.0f;
-      sample_lod(tr, p.texels, mat.layer, ts, tt, lambda, unorm, tc);
+      sample_lod(tr, p.texels, mat.layer, ts, tt, lambda, tc);
     }
   }
 #undef GBR_INTERP
@@ -1225,8 +1231,6 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
   uint32_t* tiles = reinterpret_cast<uint32_t*>(smem + L.tiles);
   uint32_t* coarse = reinterpret_cast<uint32_t*>(smem + L.coarse);
   __shared__ uint32_t s_item, s_qcount, s_total, s_rd, s_wr, s_crd, s_cwr, s_next;
-  __shared__ float s_unorm[256];
-  for (int i = threadIdx.x; i < 256; i += T) s_unorm[i] = __fdiv_rn(float(i), 255.0f);
   __shared__ uint32_t s_warp[T / 32];
 
   for (uint32_t iter = 0;; ++iter) {
@@ -1537,7 +1541,7 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
         const uint32_t ord = uint32_t(key);
         dep = __uint_as_float(uint32_t(key >> 32));
         const uint32_t di = find_draw(prefix, vis, cached, nvis, ord);
-        if (!shade<Lod ? 1 : 0>(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, s_unorm,
+        if (!shade<Lod ? 1 : 0>(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py,
                                 lights, nlights, p.model ? p.model + vis_base + di : nullptr, col, lin, sid)) {
           keys[i] = key | kDeferred;
           deferred = true;
@@ -1560,7 +1564,7 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
         const uint32_t di = find_draw(prefix, vis, cached, nvis, ord);
         uint32_t col, sid;
         float lin;
-        shade<2>(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, s_unorm, lights, nlights,
+        shade<2>(p, c.W, c.H, vis + di, ord - __ldg(&vis[di].ordinal), px, py, lights, nlights,
                  p.model ? p.model + vis_base + di : nullptr, col, lin, sid);
         if (p.out.color) p.out.color[o] = col;
         if (p.out.depth) p.out.depth[o] = dep;
