@@ -131,6 +131,8 @@ PROTOTYPES = {
     "gbr_readback_wait": (_ST, [_P]),
     "gbr_scenes_into_async": (_ST, [_P, _U32, _U32, _U32, _P]),
     "gbr_depth_image_into": (_ST, [_P, ctypes.POINTER(_I32), _P, _U64]),
+    "gbr_semantic_image_into": (_ST, [_P, ctypes.POINTER(_I32), _P, _U64]),
+    "gbr_linear_depth_image_into": (_ST, [_P, ctypes.POINTER(_I32), _P, _U64]),
     "gbr_scene_image_into": (_ST, [_P, _U32, _U32, _P, _U64]),
     "gbr_plane_device_pointer": (_ST, [_P, _U32, ctypes.POINTER(_P), ctypes.POINTER(_U64)]),
     "gbr_plane_dlpack": (_ST, [_P, _U32, ctypes.POINTER(_P)]),

@@ -345,6 +345,16 @@ gbr_status gbr_depth_image_into(gbr_renderer* r, const int32_t rect[4], void* ds
   return gbr_image_into(r, GBR_PLANE_DEPTH, rect, dst, row_bytes);
 }
 
+gbr_status gbr_semantic_image_into(gbr_renderer* r, const int32_t rect[4], void* dst,
+                                   uint64_t row_bytes) {
+  return gbr_image_into(r, GBR_PLANE_SEMANTIC, rect, dst, row_bytes);
+}
+
+gbr_status gbr_linear_depth_image_into(gbr_renderer* r, const int32_t rect[4], void* dst,
+                                       uint64_t row_bytes) {
+  return gbr_image_into(r, GBR_PLANE_LINEAR_DEPTH, rect, dst, row_bytes);
+}
+
 gbr_status gbr_scene_image_into(gbr_renderer* r, uint32_t plane, uint32_t scene, void* dst,
                                 uint64_t row_bytes) {
   GBR_HANDLE(r);

@@ -280,6 +280,12 @@ gbr_status gbr_color_image_into(gbr_renderer* r, const int32_t rect[4], void* ds
                                 uint64_t dst_row_bytes);
 gbr_status gbr_depth_image_into(gbr_renderer* r, const int32_t rect[4], void* dst,
                                 uint64_t dst_row_bytes);
+/* The same for the planes the reference does not have: the semantic id
+ * (uint32, 0 = background) and linear depth (float metres, 0 = background). */
+gbr_status gbr_semantic_image_into(gbr_renderer* r, const int32_t rect[4], void* dst,
+                                   uint64_t dst_row_bytes);
+gbr_status gbr_linear_depth_image_into(gbr_renderer* r, const int32_t rect[4], void* dst,
+                                       uint64_t dst_row_bytes);
 /* One scene's rectangle of a plane (either layout), rows bottom-up. */
 gbr_status gbr_scene_image_into(gbr_renderer* r, uint32_t plane, uint32_t scene, void* dst,
                                 uint64_t dst_row_bytes);

@@ -465,6 +465,12 @@ class RendererStandalone : public Renderer {
   // Extensions: linear depth in metres and the semantic-id plane.
   Image2D linearDepthImage() { return image(GBR_PLANE_LINEAR_DEPTH, PixelFormat::R32F); }
   Image2D semanticImage() { return image(GBR_PLANE_SEMANTIC, PixelFormat::R32UI); }
+  void linearDepthImageInto(const Range2Di& rectangle, const MutableImageView2D& image) {
+    into(GBR_PLANE_LINEAR_DEPTH, rectangle, image, "RendererStandalone::linearDepthImageInto()");
+  }
+  void semanticImageInto(const Range2Di& rectangle, const MutableImageView2D& image) {
+    into(GBR_PLANE_SEMANTIC, rectangle, image, "RendererStandalone::semanticImageInto()");
+  }
   void imageInto(uint32_t plane, const Range2Di& rectangle, const MutableImageView2D& image) {
     into(plane, rectangle, image, "RendererStandalone::imageInto()");
   }

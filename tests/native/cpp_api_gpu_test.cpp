@@ -101,6 +101,21 @@ int main(int argc, char** argv) {
     std::vector<float> dsub(40 * 70);
     renderer.depthImageInto(rect, gb::MutableImageView2D{gb::PixelFormat::Depth32F, rect.size(), dsub.data()});
     CHECK(dsub[(64 - 10) * 40 + (48 - 30)] == depth.pixel<float>(64, 48));
+    // The extension planes' sub-rectangles against their whole images.
+    const gb::Image2D ids = renderer.semanticImage();
+    const gb::Image2D linear = renderer.linearDepthImage();
+    std::vector<uint32_t> idsub(40 * 70);
+    std::vector<float> lsub(40 * 70);
+    renderer.semanticImageInto(rect, gb::MutableImageView2D{gb::PixelFormat::R32UI, rect.size(), idsub.data()});
+    renderer.linearDepthImageInto(rect, gb::MutableImageView2D{gb::PixelFormat::R32F, rect.size(), lsub.data()});
+    same = true;
+    for (int y = 0; y < 70; ++y)
+      for (int x = 0; x < 40; ++x)
+        same = same && idsub[y * 40 + x] == ids.pixel<uint32_t>(y + 10, x + 30) &&
+               std::memcmp(&lsub[y * 40 + x], &linear.pixel<float>(y + 10, x + 30), 4) == 0;
+    CHECK(same);
+    CHECK(ids.pixel<uint32_t>(0, 0) == 0 && linear.pixel<float>(0, 0) == 0.0f);
+    CHECK(linear.pixel<float>(48, 64) > 0.0f);
     CHECK(renderer.colorCudaBufferDevicePointer() != nullptr);
     CHECK(renderer.depthCudaBufferDevicePointer() != nullptr);
 
