@@ -83,6 +83,9 @@ def parse():
     p.add_argument("--serving-texture-side", type=int, default=2048)
     p.add_argument("--serving-fractions", type=lambda t: [float(x) for x in t.split(",")],
                    default=[0.1, 0.25, 0.5, 0.75, 0.9])
+    p.add_argument("--serving-slots", default="64:96,128:64,256:16",
+                   type=lambda t: {int(a): int(b) for a, b in (kv.split(":") for kv in t.split(","))},
+                   help="render slots per square resolution, e.g. 64:96,128:64,256:16")
     return p.parse_args()
 
 
@@ -491,7 +494,7 @@ def serving_leg(pkg, args):
     closed-loop sample; a run with the budget at a quarter of the catalog's
     bytes, Zipf(1) popularity and 200 requests/s, where eviction works."""
     from habitat_sim_gb300 import server
-    slots = {64: 96, 128: 64, 256: 16}
+    slots = dict(args.serving_slots)
     n = args.serving_requests
     t0 = time.perf_counter()
     cat = server.SceneCatalog(args.serving_scenes, seed=4, tri_range=(1e4, 1e6),
