@@ -83,7 +83,7 @@ def parse():
     p.add_argument("--serving-texture-side", type=int, default=2048)
     p.add_argument("--serving-fractions", type=lambda t: [float(x) for x in t.split(",")],
                    default=[0.1, 0.25, 0.5, 0.75, 0.9])
-    p.add_argument("--serving-slots", default="64:96,128:64,256:16",
+    p.add_argument("--serving-slots", default="64:96,128:160,256:64",
                    type=lambda t: {int(a): int(b) for a, b in (kv.split(":") for kv in t.split(","))},
                    help="render slots per square resolution, e.g. 64:96,128:64,256:16")
     return p.parse_args()
@@ -485,9 +485,10 @@ def serving_leg(pkg, args):
     triangles sampled bilinear, one mesh view and material per object: about
     40 GB of geometry and textures on the device), requests (scene uniform,
     6-DoF pose, 64/128/256 px with p 0.3/0.5/0.2), a 150 GB device budget with
-    LRU eviction.  Continuous batching into 96 + 64 + 16 render slots per
-    step, one graph launch per step, slot rectangles copied back to pinned
-    host memory overlapped with the next step.  Runs: every scene loaded
+    LRU eviction.  Continuous batching into 96 + 160 + 64 render slots per
+    step (320 requests of the resolution mix), one graph launch per step,
+    slot rectangles copied back to pinned host memory overlapped with the
+    next step.  Runs: every scene loaded
     (timed); a closed-loop run of all requests (saturation); Poisson arrivals
     at fractions of saturation (the sweep; latency from arrival to the three
     images in pinned host memory); the plain path (one request per draw) on a

@@ -339,7 +339,9 @@ class RenderServer:
     """Serves requests for the scenes of ``catalog`` on one GPU.
 
     ``slots`` maps each square resolution to its number of render slots (the
-    largest batch of that class one step takes); ``max_resident`` bounds the
+    largest batch of that class one step takes; the default, 96 + 160 + 64,
+    is 320 requests of the 0.3 / 0.5 / 0.2 mix of 64, 128 and 256 px, so that
+    no class saturates before the others); ``max_resident`` bounds the
     resident scenes; ``budget_bytes`` bounds their device bytes (geometry,
     textures, chunk boxes; default: no limit); ``max_loads_per_step`` bounds
     the scene loads one step may wait for (requests beyond it wait for a
@@ -352,7 +354,7 @@ class RenderServer:
         self.torch = torch
         self.pkg = pkg
         self.catalog = catalog
-        self.slots = dict(slots or {64: 96, 128: 64, 256: 16})
+        self.slots = dict(slots or {64: 96, 128: 160, 256: 64})
         self.graph = graph
         viewports, self.slot_base, self.class_offset = [], {}, {}
         px = 0
