@@ -489,7 +489,8 @@ def serving_leg(pkg, args):
     step (320 requests of the resolution mix), one graph launch per step,
     slot rectangles copied back to pinned host memory overlapped with the
     next step.  Runs: every scene loaded
-    (timed); a closed-loop run of all requests (saturation); Poisson arrivals
+    (timed); the launch shape chosen by closed-loop throughput (the
+    autotuner's search space); a closed-loop run of all requests (saturation); Poisson arrivals
     at fractions of saturation (the sweep; latency from arrival to the three
     images in pinned host memory); the plain path (one request per draw) on a
     closed-loop sample; a run with the budget at a quarter of the catalog's
@@ -525,6 +526,11 @@ def serving_leg(pkg, args):
     out["warm_load_s"] = time.perf_counter() - t0
     out["resident_bytes"] = int(srv.residency.bytes)
     out["device_bytes_held"] = int(srv.r.deviceMemory()[0])
+    if not args.no_autotune:
+        tuning, trials = srv.tune(lambda: server.random_requests(cat, 3000, rate=0, seed=130))
+        out["tuning"] = tuning
+        out["autotune"] = {"objective": "closed-loop requests/s serving 3000 requests",
+                           "trials": trials}
 
     def keep(st, closed=False):
         # A closed-loop run has every request pending at the start: its
@@ -545,6 +551,8 @@ def serving_leg(pkg, args):
     srv.close()
     budget = total_bytes // 4
     srv = server.RenderServer(pkg, cat, slots=slots, max_resident=len(cat), budget_bytes=budget)
+    if "tuning" in out:
+        srv.r.setTuning(**out["tuning"])
     st = srv.serve(server.random_requests(cat, 1000, rate=200.0, seed=110, zipf=1.0), keep_images=False)
     out["small_budget"] = dict(budget_bytes=budget, offered_per_s=200.0, popularity="zipf 1.0",
                                **keep(st))

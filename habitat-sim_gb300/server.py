@@ -9,8 +9,9 @@ render slots: fixed square viewports of each resolution class, laid out at
 the start of one ragged framebuffer.  Every used slot is pointed at its
 request's resident scene (``setSceneSources``), unused slots are disabled,
 all slots are drawn by one batched launch (a CUDA graph), and the used slot
-rectangles are copied to pinned host memory while the host prepares the next
-step.  Scenes are loaded on first use into "content" scenes (1 x 1 viewports
+rectangles are copied to pinned host memory on a second stream while the
+host prepares the next step and the GPU draws it (two plane sets, alternated
+by the draws).  Scenes are loaded on first use into "content" scenes (1 x 1 viewports
 that are never drawn themselves) and evicted least-recently-used when the
 device budget or the number of content scenes would be exceeded; eviction
 returns their device ranges to the renderer's free lists.
@@ -368,8 +369,10 @@ class RenderServer:
         self.content_base = len(viewports)
         viewports += [(1, 1)] * max_resident
         cfg = pkg.RendererConfiguration().setViewports(viewports).setDrawMode(pkg.DrawMode.Batched)
+        # Two plane sets, alternated by the draws: the copy-back of step k
+        # reads one set while step k + 1 draws into the other.
         self.r = pkg.RendererStandalone(cfg, pkg.RendererStandaloneConfiguration().setCudaDevice(
-            device).setFlags(pkg.RendererStandaloneFlags.QuietLog))
+            device).setFlags(pkg.RendererStandaloneFlags.QuietLog | pkg.RendererStandaloneFlags.DoubleBuffer))
         for s in range(len(viewports)):
             self.r.setSceneEnabled(s, False)
         self.enabled = np.zeros(self.n_slots, bool)
@@ -381,19 +384,30 @@ class RenderServer:
         self.max_loads_per_step = max_loads_per_step
         self.device = torch.device("cuda", device)
         self.stream = torch.cuda.Stream(device=self.device)
-        planes = (pkg.Plane.Color, pkg.Plane.LinearDepth, pkg.Plane.Semantic)
-        self.planes = [self.r.deviceTensor(p) for p in planes]
+        self.copy_stream = torch.cuda.Stream(device=self.device)
+        self._planes = (pkg.Plane.Color, pkg.Plane.LinearDepth, pkg.Plane.Semantic)
+        self._views = {}  # device address of a plane set's colour plane -> views of its planes
+        first = self._set_views()
         self.host = [[torch.empty((self.slot_px,) + tuple(t.shape[1:]), dtype=t.dtype,
-                                  pin_memory=True) for t in self.planes] for _ in range(2)]
+                                  pin_memory=True) for t in first] for _ in range(2)]
+        self._copies = collections.deque()  # copy-back events of the last two steps
         self._proj = {}
         self._step = 0
         self._copier = concurrent.futures.ThreadPoolExecutor(
             max_workers=max(1, min(8, (os.cpu_count() or 2) - 1)))
 
+    def _set_views(self):
+        """Device views of the plane set the last draw wrote (made once per set)."""
+        key = self.r.planeDevicePointer(self.pkg.Plane.Color)[0]
+        views = self._views.get(key)
+        if views is None:
+            views = self._views[key] = [self.r.deviceTensor(p) for p in self._planes]
+        return views
+
     def close(self):
         self._copier.shutdown()
         self.torch.cuda.synchronize(self.device)
-        self.planes = None
+        self._views = {}
         self.r.close()
 
     # -- residency
@@ -476,16 +490,23 @@ class RenderServer:
             self.r.setSceneEnabled(int(s), bool(want[s]))
         self.enabled = want
         self.r.setSceneSources(self.sources[:self.n_slots])
+        # This draw writes the plane set of the step before last: its
+        # copy-back must be done first.
+        if len(self._copies) == 2:
+            self.stream.wait_event(self._copies.popleft())
         self.r.draw(self.stream, graph=self.graph)
+        planes = self._set_views()
         buf = self.host[self._step % 2]
         self._step += 1
-        with torch.cuda.stream(self.stream):
+        self.copy_stream.wait_stream(self.stream)
+        with torch.cuda.stream(self.copy_stream):
             for c, reqs in batch.items():
                 o, n = self.class_offset[c], len(reqs) * c * c
-                for dst, src in zip(buf, self.planes):
+                for dst, src in zip(buf, planes):
                     dst[o:o + n].copy_(src[o:o + n], non_blocking=True)
         ev = torch.cuda.Event()
-        ev.record(self.stream)
+        ev.record(self.copy_stream)
+        self._copies.append(ev)
         return (batch, buf, ev), deferred
 
     def finish(self, handle, clock=None, keep_images=True):
@@ -518,6 +539,41 @@ class RenderServer:
                     req.semantic = img.reshape(c, c).view(np.uint32)
                     req.done = now
         return batch
+
+    # -- launch shape
+    def tune(self, make_requests, reps=2):
+        """Choose the raster kernel's launch shape for serving: every shape of
+        the autotuner's search space (threads per CTA, region, small-triangle
+        threshold), then the bin capacity on the best, each timed as the
+        closed-loop throughput of serving ``make_requests()`` (a fresh list
+        per run, for scenes that are already resident; the best of ``reps``
+        runs after an untimed one).  Applies the best and returns (tuning,
+        trials)."""
+        from . import autotune
+
+        def rate(**cand):
+            self.r.setTuning(**cand)
+            self.serve(make_requests(), realtime=False, keep_images=False)
+            return max(self.serve(make_requests(), realtime=False, keep_images=False)["requests_per_s"]
+                       for _ in range(reps))
+
+        trials = []
+        for cand in autotune.BATCHED_SPACE:
+            try:
+                trials.append(dict(cand, queue_fill_percent=75, requests_per_s=rate(queue_fill_percent=75,
+                                                                                   **cand)))
+            except Exception as e:  # does not fit this GPU's shared memory
+                trials.append(dict(cand, error=str(e)))
+        best = max((t for t in trials if "requests_per_s" in t), key=lambda t: t["requests_per_s"])
+        shape = {k: best[k] for k in ("threads", "region_width", "region_height", "small_area", "ctas_per_sm")}
+        for fill in autotune.QUEUE_FILL:
+            if fill != 75:
+                t = dict(shape, queue_fill_percent=fill, requests_per_s=rate(queue_fill_percent=fill, **shape))
+                trials.append(t)
+                if t["requests_per_s"] > best["requests_per_s"]:
+                    best = t
+        self.r.setTuning(**shape, queue_fill_percent=best["queue_fill_percent"])
+        return self.r.tuning(), trials
 
     # -- the request loop
     def serve(self, requests, realtime=True, keep_images=True, max_batch=None):
