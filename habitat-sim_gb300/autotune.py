@@ -4,8 +4,9 @@ Picks, for a renderer whose scenes are already populated, the CTA size
 (threads), the batched form's region size (the screen tile one CTA owns),
 the small-triangle threshold (bounding boxes up to this many pixels are
 rasterised by one lane, larger ones by the whole CTA from the shared-memory
-bin), the bin capacity in use (how full the bin gets before the CTA
-rasterises it) and the per-scene form's region size.  Each candidate is timed with CUDA
+bin; 1 and 4 px with every shape, 8 and 16 px on the best), the bin
+capacity in use (how full the bin gets before the CTA rasterises it) and
+the per-scene form's region size.  Each candidate is timed with CUDA
 events around the raster launch over a few draws of the caller's own poses;
 the best is applied and cached in a JSON file keyed by GPU name and a
 signature of the workload (scene count, resolutions, triangles), so a later
@@ -27,6 +28,9 @@ BATCHED_SPACE = ([dict(threads=1024, region_width=rw, region_height=rh, small_ar
                   for (rw, rh) in ((128, 64), (64, 64)) for sa in (1, 4)] +
                  [dict(threads=256, region_width=rw, region_height=rh, small_area=sa, ctas_per_sm=4)
                   for (rw, rh) in ((64, 64), (32, 32)) for sa in (1, 4)])
+# Larger small-triangle thresholds, tried on the best shape (sub-pixel scan
+# geometry gains from 8 px, finer-grained scenes lose beyond 4).
+SMALL_AREA = (8, 16)
 # Bin capacity in use: the share of the shared triangle queue that triggers
 # its rasterisation, tried on the best shape.
 QUEUE_FILL = (50, 75, 100)
@@ -112,6 +116,14 @@ def tune(renderer, poses, triangles, cache=DEFAULT_CACHE, draws=2, plain=True, f
             continue
         trials.append(dict(cand, raster_ms=_time_batched(renderer, poses, draws)))
     best = min((t for t in trials if "raster_ms" in t), key=lambda t: t["raster_ms"])
+    for sa in SMALL_AREA:
+        cand = dict({k: best[k] for k in ("threads", "region_width", "region_height", "ctas_per_sm")},
+                    small_area=sa)
+        renderer.setTuning(**cand)
+        t = dict(cand, raster_ms=_time_batched(renderer, poses, draws))
+        trials.append(t)
+        if t["raster_ms"] < best["raster_ms"]:
+            best = t
     shape = {k: best[k] for k in ("threads", "region_width", "region_height", "small_area", "ctas_per_sm")}
     renderer.setTuning(**shape, queue_fill_percent=75)
     best = dict(best, queue_fill_percent=75)
