@@ -338,11 +338,24 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
   TraceRange trace_("gbr.add_mesh");
   if (!m.positions || (m.index_count && !m.indices))
     return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: positions and indices are required");
-  for (uint32_t i = 0; i < m.index_count; ++i)
-    if (m.indices[i] >= m.vertex_count)
-      return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: index " + std::to_string(i) +
-                                                  " out of range for " +
-                                                  std::to_string(m.vertex_count) + " vertices");
+  // Every index below the vertex count (large meshes checked on the host pool;
+  // the first bad index is then looked up for the message).
+  std::atomic<bool> bad_index{false};
+  const std::function<void(uint32_t, uint32_t)> check = [&](uint32_t a, uint32_t b) {
+    uint32_t hi = 0;
+    for (uint32_t i = a; i < b; ++i) hi = std::max(hi, m.indices[i]);
+    if (b > a && hi >= m.vertex_count) bad_index.store(true);
+  };
+  if (m.index_count >= (1u << 18))
+    shared_pool().run(m.index_count, 1u << 16, check);
+  else
+    check(0, m.index_count);
+  if (bad_index.load())
+    for (uint32_t i = 0; i < m.index_count; ++i)
+      if (m.indices[i] >= m.vertex_count)
+        return fail(GBR_ERROR_INVALID_ARGUMENT, "addMesh: index " + std::to_string(i) +
+                                                    " out of range for " +
+                                                    std::to_string(m.vertex_count) + " vertices");
   cudaSetDevice(device_);
   const size_t nv = m.vertex_count;
   const uint64_t vb = vertex_pool_.alloc(nv), ib = index_pool_.alloc(m.index_count);
@@ -373,8 +386,8 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
   // staging is free again once a piece is drained.
   constexpr size_t kStageBytes = size_t(32) << 20;
   const size_t vbytes = normals ? 56 : 40;
-  const size_t piece_v = kStageBytes / vbytes, piece_i = kStageBytes / 4;
-  const size_t need = std::max(std::min(nv, piece_v) * vbytes, std::min<size_t>(m.index_count, piece_i) * 4);
+  const size_t piece_v = kStageBytes / vbytes;
+  const size_t need = std::min(nv, piece_v) * vbytes;
   if (!h_mesh_stage_.reserve(std::max<size_t>(need, 16))) {
     undo();
     return fail(GBR_ERROR_OUT_OF_MEMORY, "addMesh: out of pinned host memory");
@@ -419,14 +432,11 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
                "addMesh upload");
     GBR_CUDA(cudaStreamSynchronize(0), "addMesh upload");
   }
-  for (size_t i0 = 0; i0 < m.index_count; i0 += piece_i) {
-    const size_t n = std::min<size_t>(piece_i, m.index_count - i0);
-    std::memcpy(stage, m.indices + i0, n * 4);
-    GBR_CUDA(cudaMemcpyAsync(d_indices_.as<char>() + (size_t(ib) + i0) * 4, stage, n * 4,
-                             cudaMemcpyHostToDevice, 0),
+  // The indices need no repacking: one copy from the caller's memory.
+  if (m.index_count)
+    GBR_CUDA(cudaMemcpy(d_indices_.as<char>() + size_t(ib) * 4, m.indices, size_t(m.index_count) * 4,
+                        cudaMemcpyHostToDevice),
              "addMesh upload");
-    GBR_CUDA(cudaStreamSynchronize(0), "addMesh upload");
-  }
   MeshRec rec{};
   rec.vertex_base = uint32_t(vb);
   rec.vertex_count = m.vertex_count;
@@ -438,8 +448,24 @@ gbr_status Renderer::add_mesh(const gbr_mesh_data& m, uint32_t* id) {
   mesh_live_.push_back(true);
   if (host_pos_.size() < ve * 3) host_pos_.resize(ve * 3);
   if (host_indices_.size() < ie) host_indices_.resize(ie);
-  std::copy(m.positions, m.positions + nv * 3, host_pos_.begin() + vb * 3);
-  std::copy(m.indices, m.indices + m.index_count, host_indices_.begin() + ib);
+  // Host mirrors (positions and indices, for the views' bounding boxes).
+  float* hp = host_pos_.data() + vb * 3;
+  uint32_t* hi = host_indices_.data() + ib;
+  const uint64_t pos_words = uint64_t(nv) * 3, words = pos_words + m.index_count;
+  const std::function<void(uint32_t, uint32_t)> mirror = [&](uint32_t a, uint32_t b) {
+    const uint64_t w0 = uint64_t(a) << 12, w1 = std::min<uint64_t>(words, uint64_t(b) << 12);
+    if (w0 < pos_words)
+      std::memcpy(hp + w0, m.positions + w0, (std::min(w1, pos_words) - w0) * 4);
+    if (w1 > pos_words) {
+      const uint64_t i0 = std::max(w0, pos_words) - pos_words, i1 = w1 - pos_words;
+      std::memcpy(hi + i0, m.indices + i0, (i1 - i0) * 4);
+    }
+  };
+  const uint32_t blocks = uint32_t((words + 4095) >> 12);
+  if (words >= (1u << 20))
+    shared_pool().run(blocks, 64, mirror);
+  else
+    mirror(0, blocks);
   tables_dirty_ = true;
   graph_valid_ = false;
   *id = uint32_t(meshes_.size() - 1);
@@ -526,7 +552,6 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
   }
   for (uint32_t i = 0; i < count; ++i) {
     const gbr_mesh_view& v = views[i];
-    const MeshRec& m = meshes_[v.mesh];
     MeshView mv{};
     mv.mesh = v.mesh;
     mv.index_offset = v.index_offset;
@@ -535,30 +560,25 @@ gbr_status Renderer::add_template(const char* name, uint32_t count, const gbr_me
     std::memcpy(mv.transform, v.transform, 64);
     mv.chunk_count = (v.index_count / 3 + kChunkTris - 1) / kChunkTris;
     mv.box_base = uint32_t(box_pool_.alloc(mv.chunk_count + cluster_count(mv.chunk_count)));
-    if (boxes_.size() < box_pool_.end) boxes_.resize(box_pool_.end);
-    build_chunk_boxes(m, v.index_offset, v.index_count, mv.box_base, mv.bbox);
     boxes_lo_ = std::min<size_t>(boxes_lo_, mv.box_base);
     boxes_hi_ = std::max<size_t>(boxes_hi_, mv.box_base + mv.chunk_count + cluster_count(mv.chunk_count));
     mv.live = true;
     views_.push_back(mv);
   }
+  if (boxes_.size() < box_pool_.end) boxes_.resize(box_pool_.end);
+  build_chunk_boxes(begin, uint32_t(views_.size()));
   names_[name] = {begin, uint32_t(views_.size())};
   tables_dirty_ = true;
   graph_valid_ = false;
   return GBR_OK;
 }
 
-// Object-space bounding box of every kChunkTris consecutive triangles of a
-// view, of every kClusterChunks consecutive chunks, and of the whole view
-// (every index of the range, also a trailing partial triangle) into bbox
-// {lo xyz, hi xyz}.  Views of many chunks are split over the host pool.
-void Renderer::build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count,
-                                 uint32_t box_base, float bbox[6]) {
-  const uint32_t tris = index_count / 3;
-  const uint32_t chunks = (tris + kChunkTris - 1) / kChunkTris;
-  const uint32_t clusters = (chunks + kClusterChunks - 1) / kClusterChunks;
-  const uint32_t* idx = host_indices_.data() + size_t(m.index_base) + index_offset;
-  const float* pos = host_pos_.data() + size_t(m.vertex_base) * 3;
+// Object-space bounding box of every kChunkTris consecutive triangles of the
+// views [first, last), of every kClusterChunks consecutive chunks, and of each
+// whole view (every index of its range, also a trailing partial triangle)
+// into its bbox {lo xyz, hi xyz}.  The clusters of all the views are one
+// range of work for the host pool when they hold many triangles.
+void Renderer::build_chunk_boxes(uint32_t first, uint32_t last) {
   auto extend = [](ChunkBox& b, const float* p) {
     for (int c = 0; c < 3; ++c) {
       b.lo[c] = std::min(b.lo[c], p[c]);
@@ -573,40 +593,60 @@ void Renderer::build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32
     }
     return b;
   };
-  // One cluster per work unit: its chunk boxes, then their union.
-  const std::function<void(uint32_t, uint32_t)> fn = [&](uint32_t c0, uint32_t c1) {
-    for (uint32_t cl = c0; cl < c1; ++cl) {
-      ChunkBox u = empty();
+  // Work units: (view, cluster) in view order.
+  std::vector<uint32_t> unit_base(last - first + 1, 0);
+  uint64_t tris_all = 0;
+  for (uint32_t v = first; v < last; ++v) {
+    unit_base[v - first + 1] = unit_base[v - first] + cluster_count(views_[v].chunk_count);
+    tris_all += views_[v].index_count / 3;
+  }
+  const std::function<void(uint32_t, uint32_t)> fn = [&](uint32_t u0, uint32_t u1) {
+    uint32_t v = uint32_t(std::upper_bound(unit_base.begin(), unit_base.end(), u0) - unit_base.begin()) - 1;
+    for (uint32_t u = u0; u < u1; ++u) {
+      while (u >= unit_base[v + 1]) ++v;
+      const MeshView& mv = views_[first + v];
+      const MeshRec& m = meshes_[mv.mesh];
+      const uint32_t* idx = host_indices_.data() + size_t(m.index_base) + mv.index_offset;
+      const float* pos = host_pos_.data() + size_t(m.vertex_base) * 3;
+      const uint32_t tris = mv.index_count / 3, chunks = mv.chunk_count, cl = u - unit_base[v];
+      ChunkBox c = empty();
       const uint32_t ch1 = std::min(chunks, (cl + 1) * kClusterChunks);
       for (uint32_t ch = cl * kClusterChunks; ch < ch1; ++ch) {
         ChunkBox b = empty();
         const uint32_t k1 = std::min(tris, (ch + 1) * kChunkTris) * 3;
         for (uint32_t k = ch * kChunkTris * 3; k < k1; ++k) extend(b, pos + size_t(idx[k]) * 3);
-        boxes_[box_base + ch] = b;
+        boxes_[mv.box_base + ch] = b;
         for (int k = 0; k < 3; ++k) {
-          u.lo[k] = std::min(u.lo[k], b.lo[k]);
-          u.hi[k] = std::max(u.hi[k], b.hi[k]);
+          c.lo[k] = std::min(c.lo[k], b.lo[k]);
+          c.hi[k] = std::max(c.hi[k], b.hi[k]);
         }
       }
-      boxes_[box_base + chunks + cl] = u;
+      boxes_[mv.box_base + chunks + cl] = c;
     }
   };
-  if (tris >= (1u << 16))
-    shared_pool().run(clusters, 4, fn);
+  const uint32_t units = unit_base.back();
+  if (tris_all >= (1u << 16))
+    shared_pool().run(units, 4, fn);
   else
-    fn(0, clusters);
-  ChunkBox all = empty();
-  for (uint32_t cl = 0; cl < clusters; ++cl) {
-    const ChunkBox& u = boxes_[box_base + chunks + cl];
-    for (int k = 0; k < 3; ++k) {
-      all.lo[k] = std::min(all.lo[k], u.lo[k]);
-      all.hi[k] = std::max(all.hi[k], u.hi[k]);
+    fn(0, units);
+  for (uint32_t v = first; v < last; ++v) {
+    MeshView& mv = views_[v];
+    const MeshRec& m = meshes_[mv.mesh];
+    const uint32_t* idx = host_indices_.data() + size_t(m.index_base) + mv.index_offset;
+    const float* pos = host_pos_.data() + size_t(m.vertex_base) * 3;
+    ChunkBox all = empty();
+    for (uint32_t cl = 0; cl < cluster_count(mv.chunk_count); ++cl) {
+      const ChunkBox& u = boxes_[mv.box_base + mv.chunk_count + cl];
+      for (int k = 0; k < 3; ++k) {
+        all.lo[k] = std::min(all.lo[k], u.lo[k]);
+        all.hi[k] = std::max(all.hi[k], u.hi[k]);
+      }
     }
-  }
-  for (uint32_t k = tris * 3; k < index_count; ++k) extend(all, pos + size_t(idx[k]) * 3);
-  for (int c = 0; c < 3; ++c) {
-    bbox[c] = all.lo[c];
-    bbox[3 + c] = all.hi[c];
+    for (uint32_t k = mv.index_count / 3 * 3; k < mv.index_count; ++k) extend(all, pos + size_t(idx[k]) * 3);
+    for (int c = 0; c < 3; ++c) {
+      mv.bbox[c] = all.lo[c];
+      mv.bbox[3 + c] = all.hi[c];
+    }
   }
 }
 

@@ -175,8 +175,7 @@ class Renderer {
   gbr_status upload_step(cudaStream_t stream);
   gbr_status enqueue_step(cudaStream_t stream, uint32_t mode);
   gbr_status ensure_raster_config();
-  void build_chunk_boxes(const MeshRec& m, uint32_t index_offset, uint32_t index_count, uint32_t box_base,
-                         float bbox[6]);
+  void build_chunk_boxes(uint32_t first_view, uint32_t last_view);
   void* plane_ptr(uint32_t plane, size_t* elem) const;
   gbr_status sync_and_check();
   gbr_status quiesce();

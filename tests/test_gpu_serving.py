@@ -9,7 +9,7 @@
   exact;
 * the serving loop: every request served in a mixed batch is bit-identical
   to the same request rendered alone and to the oracle, with and without
-  eviction under a small device budget.
+  eviction under a small device budget, and after the launch shape is tuned.
 """
 import numpy as np
 import pytest
@@ -218,6 +218,33 @@ def test_serving_mix_matches_alone_and_oracle(pkg, mods):
         _check(q, _alone(pkg, procedural, cat.asset(q.scene), q))
     for q in reqs[:3]:
         _check(q, _oracle(procedural, cat.asset(q.scene), q))
+    srv.close()
+
+
+def test_serving_tune_then_mix_matches_alone(pkg, mods):
+    """The launch shape chosen by closed-loop throughput is one of the
+    autotuner's candidates, and requests served with it (plane sets
+    alternating, copy-back on the second stream) are bit-identical to the
+    same requests rendered alone."""
+    procedural, server = mods
+    from habitat_sim_gb300 import autotune
+    cat = server.SceneCatalog(4, seed=17, tri_range=(2e3, 1e4), texture_side=32, tris_per_layer=4000,
+                              pool_bytes=1 << 20)
+    srv = server.RenderServer(pkg, cat, slots={64: 4, 128: 4, 256: 2}, max_resident=4)
+    warm = server.random_requests(cat, 4, rate=0, seed=6)
+    for s, q in enumerate(warm):
+        q.scene = s
+    srv.serve(warm, realtime=False, keep_images=False)
+    tuning, trials = srv.tune(lambda: server.random_requests(cat, 30, rate=0, seed=7), reps=1)
+    timed = [t for t in trials if "requests_per_s" in t]
+    assert len(timed) >= len(autotune.BATCHED_SPACE) and all(t["requests_per_s"] > 0 for t in timed)
+    shape = {k: tuning[k] for k in ("threads", "region_width", "region_height", "small_area", "ctas_per_sm")}
+    assert shape in [{k: c[k] for k in shape} for c in autotune.BATCHED_SPACE]
+    reqs = server.random_requests(cat, 40, rate=0, seed=8)
+    stats = srv.serve(reqs, realtime=False)
+    assert stats["requests"] == 40 and stats["loads"] == 0
+    for q in reqs[::3]:
+        _check(q, _alone(pkg, procedural, cat.asset(q.scene), q))
     srv.close()
 
 
