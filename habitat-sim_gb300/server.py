@@ -346,10 +346,12 @@ class RenderServer:
     resident scenes; ``budget_bytes`` bounds their device bytes (geometry,
     textures, chunk boxes; default: no limit); ``max_loads_per_step`` bounds
     the scene loads one step may wait for (requests beyond it wait for a
-    later step, so that requests for resident scenes are not held up)."""
+    later step, so that requests for resident scenes are not held up: loads
+    are serial either way, and with one per step a request for a resident
+    scene waits for at most one)."""
 
     def __init__(self, pkg, catalog, slots=None, max_resident=64, budget_bytes=None, graph=True,
-                 device=0, max_loads_per_step=8):
+                 device=0, max_loads_per_step=1):
         import torch
 
         self.torch = torch
