@@ -489,6 +489,15 @@ __device__ __forceinline__ bool setup_sub(const float4* q, const Ctx& c, Setup& 
     st.X[i] = __float2int_rn(__fmul_rn(xw, 256.0f));
     st.Y[i] = __float2int_rn(__fmul_rn(yw, 256.0f));
   }
+  // A box without a pixel centre first: most sub-pixel triangles leave here,
+  // before the area and the fill rule.
+  const int minX = min(st.X[0], min(st.X[1], st.X[2])), maxX = max(st.X[0], max(st.X[1], st.X[2]));
+  const int minY = min(st.Y[0], min(st.Y[1], st.Y[2])), maxY = max(st.Y[0], max(st.Y[1], st.Y[2]));
+  st.x0 = max((minX - 128 + 255) >> 8, c.rx0);
+  st.x1 = min((maxX - 128) >> 8, c.rx0 + c.rw - 1);
+  st.y0 = max((minY - 128 + 255) >> 8, c.ry0);
+  st.y1 = min((maxY - 128) >> 8, c.ry0 + c.rh - 1);
+  if (st.x0 > st.x1 || st.y0 > st.y1) return false;
   const int64_t area = int64_t(st.X[1] - st.X[0]) * int64_t(st.Y[2] - st.Y[0]) -
                        int64_t(st.X[2] - st.X[0]) * int64_t(st.Y[1] - st.Y[0]);
   if (area <= 0) return false;
@@ -499,14 +508,7 @@ __device__ __forceinline__ bool setup_sub(const float4* q, const Ctx& c, Setup& 
     const int dx = st.X[b] - st.X[a], dy = st.Y[b] - st.Y[a];
     if (dy < 0 || (dy == 0 && dx < 0)) bias |= 1u << i;
   }
-  const int minX = min(st.X[0], min(st.X[1], st.X[2])), maxX = max(st.X[0], max(st.X[1], st.X[2]));
-  const int minY = min(st.Y[0], min(st.Y[1], st.Y[2])), maxY = max(st.Y[0], max(st.Y[1], st.Y[2]));
   st.bias = bias;
-  st.x0 = max((minX - 128 + 255) >> 8, c.rx0);
-  st.x1 = min((maxX - 128) >> 8, c.rx0 + c.rw - 1);
-  st.y0 = max((minY - 128 + 255) >> 8, c.ry0);
-  st.y1 = min((maxY - 128) >> 8, c.ry0 + c.rh - 1);
-  if (st.x0 > st.x1 || st.y0 > st.y1) return false;
   st.inva = __frcp_rn(__ll2float_rn(area));
   st.zmin = fminf(zw[0], fminf(zw[1], zw[2]));
   st.zw0 = zw[0];
