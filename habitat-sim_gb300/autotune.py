@@ -23,7 +23,7 @@ DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "gbr_autotune.js
 # region), CTAs per SM, the region (screen tile) one CTA owns -- from 128 x 128
 # down to 32 x 32 -- and the small-triangle threshold.
 BATCHED_SPACE = ([dict(threads=1024, region_width=rw, region_height=rh, small_area=sa, ctas_per_sm=1)
-                  for (rw, rh) in ((128, 128), (128, 64)) for sa in (1, 4)] +
+                  for (rw, rh) in ((128, 128), (128, 64), (64, 64)) for sa in (1, 4)] +
                  [dict(threads=512, region_width=rw, region_height=rh, small_area=sa, ctas_per_sm=2)
                   for (rw, rh) in ((128, 64), (64, 64)) for sa in (1, 4)] +
                  [dict(threads=256, region_width=rw, region_height=rh, small_area=sa, ctas_per_sm=4)
