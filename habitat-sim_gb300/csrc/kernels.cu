@@ -1234,14 +1234,15 @@ __global__ void __launch_bounds__(T, 1024 / T) raster_kernel(const RasterParams 
   uint32_t* coarse = reinterpret_cast<uint32_t*>(smem + L.coarse);
   __shared__ uint32_t s_item, s_qcount, s_total, s_rd, s_wr, s_crd, s_cwr, s_next;
   __shared__ uint32_t s_warp[T / 32];
+  const uint32_t item_count = p.item_count_dev ? min(p.item_count, *p.item_count_dev) : p.item_count;
 
   for (uint32_t iter = 0;; ++iter) {
     __syncthreads();
     if (threadIdx.x == 0)
-      s_item = p.persistent ? atomicAdd(p.counter, 1u) : (iter == 0 ? blockIdx.x : p.item_count);
+      s_item = p.persistent ? atomicAdd(p.counter, 1u) : (iter == 0 ? blockIdx.x : item_count);
     __syncthreads();
     const uint32_t item = s_item;
-    if (item >= p.item_count) return;
+    if (item >= item_count) return;
     const WorkItem wi = p.items[p.item_base + item];
     const uint32_t vis_base = p.cameras[wi.scene].vis_base;
     if (!p.cameras[wi.scene].enabled) continue;  // disabled scene: pixels untouched

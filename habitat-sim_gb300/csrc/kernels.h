@@ -67,6 +67,10 @@ struct RasterParams {
   const WorkItem* items;
   uint32_t item_base;
   uint32_t item_count;
+  // Persistent form: the items in use this launch (at most item_count), read
+  // from device memory so that a captured graph follows a list that changes
+  // from step to step; null: item_count.
+  const uint32_t* item_count_dev;
   uint32_t* counter;  // persistent mode: next item
   int32_t persistent;
   Planes out;

@@ -1093,7 +1093,7 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
   // uses small regions so that one scene spreads over several CTAs; the
   // batched form uses large ones (fewer redundant triangle setups), ordered
   // longest-processing-time first for the persistent grid by order_items().
-  std::vector<WorkItem> items, batched;
+  std::vector<WorkItem> items;
   scene_item_base_.assign(S, 0);
   scene_item_count_.assign(S, 0);
   auto tile = [&](uint32_t s, int rwm, int rhm, std::vector<WorkItem>& out) {
@@ -1109,15 +1109,18 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
         out.push_back(it);
       }
   };
+  uint64_t capacity = 0;
   for (uint32_t s = 0; s < S; ++s) {
     scene_item_base_[s] = uint32_t(items.size());
     tile(s, tuning_.plain_region_width, tuning_.plain_region_height, items);
     scene_item_count_[s] = uint32_t(items.size()) - scene_item_base_[s];
-    tile(s, tuning_.region_width, tuning_.region_height, batched);
+    int rw, rh;
+    split_region(s, kMaxSplits, rw, rh);
+    capacity += uint64_t((scenes_[s].width + rw - 1) / rw) * uint64_t((scenes_[s].height + rh - 1) / rh);
   }
+  if (capacity > 0xffffffffull) return fail(GBR_ERROR_INVALID_ARGUMENT, "draw: too many work items");
   item_count_ = uint32_t(items.size());
-  lpt_count_ = uint32_t(batched.size());
-  batched_items_ = std::move(batched);
+  lpt_count_ = uint32_t(capacity);
 
   cudaSetDevice(device_);
   if (gbr_status st = upload_tables()) return st;
@@ -1134,10 +1137,10 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
       !d_vis_clusters_.reserve(S1 * 4, false) ||
       !d_status_.reserve(4, false) || !d_counter_.reserve(4, false) ||
       !d_items_.reserve(std::max<size_t>(items.size(), 1) * sizeof(WorkItem), false) ||
-      !d_items_lpt_.reserve(std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem), false) ||
+      !d_items_lpt_.reserve((size_t(lpt_count_) + 1) * sizeof(WorkItem), false) ||
       !h_stage_[0].reserve(std::max<size_t>(camera_block_bytes(), 1) +
                            std::max<size_t>(nodes, 1) * 64 +
-                           std::max<size_t>(lpt_count_, 1) * sizeof(WorkItem)) ||
+                           (size_t(lpt_count_) + 1) * sizeof(WorkItem)) ||
       !h_stage_[1].reserve(h_stage_[0].bytes))
     return fail(GBR_ERROR_OUT_OF_MEMORY, "draw: out of memory for scene data");
   GBR_CUDA(cudaMemcpy(d_scenes_.ptr, recs.data(), S * sizeof(SceneRec), cudaMemcpyHostToDevice),
@@ -1260,7 +1263,10 @@ gbr_status Renderer::upload_step(cudaStream_t stream) {
   if (items_staged_) {
     WorkItem* istage = reinterpret_cast<WorkItem*>(stage + camera_block_bytes() +
                                                    size_t(total_nodes_) * 64);
-    GBR_CUDA(cudaMemcpyAsync(d_items_lpt_.ptr, istage, size_t(lpt_count_) * sizeof(WorkItem),
+    if (lpt_items_)
+      GBR_CUDA(cudaMemcpyAsync(d_items_lpt_.ptr, istage, size_t(lpt_items_) * sizeof(WorkItem),
+                               cudaMemcpyHostToDevice, stream), "work item upload");
+    GBR_CUDA(cudaMemcpyAsync(d_items_lpt_.as<WorkItem>() + lpt_count_, istage + lpt_count_, 4,
                              cudaMemcpyHostToDevice, stream), "work item upload");
     items_staged_ = false;
   }
@@ -1290,12 +1296,31 @@ gbr_status Renderer::upload_step(cudaStream_t stream) {
   return GBR_OK;
 }
 
-// Longest-processing-time order of the batched form's regions for the
-// persistent grid: a region's cost is its share of the source scene's
-// triangles plus a per-region setup term; disabled scenes go last.  Staged
-// for upload_step().
+// Region of scene s's work items after `level` splits of the batched form's
+// region (clamped to the viewport): each split halves the longer side, down
+// to 32 pixels.
+void Renderer::split_region(uint32_t s, int level, int& rw, int& rh) const {
+  rw = std::max(1, std::min<int>(tuning_.region_width, scenes_[s].width));
+  rh = std::max(1, std::min<int>(tuning_.region_height, scenes_[s].height));
+  for (int l = 0; l < level; ++l) {
+    if (rw >= rh && rw > 32)
+      rw = (rw + 1) / 2;
+    else if (rh > 32)
+      rh = (rh + 1) / 2;
+    else if (rw > 32)
+      rw = (rw + 1) / 2;
+  }
+}
+
+// The batched form's work items of the enabled scenes, in longest-processing-
+// time order for the persistent grid: a region's cost is its share of the
+// source scene's triangles plus a per-region setup term.  A scene whose
+// regions would each cost more than a CTA's share of the whole step (a small
+// viewport bound to a large scene) gets smaller regions (at most kMaxSplits
+// halvings), so that no single item outlasts the others.  Staged for
+// upload_step() with their count.
 void Renderer::order_items() {
-  const size_t n = batched_items_.size();
+  const uint32_t S = uint32_t(scenes_.size());
   // Geometry of each scene: the mesh of its largest draw.  Items of equal
   // cost are grouped by it, so that the CTAs in flight at any time read the
   // same vertices and indices and share them in L2 (scenes that draw the
@@ -1309,29 +1334,65 @@ void Renderer::order_items() {
         geom[s] = d.mesh;
       }
   }
-  std::vector<uint64_t> cost(n);
-  std::vector<uint32_t> key(n);
-  std::vector<uint8_t> on(n);
-  for (size_t k = 0; k < n; ++k) {
-    const WorkItem& it = batched_items_[k];
-    const SceneState& sc = scenes_[it.scene];
-    const uint64_t tris = scenes_[sc.source].tris;
-    on[k] = sc.enabled;
-    cost[k] = (tris + 1) * uint64_t(it.w) * it.h / (uint64_t(sc.width) * sc.height) + tris / 4;
-    key[k] = geom[sc.source];
+  auto item_cost = [](uint64_t tris, int w, int h, int W, int H) {
+    return (tris + 1) * uint64_t(w) * uint64_t(h) / (uint64_t(W) * uint64_t(H)) + tris / 4;
+  };
+  // A CTA's share of the step with every scene at the batched form's region.
+  uint64_t total = 0;
+  for (uint32_t s = 0; s < S; ++s) {
+    const SceneState& sc = scenes_[s];
+    if (!sc.enabled || sc.width <= 0 || sc.height <= 0) continue;
+    int rw, rh;
+    split_region(s, 0, rw, rh);
+    const uint64_t n = uint64_t((sc.width + rw - 1) / rw) * uint64_t((sc.height + rh - 1) / rh);
+    total += n * item_cost(scenes_[sc.source].tris, rw, rh, sc.width, sc.height);
   }
+  const uint64_t grid = std::max<uint64_t>(1, uint64_t(sm_count_) * uint64_t(ctas_per_sm_));
+  const uint64_t share = total / grid;
+  std::vector<WorkItem> items;
+  std::vector<uint64_t> cost;
+  std::vector<uint32_t> key;
+  for (uint32_t s = 0; s < S; ++s) {
+    const SceneState& sc = scenes_[s];
+    if (!sc.enabled || sc.width <= 0 || sc.height <= 0) continue;
+    const uint64_t tris = scenes_[sc.source].tris;
+    int rw, rh, level = 0;
+    split_region(s, 0, rw, rh);
+    while (level < kMaxSplits && item_cost(tris, rw, rh, sc.width, sc.height) > share) {
+      int nw, nh;
+      split_region(s, level + 1, nw, nh);
+      if (nw == rw && nh == rh) break;
+      rw = nw;
+      rh = nh;
+      ++level;
+    }
+    for (int y = 0; y < sc.height; y += rh)
+      for (int x = 0; x < sc.width; x += rw) {
+        WorkItem it{};
+        it.scene = s;
+        it.x0 = uint16_t(x);
+        it.y0 = uint16_t(y);
+        it.w = uint16_t(std::min(rw, sc.width - x));
+        it.h = uint16_t(std::min(rh, sc.height - y));
+        items.push_back(it);
+        cost.push_back(item_cost(tris, it.w, it.h, sc.width, sc.height));
+        key.push_back(geom[sc.source]);
+      }
+  }
+  const size_t n = items.size();
   std::vector<uint32_t> perm(n);
   std::iota(perm.begin(), perm.end(), 0u);
   std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
-    if (on[a] != on[b]) return on[a] > on[b];
     if (cost[a] != cost[b]) return cost[a] > cost[b];
     return key[a] < key[b];
   });
   WorkItem* istage = reinterpret_cast<WorkItem*>(static_cast<char*>(h_stage_[slot_].ptr) +
                                                  camera_block_bytes() +
                                                  size_t(total_nodes_) * 64);
-  for (size_t i = 0; i < n; ++i) istage[i] = batched_items_[perm[i]];
-  items_staged_ = n != 0;
+  for (size_t i = 0; i < n; ++i) istage[i] = items[perm[i]];
+  lpt_items_ = uint32_t(n);
+  std::memcpy(istage + lpt_count_, &lpt_items_, 4);
+  items_staged_ = true;
 }
 
 gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
@@ -1405,6 +1466,7 @@ gbr_status Renderer::enqueue_step(cudaStream_t stream, uint32_t mode) {
     rp.items = d_items_lpt_.as<WorkItem>();
     rp.item_base = 0;
     rp.item_count = lpt_count_;
+    rp.item_count_dev = reinterpret_cast<const uint32_t*>(d_items_lpt_.as<WorkItem>() + lpt_count_);
     rp.persistent = 1;
     rp.region_px = tuning_.region_width * tuning_.region_height;
     const uint32_t grid =

@@ -182,6 +182,8 @@ class Renderer {
   size_t camera_block_bytes() const;  // cameras then light sources, per step
   bool texture_removed(uint32_t t) const { return t < texture_live_.size() && !texture_live_[t]; }
   void order_items();
+  static constexpr int kMaxSplits = 2;  // region halvings of a costly scene's work items
+  void split_region(uint32_t scene, int level, int& rw, int& rh) const;
 
   gbr_config cfg_{};
   std::vector<int32_t> viewports_;
@@ -245,8 +247,9 @@ class Renderer {
   uint32_t total_nodes_ = 0, total_draws_ = 0;
   uint64_t total_tris_ = 0;
   std::vector<uint32_t> scene_item_base_, scene_item_count_;
-  uint32_t item_count_ = 0, lpt_count_ = 0;
-  std::vector<WorkItem> batched_items_;  // regions of the batched form, scene order
+  uint32_t item_count_ = 0;
+  uint32_t lpt_count_ = 0;  // batched form: capacity of the item list (every scene at its finest split)
+  uint32_t lpt_items_ = 0;  // batched form: items in the current list
   bool bindings_dirty_ = true;           // sources or enabled flags changed
   bool items_staged_ = false;            // a new item order waits in the staging buffer
   uint64_t vis_needed_ = 0;              // visible records the current bindings need
