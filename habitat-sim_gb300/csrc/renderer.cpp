@@ -1315,10 +1315,11 @@ void Renderer::split_region(uint32_t s, int level, int& rw, int& rh) const {
 // The batched form's work items of the enabled scenes, in longest-processing-
 // time order for the persistent grid: a region's cost is its share of the
 // source scene's triangles plus a per-region setup term.  A scene whose
-// regions would each cost more than a CTA's share of the whole step (a small
-// viewport bound to a large scene) gets smaller regions (at most kMaxSplits
-// halvings), so that no single item outlasts the others.  Staged for
-// upload_step() with their count.
+// regions would each cost more than half a CTA's share of the whole step (a
+// small viewport bound to a large scene) gets smaller regions (at most
+// kMaxSplits halvings), so that no single item outlasts the others (measured
+// on the serving workload: half the share beat the whole share by 9 % and a
+// quarter of it by 16 %).  Staged for upload_step() with their count.
 void Renderer::order_items() {
   const uint32_t S = uint32_t(scenes_.size());
   // Geometry of each scene: the mesh of its largest draw.  Items of equal
@@ -1337,7 +1338,7 @@ void Renderer::order_items() {
   auto item_cost = [](uint64_t tris, int w, int h, int W, int H) {
     return (tris + 1) * uint64_t(w) * uint64_t(h) / (uint64_t(W) * uint64_t(H)) + tris / 4;
   };
-  // A CTA's share of the step with every scene at the batched form's region.
+  // Half a CTA's share of the step with every scene at the batched form's region.
   uint64_t total = 0;
   for (uint32_t s = 0; s < S; ++s) {
     const SceneState& sc = scenes_[s];
@@ -1348,7 +1349,7 @@ void Renderer::order_items() {
     total += n * item_cost(scenes_[sc.source].tris, rw, rh, sc.width, sc.height);
   }
   const uint64_t grid = std::max<uint64_t>(1, uint64_t(sm_count_) * uint64_t(ctas_per_sm_));
-  const uint64_t share = total / grid;
+  const uint64_t share = total / grid / 2;
   std::vector<WorkItem> items;
   std::vector<uint64_t> cost;
   std::vector<uint32_t> key;
