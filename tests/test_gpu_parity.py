@@ -160,6 +160,51 @@ def test_config3_scan_subset(pkg, procedural):
     _parity(pkg, procedural, wl, steps=(0, 1, 7))
 
 
+def test_split_work_items_match_per_scene_and_oracle(pkg, procedural):
+    """A 150k-triangle scene in a 64 x 64 viewport beside 100 scenes of 2k
+    triangles at 128 x 128: the batched form cuts a viewport into smaller
+    regions when a region would outweigh half a CTA's share of the step (the
+    heavy scene's into 32 x 32 regions).  Every scene of the batched draw
+    (graph) equals the per-scene draw, and the heavy scene and a few light
+    ones equal the oracle."""
+    from habitat_sim_gb300 import server
+    from oracle.model import OracleRenderer
+    heavy, light = server.serving_scene(99, 150000), server.serving_scene(7, 2000)
+    viewports = [(64, 64)] + [(128, 128)] * 100
+    cfg = pkg.RendererConfiguration().setViewports(viewports)
+    gpu = pkg.RendererStandalone(cfg, pkg.RendererStandaloneConfiguration().setFlags(
+        pkg.RendererStandaloneFlags.QuietLog))
+    cpu_scenes = [0, 1, 50, 100]
+    cpu = OracleRenderer(viewports=[viewports[s] for s in cpu_scenes])
+    for r in (gpu, cpu):
+        server.add_asset(r, heavy, "heavy")
+        server.add_asset(r, light, "light")
+    gpu.addNodeHierarchy(0, "heavy")
+    for s in range(1, len(viewports)):
+        gpu.addNodeHierarchy(s, "light")
+    cpu.addNodeHierarchy(0, "heavy")
+    for k in range(1, len(cpu_scenes)):
+        cpu.addNodeHierarchy(k, "light")
+    rng = np.random.default_rng(12)
+    n = len(viewports)
+    views = server.pose_views(rng.uniform(-5, 5, n), rng.uniform(0.5, 2.5, n), rng.uniform(-5, 5, n),
+                              rng.uniform(0, 2 * math.pi, n), np.radians(rng.uniform(-30, 30, n)),
+                              np.zeros(n))
+    projs = np.stack([procedural.projection(90.0, w, h) for (w, h) in viewports])
+    gpu.updateCameras(projs, views)
+    cpu.updateCameras(projs[cpu_scenes], views[cpu_scenes])
+    cpu.draw(threads=4)
+    planes = (pkg.Plane.Color, pkg.Plane.Depth, pkg.Plane.LinearDepth, pkg.Plane.Semantic)
+    gpu.draw(mode=1, graph=True)
+    batched = [[gpu.sceneImage(p, s).copy() for p in planes] for s in range(n)]
+    assert_parity([compare_scene(_Subset(gpu, cpu_scenes), cpu, pkg, k) for k in range(len(cpu_scenes))])
+    gpu.draw(mode=0)
+    for s in range(n):
+        for p, a in zip(planes, batched[s]):
+            assert np.array_equal(a.view(np.uint8), gpu.sceneImage(p, s).view(np.uint8)), (s, p)
+    assert (batched[0][3] > 0).any()
+
+
 def test_config2_full_scale_sample(pkg, procedural):
     """The full uneven-batching workload (4096 envs, 64 scenes of 20k-2M
     triangles, mixed 64/128/256 px, hfov U(60, 110)): 16 envs spanning the
