@@ -1118,6 +1118,7 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
     split_region(s, kMaxSplits, rw, rh);
     capacity += uint64_t((scenes_[s].width + rw - 1) / rw) * uint64_t((scenes_[s].height + rh - 1) / rh);
   }
+  capacity += uint64_t(sm_count_) * 8;  // the last wave's halves (at most one per resident CTA, 8 per SM)
   if (capacity > 0xffffffffull) return fail(GBR_ERROR_INVALID_ARGUMENT, "draw: too many work items");
   item_count_ = uint32_t(items.size());
   lpt_count_ = uint32_t(capacity);
@@ -1380,13 +1381,44 @@ void Renderer::order_items() {
         key.push_back(geom[sc.source]);
       }
   }
-  const size_t n = items.size();
-  std::vector<uint32_t> perm(n);
+  std::vector<uint32_t> perm(items.size());
   std::iota(perm.begin(), perm.end(), 0u);
-  std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
+  auto by_cost = [&](uint32_t a, uint32_t b) {
     if (cost[a] != cost[b]) return cost[a] > cost[b];
     return key[a] < key[b];
-  });
+  };
+  std::stable_sort(perm.begin(), perm.end(), by_cost);
+  // The last wave: the cheapest `grid` items are halved (longer side, not
+  // below 32 px), so that the CTAs finishing the step wait for half an item
+  // at most instead of a whole one.
+  if (items.size() > grid) {
+    const size_t n0 = items.size();
+    for (size_t i = n0 - grid; i < n0; ++i) {
+      WorkItem& it = items[perm[i]];
+      const SceneState& sc = scenes_[it.scene];
+      WorkItem b = it;
+      if (it.w >= it.h && it.w > 32) {
+        b.w = uint16_t(it.w / 2);
+        b.x0 = uint16_t(it.x0 + (it.w - b.w));
+        it.w = uint16_t(it.w - b.w);
+      } else if (it.h > 32) {
+        b.h = uint16_t(it.h / 2);
+        b.y0 = uint16_t(it.y0 + (it.h - b.h));
+        it.h = uint16_t(it.h - b.h);
+      } else {
+        continue;
+      }
+      const uint64_t tris = scenes_[sc.source].tris;
+      cost[perm[i]] = item_cost(tris, it.w, it.h, sc.width, sc.height);
+      items.push_back(b);
+      cost.push_back(item_cost(tris, b.w, b.h, sc.width, sc.height));
+      key.push_back(key[perm[i]]);
+    }
+    perm.resize(items.size());
+    std::iota(perm.begin(), perm.end(), 0u);
+    std::stable_sort(perm.begin(), perm.end(), by_cost);
+  }
+  const size_t n = items.size();
   WorkItem* istage = reinterpret_cast<WorkItem*>(static_cast<char*>(h_stage_[slot_].ptr) +
                                                  camera_block_bytes() +
                                                  size_t(total_nodes_) * 64);
