@@ -717,7 +717,7 @@ def run_reference_impl(args):
 # stated 100-step camera walk.  The end-to-end windows run for a few hundred
 # milliseconds, so that the final readback (which nothing overlaps) and a
 # rare host stall of a few milliseconds do not dominate them.
-SUB_CONFIGS = {"config0": (20, 3, 3, 40, 16), "config2": (10, 3, 1, 30, 16), "config3": (100, 3, 1, 30, 8)}
+SUB_CONFIGS = {"config0": (20, 3, 3, 40, 16), "config2": (10, 3, 1, 60, 16), "config3": (100, 3, 1, 60, 8)}
 
 
 def main():
