@@ -14,7 +14,8 @@
 //   per step   VisibleRec[] (128 B, written by the prepare kernel) and its
 //              processing order uint2[] (8 B per visible draw); ModelRec[]
 //              (96 B per visible draw, lit renderers only),
-//              vis_count[s], vis_tris[s], vis_chunks[s]; WorkItem[] + one counter
+//              vis_count[s], vis_tris[s], vis_chunks[s]; WorkItem[] (capacity for
+//              every scene at its finest split) + the count in use + one counter
 //   views      ChunkBox[] (32 B per 32 triangles of every mesh view, then
 //              32 B per 1024 triangles: the cluster boxes)
 //   output     colour u32, window depth f32, linear depth f32, id u32
