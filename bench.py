@@ -63,7 +63,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--plain-steps", type=int, default=3)
-    p.add_argument("--e2e-steps", type=int, default=20)
+    p.add_argument("--e2e-steps", type=int, default=60)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--envs", type=int, default=None)
