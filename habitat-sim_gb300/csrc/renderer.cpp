@@ -1409,10 +1409,12 @@ void Renderer::order_items() {
         continue;
       }
       const uint64_t tris = scenes_[sc.source].tris;
-      cost[perm[i]] = item_cost(tris, it.w, it.h, sc.width, sc.height);
-      items.push_back(b);
-      cost.push_back(item_cost(tris, b.w, b.h, sc.width, sc.height));
-      key.push_back(key[perm[i]]);
+      const uint32_t geometry = key[perm[i]];
+      const int W = sc.width, H = sc.height;
+      cost[perm[i]] = item_cost(tris, it.w, it.h, W, H);
+      items.push_back(b);  // `it` and `sc` are not used past this point
+      cost.push_back(item_cost(tris, b.w, b.h, W, H));
+      key.push_back(geometry);
     }
     perm.resize(items.size());
     std::iota(perm.begin(), perm.end(), 0u);
