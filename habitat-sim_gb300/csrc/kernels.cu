@@ -1896,9 +1896,9 @@ extern "C" gbr_status gbr_render_mesh_no_alloc(
     // The device address of the fixed scratch (the host-side name of a
     // __device__ array is not a device address).  It belongs to the current
     // context, which a device reset or a caller's own driver-API context
-    // replaces, so it is looked up again on every call made outside a stream
-    // capture; inside a capture the address of the last call on this device
-    // is used, so some call on the device must come before the first capture.
+    // replaces, so it is looked up again on every call whose stream is not
+    // capturing; the first call on a device must come before any stream
+    // capture.
     cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(st, &capture) != cudaSuccess) {
       cudaGetLastError();

@@ -389,11 +389,11 @@ gbr_status gbr_debug_corrupt_parent(gbr_renderer* r, uint32_t scene, uint64_t no
  * (held by every GPU that loads it until the process exits); each call
  * rewrites what must start fresh.  All calls share that array, so calls that
  * may overlap on the GPU (different streams without ordering) race: order
- * them on one stream.  Each call made outside a stream capture looks up the
- * array's device address in the current context (cudaGetSymbolAddress); a
- * call inside a capture reuses the address of the last call on that device,
- * so make a first call before any capture, and again after a device reset.
- * Asynchronous on `stream`. */
+ * them on one stream.  The call looks up the array's device address in the
+ * current context (cudaGetSymbolAddress) whenever its stream is not
+ * capturing; the first call on a device does this set-up, so it should come
+ * before any stream capture, and a first call after a device reset does it
+ * again.  Asynchronous on `stream`. */
 gbr_status gbr_render_mesh_no_alloc(const void* positions, const void* colors,
                                     const uint32_t* indices, uint32_t vertex_count,
                                     uint32_t triangle_count, const float projection[16],
