@@ -428,11 +428,14 @@ def measure(pkg, procedural, name, wl, steps, warmup, plain_steps, e2e_steps, pa
     if os.path.exists(peaks_path):
         peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
     traffic = None
+    issue = None
     tpath = os.path.join(ROOT, "profiles", f"raster_kernel_{name}.txt")
     if os.path.exists(tpath):
         for line in open(tpath):
             if line.startswith("dram_bytes_per_launch:"):
                 traffic = float(line.split(":")[1])
+            elif line.startswith("smsp__issue_active.avg.pct_of_peak_sustained_active"):
+                issue = float(line.split()[1]) / 100.0
     res = {
         "value": value, "unit": "frames/s", "steps": steps, "warmup": warmup,
         "ms_per_step": statistics.mean(step_ms), "p50_ms": float(np.percentile(step_ms, 50)),
@@ -455,6 +458,10 @@ def measure(pkg, procedural, name, wl, steps, warmup, plain_steps, e2e_steps, pa
                        "host time of each step's calls, the last entry readbackWait")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                     "issue_active_frac": issue,
+                     "issue_note": ("the kernel is bound by instruction issue and latency, not HBM: "
+                                    "share of cycles its schedulers issued (ncu capture in profiles/)")
+                     if issue is not None else None,
                      "kernel": "raster_kernel", "bytes_per_launch": launch_bytes,
                      "bytes_breakdown": {"framebuffer": fb_bytes, "geometry_textures": geo_bytes},
                      "avg_launch_ms": raster_avg, "prepare_avg_ms": statistics.mean(prepare_ms),
