@@ -22,7 +22,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["kernels.cu", "noise.cu", "hbao.cu"]
 CPP_SOURCES = ["renderer.cpp", "importer.cpp", "capi.cpp", "replay.cpp", "pool.cpp"]
 HEADERS = ["kernels.h", "records.h", "renderer.h", "importer.h", "json.h", "replay.h", "hbao.h", "mips.h",
-           "trace.h", "pool.h"]
+           "trace.h", "pool.h", "work_items.h"]
 
 
 def _cuda_home():

@@ -22,6 +22,7 @@
 #include "mips.h"
 #include "pool.h"
 #include "trace.h"
+#include "work_items.h"
 
 namespace gbr {
 
@@ -1109,16 +1110,18 @@ gbr_status Renderer::rebuild(cudaStream_t stream) {
         out.push_back(it);
       }
   };
-  uint64_t capacity = 0;
+  std::vector<ItemScene> info(S);
   for (uint32_t s = 0; s < S; ++s) {
     scene_item_base_[s] = uint32_t(items.size());
     tile(s, tuning_.plain_region_width, tuning_.plain_region_height, items);
     scene_item_count_[s] = uint32_t(items.size()) - scene_item_base_[s];
-    int rw, rh;
-    split_region(s, kMaxSplits, rw, rh);
-    capacity += uint64_t((scenes_[s].width + rw - 1) / rw) * uint64_t((scenes_[s].height + rh - 1) / rh);
+    info[s].width = scenes_[s].width;
+    info[s].height = scenes_[s].height;
   }
-  capacity += uint64_t(sm_count_) * 8;  // the last wave's halves (at most one per resident CTA, 8 per SM)
+  // Every scene at its finest split, whichever are enabled, and the last
+  // wave's halves (at most one per resident CTA, 8 per SM).
+  const uint64_t capacity =
+      work_item_capacity(info, tuning_.region_width, tuning_.region_height, uint64_t(sm_count_) * 8);
   if (capacity > 0xffffffffull) return fail(GBR_ERROR_INVALID_ARGUMENT, "draw: too many work items");
   item_count_ = uint32_t(items.size());
   lpt_count_ = uint32_t(capacity);
@@ -1297,135 +1300,35 @@ gbr_status Renderer::upload_step(cudaStream_t stream) {
   return GBR_OK;
 }
 
-// Region of scene s's work items after `level` splits of the batched form's
-// region (clamped to the viewport): each split halves the longer side, down
-// to 32 pixels.
-void Renderer::split_region(uint32_t s, int level, int& rw, int& rh) const {
-  rw = std::max(1, std::min<int>(tuning_.region_width, scenes_[s].width));
-  rh = std::max(1, std::min<int>(tuning_.region_height, scenes_[s].height));
-  for (int l = 0; l < level; ++l) {
-    if (rw >= rh && rw > 32)
-      rw = (rw + 1) / 2;
-    else if (rh > 32)
-      rh = (rh + 1) / 2;
-    else if (rw > 32)
-      rw = (rw + 1) / 2;
-  }
-}
-
-// The batched form's work items of the enabled scenes, in longest-processing-
-// time order for the persistent grid: a region's cost is its share of the
-// source scene's triangles plus a per-region setup term.  A scene whose
-// regions would each cost more than half a CTA's share of the whole step (a
-// small viewport bound to a large scene) gets smaller regions (at most
-// kMaxSplits halvings), so that no single item outlasts the others (measured
-// on the serving workload: half the share beat the whole share by 9 % and a
-// quarter of it by 16 %).  Staged for upload_step() with their count.
+// The batched form's work items of the enabled scenes (build_work_items:
+// longest first, costly regions split, the last wave halved), staged for
+// upload_step() with their count.
 void Renderer::order_items() {
-  const uint32_t S = uint32_t(scenes_.size());
-  // Geometry of each scene: the mesh of its largest draw.  Items of equal
-  // cost are grouped by it, so that the CTAs in flight at any time read the
-  // same vertices and indices and share them in L2 (scenes that draw the
-  // same large mesh would otherwise interleave and thrash it).
-  std::vector<uint32_t> geom(scenes_.size(), 0xffffffffu);
+  std::vector<ItemScene> info(scenes_.size());
   for (size_t s = 0; s < scenes_.size(); ++s) {
+    const SceneState& sc = scenes_[s];
+    const SceneState& src = scenes_[sc.source];
+    ItemScene& it = info[s];
+    it.width = sc.width;
+    it.height = sc.height;
+    it.tris = src.tris;
+    it.enabled = sc.enabled;
+    // Geometry of the source: the mesh of its largest draw.
     uint32_t best = 0;
-    for (const HostDraw& d : scenes_[s].draws)
+    it.geometry = 0xffffffffu;
+    for (const HostDraw& d : src.draws)
       if (d.index_count > best) {
         best = d.index_count;
-        geom[s] = d.mesh;
+        it.geometry = d.mesh;
       }
-  }
-  auto item_cost = [](uint64_t tris, int w, int h, int W, int H) {
-    return (tris + 1) * uint64_t(w) * uint64_t(h) / (uint64_t(W) * uint64_t(H)) + tris / 4;
-  };
-  // Half a CTA's share of the step with every scene at the batched form's region.
-  uint64_t total = 0;
-  for (uint32_t s = 0; s < S; ++s) {
-    const SceneState& sc = scenes_[s];
-    if (!sc.enabled || sc.width <= 0 || sc.height <= 0) continue;
-    int rw, rh;
-    split_region(s, 0, rw, rh);
-    const uint64_t n = uint64_t((sc.width + rw - 1) / rw) * uint64_t((sc.height + rh - 1) / rh);
-    total += n * item_cost(scenes_[sc.source].tris, rw, rh, sc.width, sc.height);
   }
   const uint64_t grid = std::max<uint64_t>(1, uint64_t(sm_count_) * uint64_t(ctas_per_sm_));
-  const uint64_t share = total / grid / 2;
-  std::vector<WorkItem> items;
-  std::vector<uint64_t> cost;
-  std::vector<uint32_t> key;
-  for (uint32_t s = 0; s < S; ++s) {
-    const SceneState& sc = scenes_[s];
-    if (!sc.enabled || sc.width <= 0 || sc.height <= 0) continue;
-    const uint64_t tris = scenes_[sc.source].tris;
-    int rw, rh, level = 0;
-    split_region(s, 0, rw, rh);
-    while (level < kMaxSplits && item_cost(tris, rw, rh, sc.width, sc.height) > share) {
-      int nw, nh;
-      split_region(s, level + 1, nw, nh);
-      if (nw == rw && nh == rh) break;
-      rw = nw;
-      rh = nh;
-      ++level;
-    }
-    for (int y = 0; y < sc.height; y += rh)
-      for (int x = 0; x < sc.width; x += rw) {
-        WorkItem it{};
-        it.scene = s;
-        it.x0 = uint16_t(x);
-        it.y0 = uint16_t(y);
-        it.w = uint16_t(std::min(rw, sc.width - x));
-        it.h = uint16_t(std::min(rh, sc.height - y));
-        items.push_back(it);
-        cost.push_back(item_cost(tris, it.w, it.h, sc.width, sc.height));
-        key.push_back(geom[sc.source]);
-      }
-  }
-  std::vector<uint32_t> perm(items.size());
-  std::iota(perm.begin(), perm.end(), 0u);
-  auto by_cost = [&](uint32_t a, uint32_t b) {
-    if (cost[a] != cost[b]) return cost[a] > cost[b];
-    return key[a] < key[b];
-  };
-  std::stable_sort(perm.begin(), perm.end(), by_cost);
-  // The last wave: the cheapest `grid` items are halved (longer side, not
-  // below 32 px), so that the CTAs finishing the step wait for half an item
-  // at most instead of a whole one.
-  if (items.size() > grid) {
-    const size_t n0 = items.size();
-    for (size_t i = n0 - grid; i < n0; ++i) {
-      WorkItem& it = items[perm[i]];
-      const SceneState& sc = scenes_[it.scene];
-      WorkItem b = it;
-      if (it.w >= it.h && it.w > 32) {
-        b.w = uint16_t(it.w / 2);
-        b.x0 = uint16_t(it.x0 + (it.w - b.w));
-        it.w = uint16_t(it.w - b.w);
-      } else if (it.h > 32) {
-        b.h = uint16_t(it.h / 2);
-        b.y0 = uint16_t(it.y0 + (it.h - b.h));
-        it.h = uint16_t(it.h - b.h);
-      } else {
-        continue;
-      }
-      const uint64_t tris = scenes_[sc.source].tris;
-      const uint32_t geometry = key[perm[i]];
-      const int W = sc.width, H = sc.height;
-      cost[perm[i]] = item_cost(tris, it.w, it.h, W, H);
-      items.push_back(b);  // `it` and `sc` are not used past this point
-      cost.push_back(item_cost(tris, b.w, b.h, W, H));
-      key.push_back(geometry);
-    }
-    perm.resize(items.size());
-    std::iota(perm.begin(), perm.end(), 0u);
-    std::stable_sort(perm.begin(), perm.end(), by_cost);
-  }
-  const size_t n = items.size();
+  const std::vector<WorkItem> items = build_work_items(info, tuning_.region_width, tuning_.region_height, grid);
   WorkItem* istage = reinterpret_cast<WorkItem*>(static_cast<char*>(h_stage_[slot_].ptr) +
                                                  camera_block_bytes() +
                                                  size_t(total_nodes_) * 64);
-  for (size_t i = 0; i < n; ++i) istage[i] = items[perm[i]];
-  lpt_items_ = uint32_t(n);
+  std::copy(items.begin(), items.end(), istage);
+  lpt_items_ = uint32_t(items.size());
   std::memcpy(istage + lpt_count_, &lpt_items_, 4);
   items_staged_ = true;
 }

@@ -182,8 +182,6 @@ class Renderer {
   size_t camera_block_bytes() const;  // cameras then light sources, per step
   bool texture_removed(uint32_t t) const { return t < texture_live_.size() && !texture_live_[t]; }
   void order_items();
-  static constexpr int kMaxSplits = 2;  // region halvings of a costly scene's work items
-  void split_region(uint32_t scene, int level, int& rw, int& rh) const;
 
   gbr_config cfg_{};
   std::vector<int32_t> viewports_;

@@ -19,7 +19,7 @@ def _cuda_include():
     pytest.skip("CUDA headers not found")
 
 
-@pytest.mark.parametrize("name", ["worker_pool_test", "json_test", "c_abi_test"])
+@pytest.mark.parametrize("name", ["worker_pool_test", "json_test", "c_abi_test", "work_items_test"])
 def test_native(name, tmp_path):
     if shutil.which("g++") is None or shutil.which("gcc") is None:
         pytest.skip("g++/gcc not available")
