@@ -573,6 +573,18 @@ def test_errors(pkg, procedural):
     assert e.value.status == 1
     with pytest.raises(pkg.GbrError):
         r.addMesh(np.zeros((3, 3)), indices=np.array([0, 1, 3]))
+    # A large index array is checked on the host's worker pool: the first bad
+    # index is reported, and nothing is added.
+    idx = np.tile(np.array([0, 1, 2], np.uint32), 200000)
+    idx[456791] = 3
+    idx[500000] = 7
+    live = r.memoryUsage()[0]
+    with pytest.raises(pkg.GbrError) as e:
+        r.addMesh(np.zeros((3, 3), np.float32), indices=idx)
+    assert e.value.status == 1 and "index 456791 out of range for 3 vertices" in str(e.value)
+    assert r.memoryUsage()[0] == live
+    idx[456791] = idx[500000] = 2
+    assert r.addMesh(np.zeros((3, 3), np.float32), indices=idx) >= 0
     with pytest.raises(pkg.GbrError):
         r.setTuning(threads=100)
 
